@@ -1,0 +1,385 @@
+"""GB300-native TGV-DCT shading correction (sm_103a), drop-in for the reference path.
+
+This package is a thin Python view of the C ABI in ``include/tgvdct.h``
+(``_build/libtgvdct.so``).  It mirrors the reference's operator surface for the
+path — the raw launchers of ``source/modules/tgv_deshade`` and
+``source/modules/cuda_image_operations`` and the ``TGVDeshadeProcessor`` methods
+that call them — with numpy arrays in (depth, height, width) order, x fastest.
+Every compute call goes to the CUDA library; if it is missing, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import numpy as np
+
+from . import phantoms  # noqa: F401  (re-exported for users and benchmarks)
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libtgvdct.so")
+
+# enums of include/tgvdct.h
+OK, ERR_BAD_ARG, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, STOPPED = range(7)
+DATA_L1, DATA_L2 = 0, 1
+GEOMETRY_3D, GEOMETRY_2D = 0, 1
+STATE_FP32, STATE_BF16_DUAL, STATE_FX16_DUAL = 0, 1, 2
+DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
+EIGEN_REFERENCE, EIGEN_ACCURATE = 0, 1
+
+_STATUS_NAMES = {OK: "ok", ERR_BAD_ARG: "bad argument", ERR_OOM: "out of memory",
+                 ERR_CUDA: "CUDA error", ERR_NO_DEVICE: "no suitable CUDA device",
+                 ERR_UNSUPPORTED: "unsupported mode", STOPPED: "stopped by callback"}
+
+
+class TgvdctError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    """tgvdct_params."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("depth", ctypes.c_uint32), ("lambda_", ctypes.c_float),
+                ("alpha0", ctypes.c_float), ("alpha1", ctypes.c_float),
+                ("iteration_count", ctypes.c_uint32), ("tau", ctypes.c_float),
+                ("sigma", ctypes.c_float), ("theta", ctypes.c_float),
+                ("data_term", ctypes.c_int32), ("geometry", ctypes.c_int32),
+                ("state_precision", ctypes.c_int32), ("dct_mode", ctypes.c_int32),
+                ("poisson_eigen", ctypes.c_int32),
+                ("paint_iteration_interval", ctypes.c_uint32),
+                ("callback_on_device", ctypes.c_int32)]
+
+
+CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
+                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                            ctypes.c_void_p)
+
+_lib = None
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+_i32 = ctypes.c_int32
+_flt = ctypes.c_float
+
+# name -> argtypes (restype tgvdct_status unless noted)
+_SIGS = {
+    "tgvdct_params_init": [ctypes.POINTER(Params)],
+    "tgvdct_workspace_bytes": [ctypes.POINTER(Params)],
+    "tgvdct_create": [ctypes.POINTER(Params), ctypes.POINTER(_vp)],
+    "tgvdct_destroy": [_vp],
+    "tgvdct_set_params": [_vp, ctypes.POINTER(Params)],
+    "tgvdct_iterations_run": [_vp],
+    "tgvdct_tgv2_l1_deshade_launch": [_f32p, _u32, _u32, _u32, _flt, _u32, _u32, ctypes.c_int,
+                                      CALLBACK, _vp, _flt, _flt, _f32p, _f32p, _f32p, _f32p],
+    "tgvdct_tgv2_l1_deshade_launch_2d": [_f32p, _u32, _u32, _flt, _u32, _u32, CALLBACK, _vp,
+                                         _flt, _flt, _f32p, _f32p, _f32p],
+    "tgvdct_tgv2_denoise_launch": [_f32p, _u32, _u32, _u32, _i32, _flt, _u32, _flt, _flt, _f32p],
+    "tgvdct_tgv2_run_dev": [_vp, _vp, _vp, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+    "tgvdct_divergence_launch": [_f32p, _f32p, _vp, _u32, _u32, _u32, _f32p],
+    "tgvdct_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
+    "tgvdct_inverse_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
+    "tgvdct_solve_poisson_in_cosine_domain_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
+    "tgvdct_integrate_image_gradients_poisson_cosine_transform": [_f32p, _f32p, _vp, _u32, _u32,
+                                                                  _u32, _i32, _i32, _f32p],
+    "tgvdct_poisson_integrate_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "tgvdct_deshade_epilogue_dev": [_vp, _vp, _vp, ctypes.c_uint64, _i32, _i32, _i32, _vp, _vp],
+    "tgvdct_process_tgv2_l1": [ctypes.POINTER(Params), _f32p, _vp, _i32, _i32, _i32, CALLBACK,
+                               _vp, _f32p, _f32p, _f32p],
+    "tgvdct_process_dev": [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+}
+_RESTYPES = {"tgvdct_params_init": None, "tgvdct_workspace_bytes": ctypes.c_size_t,
+             "tgvdct_iterations_run": ctypes.c_uint32, "tgvdct_version": ctypes.c_char_p,
+             "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p}
+
+# symbols of include/tgvdct.h (checked by the CPU test suite)
+EXPORTED = sorted(set(_SIGS) | {"tgvdct_version", "tgvdct_last_error", "tgvdct_status_string"})
+
+
+def lib() -> ctypes.CDLL:
+    """The CUDA library; raises if it has not been built (there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run "
+                              "`python -m ambient_image_processor_gb300.build` first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        for name in ("tgvdct_version", "tgvdct_last_error"):
+            getattr(L, name).restype = ctypes.c_char_p
+            getattr(L, name).argtypes = []
+        L.tgvdct_status_string.restype = ctypes.c_char_p
+        L.tgvdct_status_string.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def version() -> str:
+    return lib().tgvdct_version().decode()
+
+
+def _check(status: int, allow_stop: bool = True) -> int:
+    if status == OK or (allow_stop and status == STOPPED):
+        return status
+    raise TgvdctError(status, lib().tgvdct_last_error().decode())
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().tgvdct_params_init(ctypes.byref(p))
+    for k, v in kw.items():
+        if k == "lambda":
+            k = "lambda_"
+        if not hasattr(p, k):
+            raise AttributeError(f"tgvdct_params has no field {k}")
+        setattr(p, k, v)
+    return p
+
+
+def _dims(a: np.ndarray):
+    if a.ndim == 2:
+        return a.shape[1], a.shape[0], 1
+    if a.ndim == 3:
+        return a.shape[2], a.shape[1], a.shape[0]
+    raise ValueError("expected a 2-D (H, W) or 3-D (D, H, W) array")
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _make_callback(fn, shape, n_out):
+    """Wraps a Python callable(iteration_index, iteration_count, *images) -> stop?"""
+    if fn is None:
+        return CALLBACK(), None
+    size = int(np.prod(shape))
+
+    def trampoline(it, count, a, b, c, d, _user):
+        arrs = []
+        for ptr in (a, b, c, d)[:n_out]:
+            if ptr:
+                arrs.append(np.ctypeslib.as_array(ptr, shape=(size,)).reshape(shape).copy())
+            else:
+                arrs.append(None)
+        try:
+            return 1 if fn(int(it), int(count), *arrs) else 0
+        except Exception:  # a raising callback stops the loop
+            return 1
+
+    cb = CALLBACK(trampoline)
+    return cb, cb
+
+
+# ---------------------------------------------------------------------------
+# Raw launchers (reference: tgv_deshade/*.cu, tgv_cuda/*.cu, cuda_image_operations/*.cu)
+
+def tgv2_l1_deshade_launch(f, lambda_, iteration_count, paint_iteration_interval=0,
+                           cuda_block_dimension=-1, iteration_finished_callback=None,
+                           alpha0=2.0, alpha1=1.0):
+    """tgv2_l1_deshade_launch<float> (tgv_deshade/tgv2_l1_deshade.cu:33-41).
+
+    Returns (u, v_x, v_y, v_z).  The callback gets (iteration_index,
+    iteration_count, u, v_x, v_y, v_z) and stops the loop by returning True.
+    """
+    f = _f32(f)
+    w, h, d = _dims(f)
+    u, vx, vy, vz = (np.empty_like(f) for _ in range(4))
+    cb, keep = _make_callback(iteration_finished_callback, f.shape, 4)
+    _check(lib().tgvdct_tgv2_l1_deshade_launch(f, w, h, d, lambda_, iteration_count,
+                                               paint_iteration_interval, cuda_block_dimension,
+                                               cb, None, alpha0, alpha1, u, vx, vy, vz))
+    del keep
+    return u, vx, vy, vz
+
+
+def tgv2_l1_deshade_launch_2d(f, lambda_, iteration_count, paint_iteration_interval=0,
+                              iteration_finished_callback=None, alpha0=2.0, alpha1=1.0):
+    """tgv2_l1_deshade_launch_2d<float> (tgv_deshade/tgv2_l1_deshade_2d.cu:29-36)."""
+    f = _f32(f)
+    if f.ndim != 2:
+        raise ValueError("the 2-D launcher takes an (H, W) image")
+    h, w = f.shape
+    u, vx, vy = (np.empty_like(f) for _ in range(3))
+    cb, keep = _make_callback(iteration_finished_callback, f.shape, 3)
+    _check(lib().tgvdct_tgv2_l1_deshade_launch_2d(f, w, h, lambda_, iteration_count,
+                                                  paint_iteration_interval, cb, None, alpha0,
+                                                  alpha1, u, vx, vy))
+    del keep
+    return u, vx, vy
+
+
+def tgv2_denoise_launch(f, lambda_, iteration_count, alpha0=2.0, alpha1=1.0, data_term=DATA_L1):
+    """tgv2_l1_launch / tgv2_l2_launch (tgv_cuda/tgv2_l1.cu:64, tgv_cuda/tgv2_l2.cu:60)."""
+    f = _f32(f)
+    w, h, d = _dims(f)
+    u = np.empty_like(f)
+    _check(lib().tgvdct_tgv2_denoise_launch(f, w, h, d, data_term, lambda_, iteration_count,
+                                            alpha0, alpha1, u), allow_stop=False)
+    return u
+
+
+def divergence_kernel_launch(dx, dy, dz=None):
+    """divergence_kernel_launch (cuda_image_operations/divergence.cu:59-61)."""
+    dx, dy = _f32(dx), _f32(dy)
+    w, h, d = _dims(dx)
+    dzp = None
+    if d > 1:
+        dz = _f32(dz)
+        dzp = dz.ctypes.data_as(_vp)
+    out = np.empty_like(dx)
+    _check(lib().tgvdct_divergence_launch(dx, dy, dzp, w, h, d, out), allow_stop=False)
+    return out
+
+
+def cosine_transform_kernel_launch(x, dct_mode=DCT_FP32):
+    """cosine_transform_kernel_launch (cuda_image_operations/cosine_transform.cu:226-227)."""
+    x = _f32(x)
+    w, h, d = _dims(x)
+    out = np.empty_like(x)
+    _check(lib().tgvdct_cosine_transform_launch(x, w, h, d, dct_mode, out), allow_stop=False)
+    return out
+
+
+def inverse_cosine_transform_kernel_launch(x, dct_mode=DCT_FP32):
+    """inverse_cosine_transform_kernel_launch (inverse_cosine_transform.cu:167-168)."""
+    x = _f32(x)
+    w, h, d = _dims(x)
+    out = np.empty_like(x)
+    _check(lib().tgvdct_inverse_cosine_transform_launch(x, w, h, d, dct_mode, out),
+           allow_stop=False)
+    return out
+
+
+def solve_poisson_in_cosine_domain_kernel_launch(x, poisson_eigen=EIGEN_REFERENCE):
+    """solve_poisson_in_cosine_domain_kernel_launch (solve_poisson_in_cosine_domain.cu:86-87)."""
+    x = _f32(x)
+    w, h, d = _dims(x)
+    out = np.empty_like(x)
+    _check(lib().tgvdct_solve_poisson_in_cosine_domain_launch(x, w, h, d, poisson_eigen, out),
+           allow_stop=False)
+    return out
+
+
+# ---------------------------------------------------------------------------
+class TGVDeshadeProcessor:
+    """Mirror of the reference's TGVDeshadeProcessor static API
+    (tgv_deshade/TGVDeshadeProcessor.h:23-183) over numpy images."""
+
+    @staticmethod
+    def integrate_image_gradients_poisson_cosine_transform(gradient_x, gradient_y,
+                                                           gradient_z=None, dct_mode=DCT_FP32,
+                                                           poisson_eigen=EIGEN_REFERENCE):
+        """TGVDeshadeProcessor.cpp:386-408 (2-D inputs: :410-431)."""
+        gx, gy = _f32(gradient_x), _f32(gradient_y)
+        w, h, d = _dims(gx)
+        gzp = None
+        if d > 1:
+            gz = _f32(gradient_z)
+            gzp = gz.ctypes.data_as(_vp)
+        out = np.empty_like(gx)
+        _check(lib().tgvdct_integrate_image_gradients_poisson_cosine_transform(
+            gx, gy, gzp, w, h, d, dct_mode, poisson_eigen, out), allow_stop=False)
+        return out
+
+    @staticmethod
+    def processTGV2L1GPUCuda(input_image, lambda_, alpha0, alpha1, iteration_count,
+                             cuda_block_dimension=-1, mask_image=None,
+                             set_negative_values_to_zero=True, *, paint_iteration_interval=0,
+                             iteration_finished_callback=None, add_background_back=False,
+                             log_domain=False, data_term=DATA_L1, two_d=False,
+                             state_precision=STATE_FP32, dct_mode=DCT_FP32,
+                             poisson_eigen=EIGEN_REFERENCE, tau=None, sigma=None):
+        """TGVDeshadeProcessor::processTGV2L1GPUCuda (TGVDeshadeProcessor.cpp:122-166; the
+        GUI overload with mask, callback and add-back: :285-314).
+
+        Returns (denoised_image, shading_image, deshaded_image).  The callback gets
+        (iteration_index, iteration_count, u, l, r) — the reference's
+        IterationFinishedThreeImages (TGVDeshadeProcessor.h:34-36).
+        """
+        f = _f32(input_image)
+        w, h, d = _dims(f)
+        p = default_params(width=w, height=h, depth=d, lambda_=lambda_, alpha0=alpha0,
+                           alpha1=alpha1, iteration_count=iteration_count,
+                           data_term=data_term,
+                           geometry=GEOMETRY_2D if two_d else GEOMETRY_3D,
+                           state_precision=state_precision, dct_mode=dct_mode,
+                           poisson_eigen=poisson_eigen,
+                           paint_iteration_interval=paint_iteration_interval)
+        if tau is not None:
+            p.tau = tau
+        if sigma is not None:
+            p.sigma = sigma
+        mptr, mask = None, None
+        if mask_image is not None:
+            mask = _f32(mask_image)
+            mptr = mask.ctypes.data_as(_vp)
+        u, l, r = (np.empty_like(f) for _ in range(3))
+        cb, keep = _make_callback(iteration_finished_callback, f.shape, 3)
+        _check(lib().tgvdct_process_tgv2_l1(ctypes.byref(p), f, mptr,
+                                            int(set_negative_values_to_zero),
+                                            int(add_background_back), int(log_domain), cb, None,
+                                            u, l, r))
+        del keep
+        return u, l, r
+
+
+# ---------------------------------------------------------------------------
+class Context:
+    """A device workspace for one volume shape (tgvdct_context).
+
+    Device buffers are passed as raw pointers (ints), e.g. ``tensor.data_ptr()``,
+    and streams as raw handles (``torch.cuda.Stream.cuda_stream``) or None.
+    """
+
+    def __init__(self, params: Params):
+        self.params = params
+        self._ctx = _vp()
+        _check(lib().tgvdct_create(ctypes.byref(params), ctypes.byref(self._ctx)),
+               allow_stop=False)
+
+    def close(self):
+        if self._ctx:
+            lib().tgvdct_destroy(self._ctx)
+            self._ctx = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def iterations_run(self) -> int:
+        return int(lib().tgvdct_iterations_run(self._ctx))
+
+    def set_params(self, params: Params):
+        _check(lib().tgvdct_set_params(self._ctx, ctypes.byref(params)), allow_stop=False)
+        self.params = params
+
+    def run_dev(self, f_ptr, u_ptr, vx_ptr, vy_ptr, vz_ptr=None, stream=None,
+                callback=None) -> int:
+        return _check(lib().tgvdct_tgv2_run_dev(self._ctx, f_ptr, u_ptr, vx_ptr, vy_ptr, vz_ptr,
+                                                callback or CALLBACK(), None, stream))
+
+    def poisson_integrate_dev(self, vx_ptr, vy_ptr, vz_ptr, l_ptr, stream=None):
+        _check(lib().tgvdct_poisson_integrate_dev(self._ctx, vx_ptr, vy_ptr, vz_ptr, l_ptr,
+                                                  stream), allow_stop=False)
+
+    def process_dev(self, f_ptr, u_ptr, l_ptr, r_ptr, mask_ptr=None,
+                    set_negative_values_to_zero=True, add_background_back=False,
+                    log_domain=False, stream=None, callback=None) -> int:
+        return _check(lib().tgvdct_process_dev(self._ctx, f_ptr, mask_ptr,
+                                               int(set_negative_values_to_zero),
+                                               int(add_background_back), int(log_domain), u_ptr,
+                                               l_ptr, r_ptr, callback or CALLBACK(), None,
+                                               stream))

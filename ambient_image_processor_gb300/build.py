@@ -1,0 +1,81 @@
+"""Builds libtgvdct.so (the C-ABI library) and the terminal programs for sm_103a.
+
+Every CUDA translation unit is compiled by nvcc for ``sm_103a`` only, in
+parallel, then linked into ``ambient_image_processor_gb300/_build/libtgvdct.so``.
+No cmake, no torch extension machinery: the library exposes plain ``extern "C"``
+symbols declared in ``include/tgvdct.h``.
+
+    python -m ambient_image_processor_gb300.build
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+OUT = os.path.join(PKG, "_build")
+LIB = os.path.join(OUT, "libtgvdct.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
+               "--expt-relaxed-constexpr"]
+
+# translation unit -> extra flags
+UNITS = {
+    # -fmad=false keeps the reference's rounding sequence: only the explicit
+    # __fmaf_rn calls (the reference's fmaf) fuse.
+    "tgv_kernels.cu": ["-fmad=false"],
+    "dct_kernels.cu": [],
+    "capi.cu": [],
+}
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout[-4000:]
+                           + r.stderr[-8000:])
+    return r
+
+
+def _stale(target: str, deps) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False, jobs: int = 8) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(INCLUDE, "tgvdct.h"))
+    objs, cmds = [], []
+    for unit, extra in UNITS.items():
+        src = os.path.join(CSRC, unit)
+        obj = os.path.join(OUT, unit + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src, *headers, __file__]):
+            cmds.append([nvcc(), *ARCH, *NVCC_COMMON, *extra, "-c", src, "-o", obj])
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        for r in ex.map(_run, cmds):
+            if verbose and r.stderr:
+                print(r.stderr)
+    if force or cmds or _stale(LIB, objs):
+        _run([nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

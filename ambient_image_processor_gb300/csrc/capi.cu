@@ -1,0 +1,605 @@
+// C ABI of the TGV-DCT path (include/tgvdct.h): contexts, status codes, the
+// iteration loop with its callback, and the host-buffer drop-in launchers.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tgvdct {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace tgvdct
+
+using namespace tgvdct;
+
+struct tgvdct_context {
+    tgvdct_params prm;
+    TgvState st;
+    void* state_block = nullptr;
+    DctPlan* plan = nullptr;
+    uint32_t iterations_run = 0;
+    // pinned host buffers for callbacks that receive host copies
+    float* host_cb = nullptr;
+    size_t host_cb_count = 0;
+    // device scratch for the per-callback deshade of tgvdct_process_dev
+    float* cb_dev = nullptr;
+};
+
+namespace {
+
+size_t voxels(const tgvdct_params& p) { return (size_t)p.width * p.height * p.depth; }
+
+void validate(const tgvdct_params* p) {
+    TGV_REQUIRE(p != nullptr, "null parameter block");
+    TGV_REQUIRE(p->width >= 1 && p->height >= 1 && p->depth >= 1, "width, height, depth must be >= 1");
+    TGV_REQUIRE(p->depth <= 65535, "depth must be <= 65535");
+    TGV_REQUIRE((uint64_t)p->width * p->height * p->depth <= (uint64_t)1 << 34,
+                "volume larger than 2^34 voxels");
+    TGV_REQUIRE(p->geometry == TGVDCT_GEOMETRY_3D || p->geometry == TGVDCT_GEOMETRY_2D,
+                "unknown geometry");
+    TGV_REQUIRE(p->geometry == TGVDCT_GEOMETRY_3D || p->depth == 1,
+                "2-D geometry requires depth == 1");
+    TGV_REQUIRE(p->data_term == TGVDCT_DATA_L1 || p->data_term == TGVDCT_DATA_L2,
+                "unknown data term");
+    TGV_REQUIRE(p->state_precision >= TGVDCT_STATE_FP32 &&
+                    p->state_precision <= TGVDCT_STATE_FX16_DUAL,
+                "unknown state precision");
+    TGV_REQUIRE(p->dct_mode >= TGVDCT_DCT_FP32 && p->dct_mode <= TGVDCT_DCT_BF16X3,
+                "unknown DCT mode");
+    TGV_REQUIRE(p->poisson_eigen == TGVDCT_EIGEN_REFERENCE ||
+                    p->poisson_eigen == TGVDCT_EIGEN_ACCURATE,
+                "unknown Poisson eigenvalue mode");
+    TGV_REQUIRE(std::isfinite(p->alpha0) && p->alpha0 > 0.f, "alpha0 must be > 0");
+    TGV_REQUIRE(std::isfinite(p->alpha1) && p->alpha1 > 0.f, "alpha1 must be > 0");
+    TGV_REQUIRE(std::isfinite(p->lambda) && p->lambda >= 0.f, "lambda must be >= 0");
+    TGV_REQUIRE(std::isfinite(p->tau) && p->tau > 0.f, "tau must be > 0");
+    TGV_REQUIRE(std::isfinite(p->sigma) && p->sigma > 0.f, "sigma must be > 0");
+    TGV_REQUIRE(std::isfinite(p->theta), "theta must be finite");
+}
+
+void check_device() {
+    int dev = 0, n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error("no CUDA device available");
+        throw Error{TGVDCT_ERR_NO_DEVICE};
+    }
+    TGV_CUDA(cudaGetDevice(&dev));
+    int major = 0, minor = 0;
+    TGV_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    TGV_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3) {
+        set_error("this library is built for sm_103a (GB300); device is sm_" +
+                  std::to_string(major) + std::to_string(minor));
+        throw Error{TGVDCT_ERR_NO_DEVICE};
+    }
+}
+
+TgvStep step_of(const tgvdct_params& p) {
+    TgvStep k;
+    k.tau = p.tau;
+    k.sigma = p.sigma;
+    k.theta = p.theta;
+    k.lambda = p.lambda;
+    k.alpha0 = p.alpha0;
+    k.alpha1 = p.alpha1;
+    k.data_term = p.data_term;
+    return k;
+}
+
+template <class F>
+tgvdct_status guarded(F&& f) {
+    try {
+        return f();
+    } catch (const Error& e) {
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        set_error("host allocation failed");
+        return TGVDCT_ERR_OOM;
+    } catch (...) {
+        set_error("unexpected exception");
+        return TGVDCT_ERR_CUDA;
+    }
+}
+
+DctPlan* plan_of(tgvdct_context* c) {
+    if (!c->plan) c->plan = dct_plan_create((int)c->prm.width, (int)c->prm.height, (int)c->prm.depth);
+    return c->plan;
+}
+
+float* host_cb_buffers(tgvdct_context* c) {
+    const size_t need = 4 * voxels(c->prm);
+    if (c->host_cb_count < need) {
+        if (c->host_cb) cudaFreeHost(c->host_cb);
+        c->host_cb = nullptr;
+        c->host_cb_count = 0;
+        TGV_CUDA(cudaMallocHost(&c->host_cb, need * sizeof(float)));
+        c->host_cb_count = need;
+    }
+    return c->host_cb;
+}
+
+// Hands u, a, b, c (device) to a callback: host copies unless callback_on_device.
+int deliver(tgvdct_context* c, tgvdct_iteration_callback cb, void* user, uint32_t it,
+            const float* u, const float* a, const float* b, const float* cc, cudaStream_t s) {
+    const size_t n = voxels(c->prm);
+    if (c->prm.callback_on_device) {
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return cb(it, c->prm.iteration_count, u, a, b, cc, user);
+    }
+    float* h = host_cb_buffers(c);
+    const float* src[4] = {u, a, b, cc};
+    const float* dst[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < 4; ++k) {
+        if (!src[k]) continue;
+        TGV_CUDA(cudaMemcpyAsync(h + k * n, src[k], n * 4, cudaMemcpyDeviceToHost, s));
+        dst[k] = h + k * n;
+    }
+    TGV_CUDA(cudaStreamSynchronize(s));
+    return cb(it, c->prm.iteration_count, dst[0], dst[1], dst[2], dst[3], user);
+}
+
+// The iteration loop on the context's state (st.f already holds the input).
+// `on_iteration` decides what a callback sees; returns true if stopped.
+template <class OnIteration>
+bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration) {
+    const TgvStep k = step_of(c->prm);
+    tgv_state_init(c->st, s);
+    const uint32_t n_it = c->prm.iteration_count, paint = c->prm.paint_iteration_interval;
+    c->iterations_run = 0;
+    for (uint32_t it = 0; it < n_it; ++it) {
+        tgv_iterate(c->st, k, s);
+        if (have_cb && paint > 0 && it > 0 && it % paint == 0) {  // tgv2_common.cu:381-384
+            if (on_iteration(it)) {
+                c->iterations_run = it + 1;
+                return true;
+            }
+        }
+    }
+    c->iterations_run = n_it;
+    return false;
+}
+
+void create_into(const tgvdct_params* p, tgvdct_context** out) {
+    validate(p);
+    TGV_REQUIRE(out != nullptr, "null context output pointer");
+    check_device();
+    tgvdct_context* c = new tgvdct_context();
+    c->prm = *p;
+    c->st.W = (int)p->width;
+    c->st.H = (int)p->height;
+    c->st.D = (int)p->depth;
+    c->st.three = p->geometry == TGVDCT_GEOMETRY_3D;
+    c->st.precision = p->state_precision;
+    const size_t bytes = tgv_state_bytes(c->st.W, c->st.H, c->st.D, c->st.three, c->st.precision);
+    cudaError_t e = cudaMalloc(&c->state_block, bytes);
+    if (e != cudaSuccess) {
+        delete c;
+        cudaGetLastError();
+        set_error(std::string("cudaMalloc of the TGV state: ") + cudaGetErrorString(e));
+        throw Error{TGVDCT_ERR_OOM};
+    }
+    tgv_state_bind(c->st, (char*)c->state_block);
+    *out = c;
+}
+
+void destroy_ctx(tgvdct_context* c) {
+    if (!c) return;
+    if (c->state_block) cudaFree(c->state_block);
+    if (c->cb_dev) cudaFree(c->cb_dev);
+    if (c->host_cb) cudaFreeHost(c->host_cb);
+    dct_plan_destroy(c->plan);
+    delete c;
+}
+
+struct CtxGuard {
+    tgvdct_context* c = nullptr;
+    ~CtxGuard() { destroy_ctx(c); }
+};
+
+struct DevBuf {
+    float* p = nullptr;
+    explicit DevBuf(size_t n) {
+        if (n) TGV_CUDA(cudaMalloc(&p, n * sizeof(float)));
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_dev, bool clamp,
+                       bool add_back, bool log_domain, float* u_dev, float* l_dev, float* r_dev,
+                       tgvdct_iteration_callback cb, void* user, cudaStream_t s) {
+    const size_t n = voxels(c->prm);
+    TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
+    if (log_domain) log_inplace(c->st.f, n, s);
+    DctPlan* plan = plan_of(c);
+    const bool mask_shading = mask_dev != nullptr;
+    const bool stopped = run_loop(c, s, cb != nullptr, [&](uint32_t it) {
+        // The GUI module deshades at every paint interval and hands u, l, r to its
+        // callback (TGVDeshadeProcessor.cpp:241-261); here that runs on the device.
+        if (!c->cb_dev) TGV_CUDA(cudaMalloc(&c->cb_dev, 2 * n * sizeof(float)));
+        float* l = c->cb_dev;
+        float* r = c->cb_dev + n;
+        poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, l,
+                          c->prm.dct_mode, c->prm.poisson_eigen, s);
+        deshade_epilogue(c->st.u, l, mask_dev, n, mask_shading, clamp, add_back, r, s);
+        return deliver(c, cb, user, it, c->st.u, l, r, nullptr, s) != 0;
+    });
+    (void)stopped;
+    TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
+    poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, l_dev,
+                      c->prm.dct_mode, c->prm.poisson_eigen, s);
+    deshade_epilogue(u_dev, l_dev, mask_dev, n, mask_shading, clamp, add_back, r_dev, s);
+    if (log_domain) {
+        exp_inplace(u_dev, n, s);
+        exp_inplace(l_dev, n, s);
+        exp_inplace(r_dev, n, s);
+    }
+}
+
+}  // namespace
+
+namespace {
+template <class Body>
+tgvdct_status with_plan(uint32_t w, uint32_t h, uint32_t d, Body&& body) {
+    return guarded([&] {
+        TGV_REQUIRE(w >= 1 && h >= 1 && d >= 1, "width, height, depth must be >= 1");
+        check_device();
+        DctPlan* plan = dct_plan_create((int)w, (int)h, (int)d);
+        struct PlanGuard {
+            DctPlan* p;
+            ~PlanGuard() { dct_plan_destroy(p); }
+        } pg{plan};
+        body(plan, (size_t)w * h * d);
+        TGV_CUDA(cudaStreamSynchronize(0));
+        return TGVDCT_OK;
+    });
+}
+}  // namespace
+
+extern "C" {
+
+const char* tgvdct_version(void) { return "tgvdct 0.1 (sm_103a)"; }
+
+const char* tgvdct_status_string(tgvdct_status s) {
+    switch (s) {
+        case TGVDCT_OK: return "ok";
+        case TGVDCT_ERR_BAD_ARG: return "bad argument";
+        case TGVDCT_ERR_OOM: return "out of memory";
+        case TGVDCT_ERR_CUDA: return "CUDA error";
+        case TGVDCT_ERR_NO_DEVICE: return "no suitable CUDA device";
+        case TGVDCT_ERR_UNSUPPORTED: return "unsupported mode";
+        case TGVDCT_STOPPED: return "stopped by the iteration callback";
+    }
+    return "unknown status";
+}
+
+const char* tgvdct_last_error(void) { return tgvdct::g_last_error.c_str(); }
+
+void tgvdct_params_init(tgvdct_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    // defaults of the TGV deshade widget (tgv_deshade/TGVDeshadeWidget.ui:43-119)
+    p->lambda = 1.f;
+    p->alpha0 = 2.f;
+    p->alpha1 = 1.f;
+    p->iteration_count = 10000;
+    const float step = (float)(1.0 / std::sqrt(20.0));  // tgv2_l1_deshade.cu:148-150
+    p->tau = step;
+    p->sigma = step;
+    p->theta = 1.f;
+    p->data_term = TGVDCT_DATA_L1;
+    p->geometry = TGVDCT_GEOMETRY_3D;
+    p->state_precision = TGVDCT_STATE_FP32;
+    p->dct_mode = TGVDCT_DCT_FP32;
+    p->poisson_eigen = TGVDCT_EIGEN_REFERENCE;
+}
+
+size_t tgvdct_workspace_bytes(const tgvdct_params* p) {
+    if (!p) return 0;
+    return tgv_state_bytes((int)p->width, (int)p->height, (int)p->depth,
+                           p->geometry == TGVDCT_GEOMETRY_3D, p->state_precision) +
+           dct_plan_bytes((int)p->width, (int)p->height, (int)p->depth);
+}
+
+tgvdct_status tgvdct_create(const tgvdct_params* p, tgvdct_context** out) {
+    return guarded([&] {
+        create_into(p, out);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_destroy(tgvdct_context* ctx) {
+    destroy_ctx(ctx);
+    return TGVDCT_OK;
+}
+
+tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p) {
+    return guarded([&] {
+        TGV_REQUIRE(ctx != nullptr, "null context");
+        validate(p);
+        TGV_REQUIRE(p->width == ctx->prm.width && p->height == ctx->prm.height &&
+                        p->depth == ctx->prm.depth,
+                    "set_params cannot change the shape");
+        TGV_REQUIRE(p->geometry == ctx->prm.geometry &&
+                        p->state_precision == ctx->prm.state_precision,
+                    "set_params cannot change geometry or state precision");
+        ctx->prm = *p;
+        return TGVDCT_OK;
+    });
+}
+
+uint32_t tgvdct_iterations_run(const tgvdct_context* ctx) { return ctx ? ctx->iterations_run : 0; }
+
+tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* c, const float* f_dev, float* u_dev,
+                                  float* v_x_dev, float* v_y_dev, float* v_z_dev,
+                                  tgvdct_iteration_callback cb, void* user, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(f_dev && u_dev && v_x_dev && v_y_dev, "null device buffer");
+        TGV_REQUIRE(v_z_dev || !c->st.three, "v_z is required for 3-D geometry");
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t n = voxels(c->prm);
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
+        const bool stopped = run_loop(c, s, cb != nullptr, [&](uint32_t it) {
+            return deliver(c, cb, user, it, c->st.u, c->st.v[0], c->st.v[1],
+                           c->st.three ? c->st.v[2] : nullptr, s) != 0;
+        });
+        TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(v_x_dev, c->st.v[0], n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(v_y_dev, c->st.v[1], n * 4, cudaMemcpyDeviceToDevice, s));
+        if (v_z_dev) {
+            if (c->st.three)
+                TGV_CUDA(cudaMemcpyAsync(v_z_dev, c->st.v[2], n * 4, cudaMemcpyDeviceToDevice, s));
+            else
+                TGV_CUDA(cudaMemsetAsync(v_z_dev, 0, n * 4, s));
+        }
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_l1_deshade_launch(const float* f_host, uint32_t width, uint32_t height,
+                                            uint32_t depth, float lambda,
+                                            uint32_t iteration_count,
+                                            uint32_t paint_iteration_interval,
+                                            int cuda_block_dimension,
+                                            tgvdct_iteration_callback callback, void* user,
+                                            float alpha0, float alpha1, float* u_host,
+                                            float* v_x_host, float* v_y_host, float* v_z_host) {
+    (void)cuda_block_dimension;
+    return guarded([&] {
+        TGV_REQUIRE(f_host && u_host && v_x_host && v_y_host && v_z_host, "null host buffer");
+        tgvdct_params p;
+        tgvdct_params_init(&p);
+        p.width = width;
+        p.height = height;
+        p.depth = depth;
+        p.lambda = lambda;
+        p.alpha0 = alpha0;
+        p.alpha1 = alpha1;
+        p.iteration_count = iteration_count;
+        p.paint_iteration_interval = paint_iteration_interval;
+        CtxGuard g;
+        create_into(&p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(p);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        const bool stopped = run_loop(c, s, callback != nullptr, [&](uint32_t it) {
+            return deliver(c, callback, user, it, c->st.u, c->st.v[0], c->st.v[1], c->st.v[2], s) != 0;
+        });
+        TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_z_host, c->st.v[2], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t width,
+                                               uint32_t height, float lambda,
+                                               uint32_t iteration_count,
+                                               uint32_t paint_iteration_interval,
+                                               tgvdct_iteration_callback callback, void* user,
+                                               float alpha0, float alpha1, float* u_host,
+                                               float* v_x_host, float* v_y_host) {
+    return guarded([&] {
+        TGV_REQUIRE(f_host && u_host && v_x_host && v_y_host, "null host buffer");
+        tgvdct_params p;
+        tgvdct_params_init(&p);
+        p.width = width;
+        p.height = height;
+        p.depth = 1;
+        p.geometry = TGVDCT_GEOMETRY_2D;
+        p.lambda = lambda;
+        p.alpha0 = alpha0;
+        p.alpha1 = alpha1;
+        p.iteration_count = iteration_count;
+        p.paint_iteration_interval = paint_iteration_interval;
+        CtxGuard g;
+        create_into(&p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(p);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        const bool stopped = run_loop(c, s, callback != nullptr, [&](uint32_t it) {
+            return deliver(c, callback, user, it, c->st.u, c->st.v[0], c->st.v[1], nullptr, s) != 0;
+        });
+        TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, uint32_t height,
+                                         uint32_t depth, int32_t data_term, float lambda,
+                                         uint32_t iteration_count, float alpha0, float alpha1,
+                                         float* u_host) {
+    return guarded([&] {
+        TGV_REQUIRE(f_host && u_host, "null host buffer");
+        tgvdct_params p;
+        tgvdct_params_init(&p);
+        p.width = width;
+        p.height = height;
+        p.depth = depth;
+        p.data_term = data_term;
+        p.lambda = lambda;
+        p.alpha0 = alpha0;
+        p.alpha1 = alpha1;
+        p.iteration_count = iteration_count;
+        CtxGuard g;
+        create_into(&p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(p);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        run_loop(c, s, false, [](uint32_t) { return false; });
+        TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return TGVDCT_OK;
+    });
+}
+
+// ---- Poisson integration and image operations (host buffers) ----------------------
+
+
+tgvdct_status tgvdct_divergence_launch(const float* dx, const float* dy, const float* dz,
+                                       uint32_t width, uint32_t height, uint32_t depth,
+                                       float* out) {
+    return with_plan(width, height, depth, [&](DctPlan* plan, size_t n) {
+        TGV_REQUIRE(dx && dy && out && (dz || depth == 1), "null host buffer");
+        DevBuf a(n), b(n), c(depth > 1 ? n : 0), o(n);
+        TGV_CUDA(cudaMemcpy(a.p, dx, n * 4, cudaMemcpyHostToDevice));
+        TGV_CUDA(cudaMemcpy(b.p, dy, n * 4, cudaMemcpyHostToDevice));
+        if (depth > 1) TGV_CUDA(cudaMemcpy(c.p, dz, n * 4, cudaMemcpyHostToDevice));
+        divergence(plan, a.p, b.p, c.p, o.p, 0);
+        TGV_CUDA(cudaMemcpy(out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_cosine_transform_launch(const float* in, uint32_t width, uint32_t height,
+                                             uint32_t depth, int32_t dct_mode, float* out) {
+    return with_plan(width, height, depth, [&](DctPlan* plan, size_t n) {
+        TGV_REQUIRE(in && out, "null host buffer");
+        DevBuf a(n), o(n);
+        TGV_CUDA(cudaMemcpy(a.p, in, n * 4, cudaMemcpyHostToDevice));
+        cosine_transform(plan, a.p, o.p, dct_mode, 0);
+        TGV_CUDA(cudaMemcpy(out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_inverse_cosine_transform_launch(const float* in, uint32_t width,
+                                                     uint32_t height, uint32_t depth,
+                                                     int32_t dct_mode, float* out) {
+    return with_plan(width, height, depth, [&](DctPlan* plan, size_t n) {
+        TGV_REQUIRE(in && out, "null host buffer");
+        DevBuf a(n), o(n);
+        TGV_CUDA(cudaMemcpy(a.p, in, n * 4, cudaMemcpyHostToDevice));
+        inverse_cosine_transform(plan, a.p, o.p, dct_mode, 0);
+        TGV_CUDA(cudaMemcpy(out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_solve_poisson_in_cosine_domain_launch(const float* in, uint32_t width,
+                                                           uint32_t height, uint32_t depth,
+                                                           int32_t poisson_eigen, float* out) {
+    return with_plan(width, height, depth, [&](DctPlan* plan, size_t n) {
+        TGV_REQUIRE(in && out, "null host buffer");
+        DevBuf a(n), o(n);
+        TGV_CUDA(cudaMemcpy(a.p, in, n * 4, cudaMemcpyHostToDevice));
+        solve_poisson(plan, a.p, o.p, poisson_eigen, 0);
+        TGV_CUDA(cudaMemcpy(out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_integrate_image_gradients_poisson_cosine_transform(
+    const float* v_x, const float* v_y, const float* v_z, uint32_t width, uint32_t height,
+    uint32_t depth, int32_t dct_mode, int32_t poisson_eigen, float* l_out) {
+    return with_plan(width, height, depth, [&](DctPlan* plan, size_t n) {
+        TGV_REQUIRE(v_x && v_y && l_out && (v_z || depth == 1), "null host buffer");
+        DevBuf a(n), b(n), c(depth > 1 ? n : 0), o(n);
+        TGV_CUDA(cudaMemcpy(a.p, v_x, n * 4, cudaMemcpyHostToDevice));
+        TGV_CUDA(cudaMemcpy(b.p, v_y, n * 4, cudaMemcpyHostToDevice));
+        if (depth > 1) TGV_CUDA(cudaMemcpy(c.p, v_z, n * 4, cudaMemcpyHostToDevice));
+        poisson_integrate(plan, a.p, b.p, c.p, o.p, dct_mode, poisson_eigen, 0);
+        TGV_CUDA(cudaMemcpy(l_out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* c, const float* v_x_dev,
+                                           const float* v_y_dev, const float* v_z_dev,
+                                           float* l_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(v_x_dev && v_y_dev && l_dev && (v_z_dev || c->prm.depth == 1),
+                    "null device buffer");
+        poisson_integrate(plan_of(c), v_x_dev, v_y_dev, v_z_dev, l_dev, c->prm.dct_mode,
+                          c->prm.poisson_eigen, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_deshade_epilogue_dev(const float* u_dev, float* l_dev, const float* mask_dev,
+                                          uint64_t voxel_count, int32_t mask_shading,
+                                          int32_t set_negative_values_to_zero,
+                                          int32_t add_background_back, float* r_dev,
+                                          void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(u_dev && l_dev && r_dev, "null device buffer");
+        deshade_epilogue(u_dev, l_dev, mask_dev, (size_t)voxel_count, mask_shading != 0,
+                         set_negative_values_to_zero != 0, add_background_back != 0, r_dev,
+                         (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_process_dev(tgvdct_context* c, const float* f_dev, const float* mask_dev,
+                                 int32_t set_negative_values_to_zero, int32_t add_background_back,
+                                 int32_t log_domain, float* u_dev, float* l_dev, float* r_dev,
+                                 tgvdct_iteration_callback callback, void* user, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(f_dev && u_dev && l_dev && r_dev, "null device buffer");
+        process_on_device(c, f_dev, mask_dev, set_negative_values_to_zero != 0,
+                          add_background_back != 0, log_domain != 0, u_dev, l_dev, r_dev, callback,
+                          user, (cudaStream_t)stream);
+        return c->iterations_run < c->prm.iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host,
+                                     const float* mask_host, int32_t set_negative_values_to_zero,
+                                     int32_t add_background_back, int32_t log_domain,
+                                     tgvdct_iteration_callback callback, void* user,
+                                     float* denoised_host, float* shading_host,
+                                     float* deshaded_host) {
+    return guarded([&] {
+        TGV_REQUIRE(f_host && denoised_host && shading_host && deshaded_host, "null host buffer");
+        CtxGuard g;
+        create_into(p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(*p);
+        DevBuf f(n), m(mask_host ? n : 0), u(n), l(n), r(n);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(f.p, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        if (mask_host) TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        process_on_device(c, f.p, mask_host ? m.p : nullptr, set_negative_values_to_zero != 0,
+                          add_background_back != 0, log_domain != 0, u.p, l.p, r.p, callback, user,
+                          s);
+        TGV_CUDA(cudaMemcpyAsync(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return c->iterations_run < p->iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// Internal declarations shared by the kernel files and the C ABI.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "tgvdct.h"
+
+namespace tgvdct {
+
+// ---- error plumbing -------------------------------------------------------
+void set_error(const std::string& msg);
+
+struct Error {
+    tgvdct_status status;
+};
+
+#define TGV_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            ::tgvdct::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));     \
+            throw ::tgvdct::Error{e_ == cudaErrorMemoryAllocation ? TGVDCT_ERR_OOM       \
+                                                                  : TGVDCT_ERR_CUDA};    \
+        }                                                                                \
+    } while (0)
+
+#define TGV_CHECK_LAUNCH() TGV_CUDA(cudaGetLastError())
+
+#define TGV_REQUIRE(cond, msg)                                \
+    do {                                                      \
+        if (!(cond)) {                                        \
+            ::tgvdct::set_error(msg);                         \
+            throw ::tgvdct::Error{TGVDCT_ERR_BAD_ARG};        \
+        }                                                     \
+    } while (0)
+
+// ---- TGV2 loop ---------------------------------------------------------------
+// Device state of one volume.  Fields are planar (structure of arrays), x fastest.
+// p (3 or 2 components) and q (6 or 3) are stored in the state precision's
+// element type; everything else in FP32.
+struct TgvState {
+    int W = 0, H = 0, D = 0;
+    bool three = true;       // 3-D operators (also for D == 1) vs the 2-D launcher
+    int precision = TGVDCT_STATE_FP32;
+    float* u = nullptr;
+    float* ubar = nullptr;
+    float* f = nullptr;      // private copy of the input (log-domain runs rewrite it)
+    float* v[3] = {nullptr, nullptr, nullptr};
+    float* vbar[3] = {nullptr, nullptr, nullptr};
+    void* p[3] = {nullptr, nullptr, nullptr};
+    void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
+};
+
+struct TgvStep {
+    float tau, sigma, theta, lambda, alpha0, alpha1;
+    int data_term;
+};
+
+size_t tgv_state_bytes(int W, int H, int D, bool three, int precision);
+// Carves the state out of `base` (aligned to 256 bytes per field).
+void tgv_state_bind(TgvState& s, char* base);
+// u = ubar = f, p = q = v = vbar = 0.
+void tgv_state_init(const TgvState& s, cudaStream_t st);
+// One primal-dual iteration: the dual pass, then the primal pass.
+void tgv_iterate(const TgvState& s, const TgvStep& k, cudaStream_t st);
+// Number of kernels tgv_iterate launches.
+int tgv_kernels_per_iteration();
+
+// ---- Poisson integration -------------------------------------------------------
+struct DctPlan;  // per-shape cosine tables and scratch
+DctPlan* dct_plan_create(int W, int H, int D);
+void dct_plan_destroy(DctPlan* p);
+size_t dct_plan_bytes(int W, int H, int D);
+
+// l = DCT-III( DCT-II(div v) / eigenvalue ) with the reference's scale factors.
+void poisson_integrate(DctPlan* plan, const float* vx, const float* vy, const float* vz,
+                       float* l, int dct_mode, int eigen_mode, cudaStream_t st);
+// The separate steps of the reference's CudaImageOperationsProcessor.
+void divergence(DctPlan* plan, const float* vx, const float* vy, const float* vz, float* out,
+                cudaStream_t st);
+void cosine_transform(DctPlan* plan, const float* in, float* out, int dct_mode, cudaStream_t st);
+void inverse_cosine_transform(DctPlan* plan, const float* in, float* out, int dct_mode,
+                              cudaStream_t st);
+void solve_poisson(DctPlan* plan, const float* in, float* out, int eigen_mode, cudaStream_t st);
+
+// ---- element-wise ------------------------------------------------------------
+void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,
+                      bool clamp, bool add_back, float* r, cudaStream_t st);
+void log_inplace(float* x, size_t n, cudaStream_t st);
+void exp_inplace(float* x, size_t n, cudaStream_t st);
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace tgvdct

@@ -1,0 +1,341 @@
+"""Benchmark of the TGV-DCT deshade hot path on one GB300 (or N independent replicas).
+
+Workload (the 256x256x192 full deshade): the 5-class tissue phantom times a smooth
+bias exp(b), Rician-like noise (seed 2), taken to the log domain; 1500 TGV2-L1
+iterations (lambda=1, alpha0=2, alpha1=1, reference steps tau=sigma=1/sqrt(20)),
+then the DCT Poisson integration of v and r = u - l.  One "step" is one whole
+deshade of the volume.  Metric: voxel-iterations per second.
+
+  value  device-timed, input already in HBM, through tgvdct_process_dev
+  e2e    the reference-facing call tgvdct_process_tgv2_l1 with host buffers
+         (host->device copy of f and device->host copies of u, l, r inside)
+  roofline  the TGV iteration kernels, timed live with CUDA events on the stream
+         they run on; algorithmic bytes per voxel-iteration as in the design doc
+
+``--impl reference`` times the reference algorithm's CPU restatement (the oracle
+port; the reference itself has no CPU path) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    # name: (D, H, W, iterations)
+    "deshade_256x256x192": (192, 256, 256, 1500),
+    "deshade_128x128x128": (128, 128, 128, 2000),
+}
+# algorithmic bytes per voxel-iteration of one TGV2 iteration (read f, u, ubar, v3,
+# vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
+ALGO_BYTES = {0: 140, 1: 104, 2: 104}
+# bytes the two-pass FP32 iteration moves (dual 13 loads + 9 stores, primal 14 + 8)
+PASS_BYTES = {"two_pass": {0: 176, 1: 140, 2: 140}}
+PREC_NAMES = {0: "fp32", 1: "bf16_dual", 2: "fx16_dual"}
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0, period_ms=200):
+        self.index, self.period_ms = index, period_ms
+        self.proc, self.lines = None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", f"-lms", str(self.period_ms)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def make_input(workload):
+    from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
+    d, h, w, _ = WORKLOADS[workload]
+    return tissue_phantom_3d(d, h, w, seed=2)
+
+
+# ---------------------------------------------------------------------------------
+def cpu_reference(args, f, iterations_sample, threads=None):
+    """The reference algorithm on the host cores (oracle port, FP32, OpenMP)."""
+    import oracle
+    cores = oracle.set_threads(threads or os.cpu_count() or 1)
+    flog = np.log(f).astype(np.float32)
+    t0 = time.perf_counter()
+    oracle.tgv2_deshade(flog, 1.0, 2.0, 1.0, iterations_sample, dtype=np.float32)
+    dt = time.perf_counter() - t0
+    return f.size * iterations_sample / dt, cores, dt
+
+
+def run_reference_arm(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    f = make_input(args.workload)
+    d, h, w, iters = WORKLOADS[args.workload]
+    # bounded sample: a few iterations of the same volume per step
+    sample_it = args.cpu_sample_iterations
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_reference(args, f, 1)
+    rates, cores = [], 1
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r, cores, _ = cpu_reference(args, f, sample_it)
+        rates.append(r)
+    wall = time.perf_counter() - t_all
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": "voxel_iters_per_s", "value": value,
+        "unit": "voxel-iter/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wall / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "shape_dhw": [d, h, w], "iterations": iters,
+                   "sample_iterations_per_step": sample_it},
+        "cpu_baseline": {"value": value, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample_it} TGV2-L1 iterations of the {d}x{h}x{w} volume "
+                                   "per step (the reference has no CPU implementation; this is "
+                                   "its kernel sequence restated in C++/OpenMP)"},
+        "e2e": {"value": value, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import ambient_image_processor_gb300 as pkg
+
+    rank = env_int("RANK", 0)
+    world = env_int("WORLD_SIZE", 1)
+    local = env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("nccl")
+
+    d, h, w, iters = WORKLOADS[args.workload]
+    if args.iterations:
+        iters = args.iterations
+    V = d * h * w
+    f_host = make_input(args.workload)
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iters,
+                             state_precision=args.precision, dct_mode=pkg.DCT_FP32,
+                             poisson_eigen=args.eigen)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    dev = torch.device("cuda", local)
+    f = torch.from_numpy(f_host).to(dev)
+    u, l, r = (torch.empty_like(f) for _ in range(3))
+    ctx = pkg.Context(prm)
+
+    def step():
+        ctx.process_dev(f.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
+                        set_negative_values_to_zero=False, log_domain=True, stream=sh)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * V * iters / (ms * 1e-3)
+
+    # ---- roofline of the iteration kernels: iterations alone, events on the stream
+    n_prof = args.profile_iterations
+    prm_it = pkg.default_params(width=w, height=h, depth=d, iteration_count=n_prof,
+                                state_precision=args.precision)
+    ctx.set_params(prm_it)
+    vx, vy, vz = (torch.empty_like(f) for _ in range(3))
+
+    def iters_only():
+        ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr(),
+                    stream=sh)
+
+    iters_only()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iters_only()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    it_ms = e0.elapsed_time(e1) / n_prof
+    launches_per_it = 2
+    launch_ms = it_ms / launches_per_it
+    peak, peak_kind = hbm_peak()
+    algo = ALGO_BYTES[args.precision]
+    achieved = algo * V / (it_ms * 1e-3) / 1e9  # GB/s of algorithmic bytes per iteration
+
+    # ---- e2e through the host-buffer C-ABI call (reference-facing)
+    ctx.set_params(prm)
+    e2e_ms = None
+    if rank == 0 or True:
+        fh = np.ascontiguousarray(f_host)
+        uo, lo, ro = (np.empty_like(fh) for _ in range(3))
+        times = []
+        for k in range(args.e2e_steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = pkg.lib().tgvdct_process_tgv2_l1(ctypes.byref(prm), fh, None, 0, 0, 1,
+                                                  pkg.CALLBACK(), None, uo, lo, ro)
+            torch.cuda.synchronize()
+            if st != pkg.OK:
+                raise RuntimeError(pkg.lib().tgvdct_last_error().decode())
+            if k > 0:
+                times.append(time.perf_counter() - t0)
+        e2e_ms = 1e3 * float(np.median(times))
+    e2e_value = world * V * iters / (e2e_ms * 1e-3)
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            rate, cores, dt = cpu_reference(args, f_host, args.cpu_sample_iterations)
+            cpu = {"value": rate, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+                   "sample": f"{args.cpu_sample_iterations} TGV2-L1 iterations of the same "
+                             f"{d}x{h}x{w} log volume ({dt:.1f} s)"}
+        gpu_launches = iters * launches_per_it + 6 + 1 + 4  # loop, DCT passes, epilogue, log/exp
+        line = {
+            "metric": "voxel_iters_per_s", "value": value, "unit": "voxel-iter/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == 0 else "f32+" + PREC_NAMES[args.precision],
+            "data": "synthetic",
+            "config": {"workload": args.workload, "shape_dhw": [d, h, w], "iterations": iters,
+                       "state_precision": PREC_NAMES[args.precision], "dct": "fp32",
+                       "poisson_eigen": "accurate" if args.eigen else "reference",
+                       "pass_structure": "two_pass",
+                       "l2": "state of 1.6 GB per replica, larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "clocks": clocks.summary(),
+            "e2e": {"value": e2e_value, "unit": "voxel-iter/s",
+                    "h2d_bytes_per_step": V * 4, "d2h_bytes_per_step": 3 * V * 4,
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": gpu_launches * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "tgv_dual_kernel + tgv_primal_kernel (one iteration)",
+                         "algorithmic_bytes_per_voxel_iter": algo,
+                         "moved_bytes_per_voxel_iter": PASS_BYTES["two_pass"][args.precision],
+                         "iteration_ms": it_ms, "launch_ms": launch_ms,
+                         "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="deshade_256x256x192", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
+    ap.add_argument("--eigen", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--iterations", type=int, default=0, help="override the iteration count")
+    ap.add_argument("--profile-iterations", type=int, default=200)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample-iterations", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,237 @@
+/*
+ * tgvdct.h — C ABI of the GB300-native TGV-DCT shading-correction path.
+ *
+ * One data-parallel hot path of josefkoller/ambient_image_processor, rebuilt for
+ * sm_103a: the TGV2 primal-dual loop (L1 or L2 data term, Neumann boundaries) that
+ * produces the denoised image u and the bias gradient field v, followed by the
+ * DCT-II Poisson solve that integrates v into the smooth shading field l, and the
+ * deshade epilogue r = u - l.
+ *
+ * Conventions shared by every entry point:
+ *   - Images are float32, x fastest: index = z*width*height + y*width + x
+ *     (the reference's ITKImage layout, source/modules/itk/ITKImage.cpp:84).
+ *   - Functions return a tgvdct_status; they never print-and-exit the way the
+ *     reference's cudaCheckError does (source/modules/cuda/cuda_helper.in:11-21).
+ *     tgvdct_last_error() describes the last failure on the calling thread.
+ *   - "_launch" entry points take HOST buffers owned by the caller and do their
+ *     own host<->device copies, like the reference launchers; the caller
+ *     allocates the outputs (the reference returned new[] arrays instead).
+ *   - "_dev" entry points take DEVICE buffers and a cudaStream_t (passed as
+ *     void*, NULL = the legacy default stream) and are asynchronous unless a
+ *     callback forces a synchronisation.
+ *   - A context (tgvdct_context) owns the device workspace of one volume shape;
+ *     one context must not be used by two threads at the same time.  Distinct
+ *     contexts are independent.
+ */
+#ifndef TGVDCT_H
+#define TGVDCT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TGVDCT_VERSION_MAJOR 0
+#define TGVDCT_VERSION_MINOR 1
+
+typedef enum tgvdct_status {
+    TGVDCT_OK = 0,
+    TGVDCT_ERR_BAD_ARG = 1,     /* invalid shape, parameter or null pointer */
+    TGVDCT_ERR_OOM = 2,         /* device or host allocation failed */
+    TGVDCT_ERR_CUDA = 3,        /* a CUDA runtime call or kernel launch failed */
+    TGVDCT_ERR_NO_DEVICE = 4,   /* no CUDA device, or not an sm_103 device */
+    TGVDCT_ERR_UNSUPPORTED = 5, /* a mode this build does not provide */
+    TGVDCT_STOPPED = 6          /* the iteration callback asked to stop; outputs hold
+                                   the state after the iteration it was called for */
+} tgvdct_status;
+
+typedef enum tgvdct_data_term {
+    TGVDCT_DATA_L1 = 0, /* |u - f|: tgv_cuda/tgv2_l1.cu:27-60 */
+    TGVDCT_DATA_L2 = 1  /* (u - f)^2 / 2: tgv_cuda/tgv2_l2.cu:27-56 */
+} tgvdct_data_term;
+
+typedef enum tgvdct_geometry {
+    /* The 3-D launcher (tgv_deshade/tgv2_l1_deshade.cu), also for depth == 1 as
+       the reference's terminal program runs 2-D images. */
+    TGVDCT_GEOMETRY_3D = 0,
+    /* The 2-D launcher (tgv_deshade/tgv2_l1_deshade_2d.cu): two gradient
+       components, q = (xx, yy, xy).  Requires depth == 1. */
+    TGVDCT_GEOMETRY_2D = 1
+} tgvdct_geometry;
+
+typedef enum tgvdct_state_precision {
+    TGVDCT_STATE_FP32 = 0,      /* every field stored in FP32 (the plain drop-in) */
+    TGVDCT_STATE_BF16_DUAL = 1, /* dual fields p, q stored in BF16, updates in FP32 */
+    TGVDCT_STATE_FX16_DUAL = 2  /* p, q stored as 16-bit fixed point scaled by alpha1 /
+                                   alpha0 (the projections bound every component by
+                                   alpha), updates in FP32 */
+} tgvdct_state_precision;
+
+typedef enum tgvdct_dct_mode {
+    TGVDCT_DCT_FP32 = 0,   /* FP32 FMA contractions on the CUDA cores */
+    TGVDCT_DCT_TF32 = 1,   /* tensor cores (tcgen05), one TF32 product */
+    TGVDCT_DCT_BF16X3 = 2  /* tensor cores (tcgen05), BF16 hi/lo split, three
+                              products, FP32 accumulation */
+} tgvdct_dct_mode;
+
+typedef enum tgvdct_poisson_eigen {
+    /* 6 - 2cospi(kx/W) - 2cospi(ky/H) - 2cospi(kz/D) with FP32 cosines summed in
+       FP64, as solve_poisson_in_cosine_domain.cu:48-53 computes it. */
+    TGVDCT_EIGEN_REFERENCE = 0,
+    /* 4sin^2(pi kx/2W) + 4sin^2(pi ky/2H) + 4sin^2(pi kz/2D): the same value
+       without the cancellation near the zero frequency. */
+    TGVDCT_EIGEN_ACCURATE = 1
+} tgvdct_poisson_eigen;
+
+/* Parameters of one deshade.  tgvdct_params_init() fills the reference defaults. */
+typedef struct tgvdct_params {
+    uint32_t width, height, depth;
+    float lambda;             /* data-term weight */
+    float alpha0;             /* second-order weight: bounds q */
+    float alpha1;             /* first-order weight: bounds p */
+    uint32_t iteration_count;
+    float tau, sigma, theta;  /* 1/sqrt(20), 1/sqrt(20), 1 in the reference
+                                 (tgv_deshade/tgv2_l1_deshade.cu:148-150) */
+    int32_t data_term;        /* tgvdct_data_term */
+    int32_t geometry;         /* tgvdct_geometry */
+    int32_t state_precision;  /* tgvdct_state_precision */
+    int32_t dct_mode;         /* tgvdct_dct_mode */
+    int32_t poisson_eigen;    /* tgvdct_poisson_eigen */
+    uint32_t paint_iteration_interval; /* callback cadence; 0 = never */
+    int32_t callback_on_device;        /* 0: callback gets host copies (reference
+                                          behaviour); 1: device pointers */
+} tgvdct_params;
+
+/* Called after iteration `iteration_index` when iteration_index > 0 and
+   iteration_index % paint_iteration_interval == 0 (tgv_cuda/tgv2_common.cu:381-384).
+   u, v_x, v_y, v_z are valid only during the call; v_z is NULL for 2-D geometry.
+   Return nonzero to stop the loop (the reference's `return true`). */
+typedef int (*tgvdct_iteration_callback)(uint32_t iteration_index, uint32_t iteration_count,
+                                         const float* u, const float* v_x, const float* v_y,
+                                         const float* v_z, void* user);
+
+typedef struct tgvdct_context tgvdct_context;
+
+/* ---- library ------------------------------------------------------------ */
+const char* tgvdct_version(void);
+const char* tgvdct_status_string(tgvdct_status s);
+const char* tgvdct_last_error(void);
+void tgvdct_params_init(tgvdct_params* p);
+/* Bytes of device memory a context for these parameters allocates. */
+size_t tgvdct_workspace_bytes(const tgvdct_params* p);
+
+/* ---- contexts (device workspace of one shape) --------------------------- */
+tgvdct_status tgvdct_create(const tgvdct_params* p, tgvdct_context** out);
+tgvdct_status tgvdct_destroy(tgvdct_context* ctx);
+/* Change lambda, alpha, iterations, steps, data term, modes or callback cadence
+   of a context; the shape, geometry and state precision must stay the same. */
+tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p);
+/* Number of iterations the last run completed (less than iteration_count when a
+   callback stopped it). */
+uint32_t tgvdct_iterations_run(const tgvdct_context* ctx);
+
+/* ---- the TGV2 loop ------------------------------------------------------ */
+/* Replaces tgv2_l1_deshade_launch<float> (tgv_deshade/tgv2_l1_deshade.cu:33-41),
+   the reference's TGV2-L1 deshade loop: host f in, host u and v out.  The 3-D
+   operators run also when depth == 1, so v_z holds their z component then, as
+   in the reference.  cuda_block_dimension is accepted for signature
+   compatibility and ignored (launch shapes are chosen for sm_103a). */
+tgvdct_status tgvdct_tgv2_l1_deshade_launch(const float* f_host, uint32_t width, uint32_t height,
+                                            uint32_t depth, float lambda,
+                                            uint32_t iteration_count,
+                                            uint32_t paint_iteration_interval,
+                                            int cuda_block_dimension,
+                                            tgvdct_iteration_callback callback, void* user,
+                                            float alpha0, float alpha1, float* u_host,
+                                            float* v_x_host, float* v_y_host, float* v_z_host);
+
+/* Replaces tgv2_l1_deshade_launch_2d<float> (tgv_deshade/tgv2_l1_deshade_2d.cu:29-36). */
+tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t width,
+                                               uint32_t height, float lambda,
+                                               uint32_t iteration_count,
+                                               uint32_t paint_iteration_interval,
+                                               tgvdct_iteration_callback callback, void* user,
+                                               float alpha0, float alpha1, float* u_host,
+                                               float* v_x_host, float* v_y_host);
+
+/* Replaces tgv2_l1_launch / tgv2_l2_launch (tgv_cuda/tgv2_l1.cu:64-72,
+   tgv_cuda/tgv2_l2.cu:60-68): the TGV filter's denoise loop, u only. */
+tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, uint32_t height,
+                                         uint32_t depth, int32_t data_term, float lambda,
+                                         uint32_t iteration_count, float alpha0, float alpha1,
+                                         float* u_host);
+
+/* General form: every parameter of tgvdct_params, device buffers, stream.
+   v_z_dev may be NULL for 2-D geometry.  f_dev is not modified. */
+tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* ctx, const float* f_dev, float* u_dev,
+                                  float* v_x_dev, float* v_y_dev, float* v_z_dev,
+                                  tgvdct_iteration_callback callback, void* user, void* stream);
+
+/* ---- Poisson integration of v (DCT-II / DCT-III) -------------------------- */
+/* Each replaces the host-in/host-out launcher of the same name:
+   divergence_kernel_launch (cuda_image_operations/divergence.cu:59-61; depth == 1
+   uses the 2-D kernels as CudaImageOperationsProcessor.cpp:290-291 does),
+   cosine_transform_kernel_launch (cosine_transform.cu:226-227),
+   solve_poisson_in_cosine_domain_kernel_launch (solve_poisson_in_cosine_domain.cu:86-87),
+   inverse_cosine_transform_kernel_launch (inverse_cosine_transform.cu:167-168). */
+tgvdct_status tgvdct_divergence_launch(const float* dx, const float* dy, const float* dz,
+                                       uint32_t width, uint32_t height, uint32_t depth,
+                                       float* out);
+tgvdct_status tgvdct_cosine_transform_launch(const float* in, uint32_t width, uint32_t height,
+                                             uint32_t depth, int32_t dct_mode, float* out);
+tgvdct_status tgvdct_inverse_cosine_transform_launch(const float* in, uint32_t width,
+                                                     uint32_t height, uint32_t depth,
+                                                     int32_t dct_mode, float* out);
+tgvdct_status tgvdct_solve_poisson_in_cosine_domain_launch(const float* in, uint32_t width,
+                                                           uint32_t height, uint32_t depth,
+                                                           int32_t poisson_eigen, float* out);
+
+/* Replaces TGVDeshadeProcessor::integrate_image_gradients_poisson_cosine_transform
+   (tgv_deshade/TGVDeshadeProcessor.cpp:386-408, 2-D :410-431): l from v. */
+tgvdct_status tgvdct_integrate_image_gradients_poisson_cosine_transform(
+    const float* v_x, const float* v_y, const float* v_z, uint32_t width, uint32_t height,
+    uint32_t depth, int32_t dct_mode, int32_t poisson_eigen, float* l_out);
+
+/* Device form on a context: l_dev from v on the device (v_z_dev may be NULL when
+   depth == 1).  Uses the context's dct_mode and poisson_eigen. */
+tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* ctx, const float* v_x_dev,
+                                           const float* v_y_dev, const float* v_z_dev,
+                                           float* l_dev, void* stream);
+
+/* ---- deshade epilogue and the whole processor ----------------------------- */
+/* Device form of TGVDeshadeProcessor::deshade_poisson_cosine_transform's tail
+   (TGVDeshadeProcessor.cpp:83-92) plus the background add-back (:275-279):
+   r = u - l; with a mask, l *= mask (when mask_shading) and r *= mask; clamp
+   r < 0 to 0; add u*(1-mask) back.  mask_dev may be NULL. */
+tgvdct_status tgvdct_deshade_epilogue_dev(const float* u_dev, float* l_dev, const float* mask_dev,
+                                          uint64_t voxel_count, int32_t mask_shading,
+                                          int32_t set_negative_values_to_zero,
+                                          int32_t add_background_back, float* r_dev,
+                                          void* stream);
+
+/* Replaces TGVDeshadeProcessor::processTGV2L1GPUCuda (TGVDeshadeProcessor.cpp:122-166
+   for the terminal program; :285-314 with a mask, callback and add-back for the
+   GUI module): denoised u, shading l and deshaded r from f, host buffers.
+   mask may be NULL.  With log_domain, f is replaced by log(f) before the loop and
+   the three outputs are exponentiated (the multiplicative-bias use). */
+tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host,
+                                     const float* mask_host, int32_t set_negative_values_to_zero,
+                                     int32_t add_background_back, int32_t log_domain,
+                                     tgvdct_iteration_callback callback, void* user,
+                                     float* denoised_host, float* shading_host,
+                                     float* deshaded_host);
+
+/* Device form of the whole deshade on a context (no host copies): f_dev in; u,
+   l, r out; mask_dev may be NULL.  Stream-ordered. */
+tgvdct_status tgvdct_process_dev(tgvdct_context* ctx, const float* f_dev, const float* mask_dev,
+                                 int32_t set_negative_values_to_zero, int32_t add_background_back,
+                                 int32_t log_domain, float* u_dev, float* l_dev, float* r_dev,
+                                 tgvdct_iteration_callback callback, void* user, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TGVDCT_H */

@@ -1,0 +1,198 @@
+"""TEST INFRASTRUCTURE — Python bindings of the CPU oracle.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may use
+this package, and only as the checker.  ``liboracle.so`` is the C++ restatement of
+the reference's TGV-DCT kernel sequence (``tgv_oracle.hpp``); ``libref_cpu.so``
+(optional, ``oracle/_ref``) is the reference's own CUDA source compiled for the CPU
+by ``ref_cpu/build_ref_cpu.py`` where the reference tree is available.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "liboracle.so")
+_REF_PATH = os.path.join(HERE, "_ref", "libref_cpu.so")
+
+_lib = None
+_ref = None
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u = ctypes.c_uint
+_d = ctypes.c_double
+
+
+def build() -> str:
+    """Compile liboracle.so with the committed Makefile (g++, OpenMP)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_set_threads.restype = ctypes.c_int
+        for suf, p in (("f32", _f32p), ("f64", _f64p)):
+            fn = getattr(L, f"oracle_tgv2_deshade_{suf}")
+            fn.argtypes = [p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int, ctypes.c_int,
+                           p, p, p, p]
+            fn.restype = _u
+            fn = getattr(L, f"oracle_divergence_{suf}")
+            fn.argtypes = [p, p, p, _u, _u, _u, p]
+            for name in ("cosine_transform", "inverse_cosine_transform", "solve_poisson"):
+                fn = getattr(L, f"oracle_{name}_{suf}")
+                fn.argtypes = [p, _u, _u, _u, p]
+            fn = getattr(L, f"oracle_integrate_poisson_dct_{suf}")
+            fn.argtypes = [p, p, p, _u, _u, _u, p]
+            fn = getattr(L, f"oracle_deshade_epilogue_{suf}")
+            fn.argtypes = [p, p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int) -> int:
+    return lib().oracle_set_threads(int(n))
+
+
+def _dt(dtype):
+    dtype = np.dtype(dtype)
+    if dtype == np.float32:
+        return "f32"
+    if dtype == np.float64:
+        return "f64"
+    raise TypeError(f"unsupported dtype {dtype}")
+
+
+def _shape3(a: np.ndarray):
+    """(depth, height, width) array -> (w, h, d); 2-D arrays are (height, width)."""
+    if a.ndim == 2:
+        return a.shape[1], a.shape[0], 1
+    if a.ndim == 3:
+        return a.shape[2], a.shape[1], a.shape[0]
+    raise ValueError("expected a 2-D (H, W) or 3-D (D, H, W) array")
+
+
+def tgv2_deshade(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *, tau=0.0, sigma=0.0,
+                 theta=1.0, data_term="l1", two_d=False, dtype=np.float64):
+    """Run the restated TGV2 loop.  Returns (u, v_x, v_y, v_z) shaped like f."""
+    f = np.ascontiguousarray(f, dtype=dtype)
+    w, h, d = _shape3(f)
+    u = np.empty_like(f)
+    vx, vy, vz = np.empty_like(f), np.empty_like(f), np.empty_like(f)
+    dt = 0 if data_term in ("l1", 0) else 1
+    getattr(lib(), f"oracle_tgv2_deshade_{_dt(dtype)}")(
+        f, w, h, d, lambda_, alpha0, alpha1, iterations, tau, sigma, theta, dt, int(two_d),
+        u, vx, vy, vz)
+    return u, vx, vy, vz
+
+
+def divergence(vx, vy, vz):
+    vx = np.ascontiguousarray(vx)
+    dtype = vx.dtype
+    vy = np.ascontiguousarray(vy, dtype=dtype)
+    vz = np.ascontiguousarray(vz if vz is not None else np.zeros_like(vx), dtype=dtype)
+    w, h, d = _shape3(vx)
+    out = np.empty_like(vx)
+    getattr(lib(), f"oracle_divergence_{_dt(dtype)}")(vx, vy, vz, w, h, d, out)
+    return out
+
+
+def _unary(name, x):
+    x = np.ascontiguousarray(x)
+    w, h, d = _shape3(x)
+    out = np.empty_like(x)
+    getattr(lib(), f"oracle_{name}_{_dt(x.dtype)}")(x, w, h, d, out)
+    return out
+
+
+def cosine_transform(x):
+    return _unary("cosine_transform", x)
+
+
+def inverse_cosine_transform(x):
+    return _unary("inverse_cosine_transform", x)
+
+
+def solve_poisson(x):
+    return _unary("solve_poisson", x)
+
+
+def integrate_poisson_dct(vx, vy, vz):
+    vx = np.ascontiguousarray(vx)
+    dtype = vx.dtype
+    vy = np.ascontiguousarray(vy, dtype=dtype)
+    vz = np.ascontiguousarray(vz if vz is not None else np.zeros_like(vx), dtype=dtype)
+    w, h, d = _shape3(vx)
+    out = np.empty_like(vx)
+    getattr(lib(), f"oracle_integrate_poisson_dct_{_dt(dtype)}")(vx, vy, vz, w, h, d, out)
+    return out
+
+
+def deshade_epilogue(u, l, mask=None, set_negative_values_to_zero=True, add_background_back=False):
+    """r = u - l, optional mask (also applied to l, returned), clamp, add-back."""
+    u = np.ascontiguousarray(u)
+    l = np.array(l, dtype=u.dtype, copy=True, order="C")
+    r = np.empty_like(u)
+    mptr = None
+    if mask is not None:
+        mask = np.ascontiguousarray(mask, dtype=u.dtype)
+        mptr = mask.ctypes.data_as(ctypes.c_void_p)
+    getattr(lib(), f"oracle_deshade_epilogue_{_dt(u.dtype)}")(
+        u, l, mptr, int(set_negative_values_to_zero), int(add_background_back), u.size, r)
+    return r, l
+
+
+def process_tgv2_l1(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *,
+                    set_negative_values_to_zero=True, data_term="l1", two_d=False,
+                    tau=0.0, sigma=0.0, dtype=np.float64):
+    """The whole deshade: loop, Poisson-DCT integration of v, r = u - l (+clamp).
+
+    Returns (denoised u, shading l, deshaded r) — the three images of
+    TGVDeshadeProcessor::processTGV2L1GPUCuda (TGVDeshadeProcessor.cpp:122-166).
+    """
+    u, vx, vy, vz = tgv2_deshade(f, lambda_, alpha0, alpha1, iterations, tau=tau, sigma=sigma,
+                                 data_term=data_term, two_d=two_d, dtype=dtype)
+    l = integrate_poisson_dct(vx, vy, vz)
+    r, _ = deshade_epilogue(u, l, None, set_negative_values_to_zero, False)
+    return u, l, r
+
+
+# ---------------------------------------------------------------------------
+# The reference's own kernels compiled for the CPU (available where they were built).
+
+def ref_available() -> bool:
+    return os.path.exists(_REF_PATH)
+
+
+def ref() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise FileNotFoundError(
+                "oracle/_ref/libref_cpu.so is missing; run oracle/ref_cpu/build_ref_cpu.py "
+                "where the reference sources are available")
+        R = ctypes.CDLL(_REF_PATH)
+        f = ctypes.c_float
+        R.ref_tgv2_l1_deshade_f32.argtypes = [_f32p, _u, _u, _u, f, f, f, _u, _f32p, _f32p,
+                                              _f32p, _f32p]
+        R.ref_tgv2_l1_deshade_2d_f32.argtypes = [_f32p, _u, _u, f, f, f, _u, _f32p, _f32p, _f32p]
+        R.ref_tgv2_denoise_f32.argtypes = [ctypes.c_int, _f32p, _u, _u, _u, f, f, f, _u, _f32p]
+        R.ref_process_tgv2_l1_f32.argtypes = [_f32p, _u, _u, _u, f, f, f, _u, ctypes.c_int,
+                                              _f32p, _f32p, _f32p]
+        for suf, p in (("f32", _f32p), ("f64", _f64p)):
+            getattr(R, f"ref_divergence_{suf}").argtypes = [p, p, p, _u, _u, _u, p]
+            for name in ("cosine_transform", "inverse_cosine_transform", "solve_poisson"):
+                getattr(R, f"ref_{name}_{suf}").argtypes = [p, _u, _u, _u, p]
+            getattr(R, f"ref_integrate_poisson_dct_{suf}").argtypes = [p, p, p, _u, _u, _u, p]
+        _ref = R
+    return _ref

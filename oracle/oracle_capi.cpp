@@ -1,0 +1,81 @@
+// TEST INFRASTRUCTURE — extern "C" entry points of the CPU oracle (tgv_oracle.hpp),
+// loaded by tests/ and bench.py's CPU-baseline leg through ctypes.  Not product code.
+#include "tgv_oracle.hpp"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using oracle::Dims;
+using oracle::index_t;
+
+namespace {
+oracle::Params make_params(double lambda, double alpha0, double alpha1, unsigned iterations,
+                           double tau, double sigma, double theta, int data_term, int two_d) {
+    oracle::Params p;
+    p.lambda = lambda;
+    p.alpha0 = alpha0;
+    p.alpha1 = alpha1;
+    p.iterations = iterations;
+    p.tau = tau;
+    p.sigma = sigma;
+    p.theta = theta;
+    p.data_term = data_term;
+    p.two_d = two_d != 0;
+    return p;
+}
+Dims dims(unsigned w, unsigned h, unsigned d) { return Dims{(index_t)w, (index_t)h, (index_t)d}; }
+}  // namespace
+
+extern "C" {
+
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+#define ORACLE_TYPED(T, SUF)                                                                      \
+    unsigned oracle_tgv2_deshade_##SUF(const T* f, unsigned w, unsigned h, unsigned d,            \
+                                       double lambda, double alpha0, double alpha1,               \
+                                       unsigned iterations, double tau, double sigma,             \
+                                       double theta, int data_term, int two_d, T* u, T* vx,       \
+                                       T* vy, T* vz) {                                            \
+        return oracle::tgv2_deshade<T>(f, dims(w, h, d),                                          \
+                                       make_params(lambda, alpha0, alpha1, iterations, tau,       \
+                                                   sigma, theta, data_term, two_d),               \
+                                       u, vx, vy, vz);                                            \
+    }                                                                                             \
+    void oracle_divergence_##SUF(const T* vx, const T* vy, const T* vz, unsigned w, unsigned h,   \
+                                 unsigned d, T* out) {                                            \
+        oracle::divergence<T>(vx, vy, vz, dims(w, h, d), out);                                    \
+    }                                                                                             \
+    void oracle_cosine_transform_##SUF(const T* in, unsigned w, unsigned h, unsigned d, T* out) { \
+        oracle::cosine_transform<T>(in, dims(w, h, d), out);                                      \
+    }                                                                                             \
+    void oracle_inverse_cosine_transform_##SUF(const T* in, unsigned w, unsigned h, unsigned d,   \
+                                               T* out) {                                          \
+        oracle::inverse_cosine_transform<T>(in, dims(w, h, d), out);                              \
+    }                                                                                             \
+    void oracle_solve_poisson_##SUF(const T* in, unsigned w, unsigned h, unsigned d, T* out) {    \
+        oracle::solve_poisson_in_cosine_domain<T>(in, dims(w, h, d), out);                        \
+    }                                                                                             \
+    void oracle_integrate_poisson_dct_##SUF(const T* vx, const T* vy, const T* vz, unsigned w,    \
+                                            unsigned h, unsigned d, T* l) {                       \
+        oracle::integrate_poisson_dct<T>(vx, vy, vz, dims(w, h, d), l);                           \
+    }                                                                                             \
+    void oracle_deshade_epilogue_##SUF(const T* u, T* l, const T* mask, int clamp, int add_back,  \
+                                       unsigned long long n, T* r) {                              \
+        oracle::deshade_epilogue<T>(u, l, mask, clamp != 0, add_back != 0, (index_t)n, r);        \
+    }
+
+ORACLE_TYPED(float, f32)
+ORACLE_TYPED(double, f64)
+
+#undef ORACLE_TYPED
+
+}  // extern "C"

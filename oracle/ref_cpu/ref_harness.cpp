@@ -1,0 +1,202 @@
+// TEST INFRASTRUCTURE — extern "C" driver around the reference's own launchers,
+// built for the CPU by build_ref_cpu.py (the launchers come from the reference's
+// unmodified .cu sources, compiled by g++ against shim/cuda.h).  The few lines of
+// ITK-level glue that call them are restated here from
+// source/modules/tgv_deshade/TGVDeshadeProcessor.cpp:122-166,386-408 and
+// source/modules/cuda_image_operations/CudaImageOperationsProcessor.cpp:286-294.
+#include <cstring>
+#include <functional>
+
+#include "cuda.h"
+
+uint3_ blockIdx;
+uint3_ threadIdx;
+dim3 blockDim;
+dim3 gridDim;
+
+template <typename Pixel>
+using DeshadeIterationCallback =
+    std::function<bool(uint, uint, Pixel*, Pixel*, Pixel*, Pixel*)>;
+template <typename Pixel>
+using DeshadeIterationCallback2D = std::function<bool(uint, uint, Pixel*, Pixel*, Pixel*)>;
+template <typename Pixel>
+using IterationCallback = std::function<bool(uint, uint, Pixel*)>;
+
+// Declarations of the reference's explicit instantiations.
+template <typename Pixel>
+Pixel* tgv2_l1_deshade_launch(Pixel* f_host, uint width, uint height, uint depth, Pixel lambda,
+                              uint iteration_count, uint paint_iteration_interval,
+                              const int cuda_block_dimension,
+                              DeshadeIterationCallback<Pixel> iteration_finished_callback,
+                              Pixel alpha0, Pixel alpha1, Pixel** v_x, Pixel** v_y, Pixel** v_z);
+template <typename Pixel>
+Pixel* tgv2_l1_deshade_launch_2d(Pixel* f_host, uint width, uint height, Pixel lambda,
+                                 uint iteration_count, uint paint_iteration_interval,
+                                 DeshadeIterationCallback2D<Pixel> iteration_finished_callback,
+                                 Pixel alpha0, Pixel alpha1, Pixel** v_x, Pixel** v_y);
+template <typename Pixel>
+Pixel* tgv2_l1_launch(Pixel* f_host, uint width, uint height, uint depth, Pixel lambda,
+                      uint iteration_count, uint paint_iteration_interval,
+                      IterationCallback<Pixel> iteration_finished_callback, Pixel alpha0,
+                      Pixel alpha1);
+template <typename Pixel>
+Pixel* tgv2_l2_launch(Pixel* f_host, uint width, uint height, uint depth, Pixel lambda,
+                      uint iteration_count, uint paint_iteration_interval,
+                      IterationCallback<Pixel> iteration_finished_callback, Pixel alpha0,
+                      Pixel alpha1);
+template <typename Pixel>
+Pixel* divergence_kernel_launch(Pixel* dx, Pixel* dy, Pixel* dz, const uint width,
+                                const uint height, const uint depth, bool is_host_data);
+template <typename Pixel>
+Pixel* divergence_2d_kernel_launch(Pixel* dx, Pixel* dy, const uint width, const uint height,
+                                   bool is_host_data);
+template <typename Pixel>
+Pixel* cosine_transform_kernel_launch(Pixel* image_host, uint width, uint height, uint depth);
+template <typename Pixel>
+Pixel* inverse_cosine_transform_kernel_launch(Pixel* image_host, uint width, uint height,
+                                              uint depth);
+template <typename Pixel>
+Pixel* solve_poisson_in_cosine_domain_kernel_launch(Pixel* image_host, uint width, uint height,
+                                                    uint depth);
+template <typename Pixel>
+Pixel* subtract_kernel_launch(Pixel* image1, Pixel* image2, uint width, uint height, uint depth);
+template <typename Pixel>
+Pixel* clamp_negative_values_kernel_launch(Pixel* image, uint width, uint height, uint depth,
+                                           Pixel value);
+
+namespace {
+template <class P>
+void take(P* src, P* dst, size_t n) {
+    std::memcpy(dst, src, sizeof(P) * n);
+    delete[] src;
+}
+
+// CudaImageOperationsProcessor::divergence: depth == 1 goes to the 2-D kernels.
+template <class P>
+P* divergence_any(P* vx, P* vy, P* vz, uint w, uint h, uint d) {
+    if (d == 1) return divergence_2d_kernel_launch<P>(vx, vy, w, h, true);
+    return divergence_kernel_launch<P>(vx, vy, vz, w, h, d, true);
+}
+
+// integrate_image_gradients_poisson_cosine_transform (TGVDeshadeProcessor.cpp:386-408)
+template <class P>
+P* integrate(P* vx, P* vy, P* vz, uint w, uint h, uint d) {
+    P* div = divergence_any<P>(vx, vy, vz, w, h, d);
+    P* dct = cosine_transform_kernel_launch<P>(div, w, h, d);
+    delete[] div;
+    P* sol = solve_poisson_in_cosine_domain_kernel_launch<P>(dct, w, h, d);
+    delete[] dct;
+    P* l = inverse_cosine_transform_kernel_launch<P>(sol, w, h, d);
+    delete[] sol;
+    return l;
+}
+}  // namespace
+
+extern "C" {
+
+// tgv2_l1_deshade_launch<float> as TGVDeshadeProcessor.cpp:137-145 calls it
+// (paint interval = iterations + 1, so no callback).
+void ref_tgv2_l1_deshade_f32(const float* f, uint w, uint h, uint d, float lambda, float alpha0,
+                             float alpha1, uint iterations, float* u, float* vx, float* vy,
+                             float* vz) {
+    const size_t n = (size_t)w * h * d;
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    float *ox, *oy, *oz;
+    float* ou = tgv2_l1_deshade_launch<float>(fin, w, h, d, lambda, iterations, iterations + 1,
+                                              -1, nullptr, alpha0, alpha1, &ox, &oy, &oz);
+    delete[] fin;
+    take(ou, u, n);
+    take(ox, vx, n);
+    take(oy, vy, n);
+    take(oz, vz, n);
+}
+
+void ref_tgv2_l1_deshade_2d_f32(const float* f, uint w, uint h, float lambda, float alpha0,
+                                float alpha1, uint iterations, float* u, float* vx, float* vy) {
+    const size_t n = (size_t)w * h;
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    float *ox, *oy;
+    float* ou = tgv2_l1_deshade_launch_2d<float>(fin, w, h, lambda, iterations, iterations + 1,
+                                                 nullptr, alpha0, alpha1, &ox, &oy);
+    delete[] fin;
+    take(ou, u, n);
+    take(ox, vx, n);
+    take(oy, vy, n);
+}
+
+// The TGV filter's denoise launchers (tgv_cuda/tgv2_l1.cu:64, tgv_cuda/tgv2_l2.cu:60).
+void ref_tgv2_denoise_f32(int data_term, const float* f, uint w, uint h, uint d, float lambda,
+                          float alpha0, float alpha1, uint iterations, float* u) {
+    const size_t n = (size_t)w * h * d;
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    float* ou = data_term == 0
+                    ? tgv2_l1_launch<float>(fin, w, h, d, lambda, iterations, iterations + 1,
+                                            nullptr, alpha0, alpha1)
+                    : tgv2_l2_launch<float>(fin, w, h, d, lambda, iterations, iterations + 1,
+                                            nullptr, alpha0, alpha1);
+    delete[] fin;
+    take(ou, u, n);
+}
+
+#define REF_TYPED(P, SUF)                                                                        \
+    void ref_divergence_##SUF(const P* vx, const P* vy, const P* vz, uint w, uint h, uint d,    \
+                              P* out) {                                                          \
+        const size_t n = (size_t)w * h * d;                                                      \
+        P* r = divergence_any<P>(const_cast<P*>(vx), const_cast<P*>(vy), const_cast<P*>(vz), w, \
+                                 h, d);                                                          \
+        take(r, out, n);                                                                         \
+    }                                                                                            \
+    void ref_cosine_transform_##SUF(const P* in, uint w, uint h, uint d, P* out) {               \
+        take(cosine_transform_kernel_launch<P>(const_cast<P*>(in), w, h, d), out,                \
+             (size_t)w * h * d);                                                                 \
+    }                                                                                            \
+    void ref_inverse_cosine_transform_##SUF(const P* in, uint w, uint h, uint d, P* out) {       \
+        take(inverse_cosine_transform_kernel_launch<P>(const_cast<P*>(in), w, h, d), out,        \
+             (size_t)w * h * d);                                                                 \
+    }                                                                                            \
+    void ref_solve_poisson_##SUF(const P* in, uint w, uint h, uint d, P* out) {                  \
+        take(solve_poisson_in_cosine_domain_kernel_launch<P>(const_cast<P*>(in), w, h, d), out,  \
+             (size_t)w * h * d);                                                                 \
+    }                                                                                            \
+    void ref_integrate_poisson_dct_##SUF(const P* vx, const P* vy, const P* vz, uint w, uint h, \
+                                         uint d, P* out) {                                       \
+        take(integrate<P>(const_cast<P*>(vx), const_cast<P*>(vy), const_cast<P*>(vz), w, h, d), \
+             out, (size_t)w * h * d);                                                            \
+    }
+
+REF_TYPED(float, f32)
+REF_TYPED(double, f64)
+#undef REF_TYPED
+
+// TGVDeshadeProcessor::processTGV2L1GPUCuda, the terminal-program overload
+// (TGVDeshadeProcessor.cpp:122-166) with no mask and set_negative_values_to_zero
+// as the CLI passes it (terminal_programs/tgv2_deshade_main.cpp:57-68).
+void ref_process_tgv2_l1_f32(const float* f, uint w, uint h, uint d, float lambda, float alpha0,
+                             float alpha1, uint iterations, int set_negative_values_to_zero,
+                             float* denoised, float* shading, float* deshaded) {
+    const size_t n = (size_t)w * h * d;
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    float *vx, *vy, *vz;
+    float* u = tgv2_l1_deshade_launch<float>(fin, w, h, d, lambda, iterations, iterations + 1, -1,
+                                             nullptr, alpha0, alpha1, &vx, &vy, &vz);
+    delete[] fin;
+    float* l = integrate<float>(vx, vy, vz, w, h, d);
+    delete[] vx;
+    delete[] vy;
+    delete[] vz;
+    float* r = subtract_kernel_launch<float>(u, l, w, h, d);
+    if (set_negative_values_to_zero) {
+        float* r2 = clamp_negative_values_kernel_launch<float>(r, w, h, d, 0.0f);
+        delete[] r;
+        r = r2;
+    }
+    take(u, denoised, n);
+    take(l, shading, n);
+    take(r, deshaded, n);
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+"""Generates tests/golden/*.npz from the reference's own kernels.
+
+Each fixture holds seeded inputs and the outputs of the reference's CUDA sources
+(source/modules/tgv_deshade, tgv_cuda, cuda_image_operations) compiled for the
+CPU by oracle/ref_cpu/build_ref_cpu.py and run in the build container, where the
+reference tree is available.  The GPU machine never runs this script; tests there
+read the committed .npz files.
+
+    python oracle/ref_cpu/build_ref_cpu.py && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from ambient_image_processor_gb300.phantoms import (  # noqa: E402
+    rectangles_ellipses_2d, tissue_phantom_3d)
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+# (name, shape (D,H,W), seed, lambda, alpha0, alpha1, iterations)
+DESHADE_3D = [
+    ("deshade3d", (8, 12, 16), 11, 1.0, 2.0, 1.0, 60),
+    ("deshade3d_odd", (9, 13, 17), 12, 0.7, 1.5, 0.8, 45),
+    ("deshade3d_d1", (1, 24, 32), 13, 1.0, 2.0, 1.0, 50),
+    ("deshade3d_h1", (5, 1, 7), 14, 1.0, 2.0, 1.0, 30),
+    ("deshade3d_w1", (6, 9, 1), 15, 1.0, 2.0, 1.0, 30),
+    ("deshade3d_tiny", (2, 2, 2), 16, 1.0, 2.0, 1.0, 10),
+]
+DESHADE_2D = [
+    ("deshade2d", (28, 40), 21, 1.0, 2.0, 1.0, 60),
+    ("deshade2d_odd", (19, 23), 22, 0.5, 3.0, 1.5, 40),
+]
+DENOISE = [  # (name, data term, shape, seed, lambda, alpha0, alpha1, iterations)
+    ("denoise_l1", 0, (7, 11, 13), 31, 0.9, 1.7, 1.1, 50),
+    ("denoise_l2", 1, (7, 11, 13), 32, 0.9, 1.7, 1.1, 50),
+    ("denoise_l2_d1", 1, (1, 16, 20), 33, 0.9, 1.7, 1.1, 50),
+]
+DCT_SHAPES = [(10, 12, 16), (1, 18, 24), (5, 7, 1), (1, 1, 9), (3, 1, 1), (4, 4, 4)]
+PROCESS = [("process3d", (8, 12, 16), 41, 1.0, 2.0, 1.0, 40),
+           ("process3d_d1", (1, 20, 24), 42, 1.0, 2.0, 1.0, 40)]
+
+
+def empties(f, k):
+    return [np.empty_like(f) for _ in range(k)]
+
+
+def main() -> int:
+    R = oracle.ref()
+    cases = {}
+    for name, shape, seed, lam, a0, a1, it in DESHADE_3D:
+        f = tissue_phantom_3d(*shape, seed=seed)
+        d, h, w = shape
+        u, vx, vy, vz = empties(f, 4)
+        R.ref_tgv2_l1_deshade_f32(f, w, h, d, lam, a0, a1, it, u, vx, vy, vz)
+        cases[name] = dict(f=f, u=u, v_x=vx, v_y=vy, v_z=vz,
+                           params=np.array([lam, a0, a1, it], np.float64))
+    for name, shape, seed, lam, a0, a1, it in DESHADE_2D:
+        f = rectangles_ellipses_2d(*shape, seed=seed)
+        h, w = shape
+        u, vx, vy = empties(f, 3)
+        R.ref_tgv2_l1_deshade_2d_f32(f, w, h, lam, a0, a1, it, u, vx, vy)
+        cases[name] = dict(f=f, u=u, v_x=vx, v_y=vy, params=np.array([lam, a0, a1, it], np.float64))
+    for name, dt, shape, seed, lam, a0, a1, it in DENOISE:
+        f = tissue_phantom_3d(*shape, seed=seed)
+        d, h, w = shape
+        (u,) = empties(f, 1)
+        R.ref_tgv2_denoise_f32(dt, f, w, h, d, lam, a0, a1, it, u)
+        cases[name] = dict(f=f, u=u, data_term=np.array(dt), params=np.array([lam, a0, a1, it]))
+    rng = np.random.default_rng(51)
+    for shape in DCT_SHAPES:
+        d, h, w = shape
+        tag = "x".join(str(s) for s in shape)
+        for dtype, suf in ((np.float32, "f32"), (np.float64, "f64")):
+            x = rng.standard_normal(shape).astype(dtype)
+            vx, vy, vz = (rng.standard_normal(shape).astype(dtype) for _ in range(3))
+            c = dict(x=x, v_x=vx, v_y=vy, v_z=vz)
+            for op in ("cosine_transform", "inverse_cosine_transform", "solve_poisson"):
+                out = np.empty_like(x)
+                getattr(R, f"ref_{op}_{suf}")(x, w, h, d, out)
+                c[op] = out
+            out = np.empty_like(x)
+            getattr(R, f"ref_divergence_{suf}")(vx, vy, vz, w, h, d, out)
+            c["divergence"] = out
+            out = np.empty_like(x)
+            getattr(R, f"ref_integrate_poisson_dct_{suf}")(vx, vy, vz, w, h, d, out)
+            c["integrate"] = out
+            cases[f"dct_{tag}_{suf}"] = c
+    for name, shape, seed, lam, a0, a1, it in PROCESS:
+        f = tissue_phantom_3d(*shape, seed=seed)
+        d, h, w = shape
+        u, l, r = empties(f, 3)
+        R.ref_process_tgv2_l1_f32(f, w, h, d, lam, a0, a1, it, 1, u, l, r)
+        cases[name] = dict(f=f, denoised=u, shading=l, deshaded=r,
+                           params=np.array([lam, a0, a1, it], np.float64))
+    for name, c in cases.items():
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **c)
+    print(f"wrote {len(cases)} fixtures to {OUT}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
