@@ -152,15 +152,21 @@ def test_2d_geometry_differs_from_3d_on_depth_one(gpu_lib):
     assert np.abs(u3[0] - u2).max() > 1e-3 and np.abs(vz3).max() > 1e-3
 
 
-@pytest.mark.parametrize("prec", [pkg.STATE_BF16_DUAL, pkg.STATE_FX16_DUAL])
-def test_mixed_precision_state_close_to_fp64(gpu_lib, prec):
+# Relative L2 error of u and r against the FP64 oracle after 100 iterations of a
+# 24x32x40 phantom, per state precision (BF16 keeps 8 mantissa bits of p and q; the
+# 16-bit fixed point keeps 15 bits of p/alpha1 and q/alpha0).
+MIXED_TOL = {pkg.STATE_FP32: 1e-5, pkg.STATE_BF16_DUAL: 5e-3, pkg.STATE_FX16_DUAL: 2e-4}
+
+
+@pytest.mark.parametrize("prec", [pkg.STATE_FP32, pkg.STATE_BF16_DUAL, pkg.STATE_FX16_DUAL])
+def test_state_precision_error_vs_fp64(gpu_lib, prec):
     f = tissue_phantom_3d(24, 32, 40, seed=10)
     u, l, r = pkg.TGVDeshadeProcessor.processTGV2L1GPUCuda(f, 1.0, 2.0, 1.0, 100,
                                                            state_precision=prec,
                                                            poisson_eigen=pkg.EIGEN_ACCURATE)
     ou, ol, orr = oracle.process_tgv2_l1(f, 1.0, 2.0, 1.0, 100, dtype=np.float64)
-    assert rel_l2(u, ou) < 1e-3
-    assert rel_l2(r, orr) < 1e-3
+    assert rel_l2(u, ou) < MIXED_TOL[prec]
+    assert rel_l2(r, orr) < MIXED_TOL[prec]
 
 
 def test_bad_arguments_raise(gpu_lib):
