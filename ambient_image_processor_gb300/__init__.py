@@ -84,6 +84,8 @@ _SIGS = {
     "tgvdct_integrate_image_gradients_poisson_cosine_transform": [_f32p, _f32p, _vp, _u32, _u32,
                                                                   _u32, _i32, _i32, _f32p],
     "tgvdct_poisson_integrate_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "tgvdct_integrate_poisson_noalloc_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _i32, _i32, _vp,
+                                             _vp],
     "tgvdct_deshade_epilogue_dev": [_vp, _vp, _vp, ctypes.c_uint64, _i32, _i32, _i32, _vp, _vp],
     "tgvdct_process_tgv2_l1": [ctypes.POINTER(Params), _f32p, _vp, _i32, _i32, _i32, CALLBACK,
                                _vp, _f32p, _f32p, _f32p],

@@ -32,6 +32,7 @@ UNITS = {
     "tgv_kernels.cu": ["-fmad=false"],
     "dct_kernels.cu": [],
     "capi.cu": [],
+    "noalloc.cu": [],
 }
 
 

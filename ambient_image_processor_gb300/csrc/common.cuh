@@ -71,7 +71,16 @@ void tgv_iterate(const TgvState& s, const TgvStep& k, cudaStream_t st);
 int tgv_kernels_per_iteration();
 
 // ---- Poisson integration -------------------------------------------------------
-struct DctPlan;  // per-shape cosine tables and scratch
+// Per-shape cosine tables and scratch of the Poisson integration.
+struct DctPlan {
+    int W = 0, H = 0, D = 0;
+    float* fwd[3] = {nullptr, nullptr, nullptr};   // C (N x N) per axis
+    float* inv[3] = {nullptr, nullptr, nullptr};   // S (N x N) per axis
+    float* cosk[3] = {nullptr, nullptr, nullptr};  // cospif(k / N), device-evaluated
+    float* eig[3] = {nullptr, nullptr, nullptr};   // 4 sin^2(pi k / 2N)
+    float* tmp[2] = {nullptr, nullptr};            // two V-sized scratch volumes
+    void* block = nullptr;                         // owning allocation (null for views)
+};
 DctPlan* dct_plan_create(int W, int H, int D);
 void dct_plan_destroy(DctPlan* p);
 size_t dct_plan_bytes(int W, int H, int D);

@@ -25,17 +25,6 @@
 
 namespace tgvdct {
 
-// ---- per-shape plan: cosine matrices and scratch ------------------------------------
-struct DctPlan {
-    int W = 0, H = 0, D = 0;
-    float* fwd[3] = {nullptr, nullptr, nullptr};   // C (N x N) per axis
-    float* inv[3] = {nullptr, nullptr, nullptr};   // S (N x N) per axis
-    float* cosk[3] = {nullptr, nullptr, nullptr};  // cospif(k / N), device-evaluated
-    float* eig[3] = {nullptr, nullptr, nullptr};   // 4 sin^2(pi k / 2N)
-    float* tmp[2] = {nullptr, nullptr};            // two V-sized scratch volumes
-    void* block = nullptr;
-};
-
 namespace {
 
 double cospi_host(double a) {

@@ -200,6 +200,28 @@ tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* ctx, const float* v_x
                                            const float* v_y_dev, const float* v_z_dev,
                                            float* l_dev, void* stream);
 
+/* Allocation-free form of tgvdct_poisson_integrate_dev.  It has no counterpart in
+   the reference.  It is for callers that must not allocate device memory while
+   they run (their memory manager owns the GPU, their footprint is fixed in
+   advance, or a cudaMalloc/cudaFree would synchronise a latency-critical
+   pipeline): it calls no cudaMalloc, cudaFree or other allocating routine.  Its
+   scratch is one static device array of the library (about 18 MB, held by every
+   GPU that loads the library until the process exits), which limits the volume
+   to TGVDCT_NOALLOC_MAX_VOXELS voxels with every side <= TGVDCT_NOALLOC_MAX_SIDE;
+   larger volumes are rejected with TGVDCT_ERR_BAD_ARG.  The first call on each
+   device looks up the array's device address (make that first call before any
+   stream capture).  All calls share the one array: calls that overlap on the
+   GPU (different streams, no ordering between them) race and corrupt each
+   other's results, so order them, e.g. on one stream.  The caller passes v on
+   the device (v_z_dev may be NULL when depth == 1) and the output l_dev. */
+#define TGVDCT_NOALLOC_MAX_VOXELS (1u << 21)
+#define TGVDCT_NOALLOC_MAX_SIDE 256u
+tgvdct_status tgvdct_integrate_poisson_noalloc_dev(const float* v_x_dev, const float* v_y_dev,
+                                                   const float* v_z_dev, uint32_t width,
+                                                   uint32_t height, uint32_t depth,
+                                                   int32_t dct_mode, int32_t poisson_eigen,
+                                                   float* l_dev, void* stream);
+
 /* ---- deshade epilogue and the whole processor ----------------------------- */
 /* Device form of TGVDeshadeProcessor::deshade_poisson_cosine_transform's tail
    (TGVDeshadeProcessor.cpp:83-92) plus the background add-back (:275-279):
