@@ -25,6 +25,7 @@ GEOMETRY_3D, GEOMETRY_2D = 0, 1
 STATE_FP32, STATE_BF16_DUAL, STATE_FX16_DUAL = 0, 1, 2
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 EIGEN_REFERENCE, EIGEN_ACCURATE = 0, 1
+KERNEL_AUTO, KERNEL_TWO_PASS, KERNEL_FUSED = 0, 1, 2
 
 _STATUS_NAMES = {OK: "ok", ERR_BAD_ARG: "bad argument", ERR_OOM: "out of memory",
                  ERR_CUDA: "CUDA error", ERR_NO_DEVICE: "no suitable CUDA device",
@@ -48,7 +49,8 @@ class Params(ctypes.Structure):
                 ("state_precision", ctypes.c_int32), ("dct_mode", ctypes.c_int32),
                 ("poisson_eigen", ctypes.c_int32),
                 ("paint_iteration_interval", ctypes.c_uint32),
-                ("callback_on_device", ctypes.c_int32)]
+                ("callback_on_device", ctypes.c_int32),
+                ("iteration_kernel", ctypes.c_int32), ("z_chunk", ctypes.c_int32)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
@@ -84,6 +86,8 @@ _SIGS = {
     "tgvdct_integrate_image_gradients_poisson_cosine_transform": [_f32p, _f32p, _vp, _u32, _u32,
                                                                   _u32, _i32, _i32, _f32p],
     "tgvdct_poisson_integrate_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "tgvdct_poisson_solve_dev": [_vp, _vp, _vp, _vp],
+    "tgvdct_check_device_error": [_vp, _vp],
     "tgvdct_integrate_poisson_noalloc_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _i32, _i32, _vp,
                                              _vp],
     "tgvdct_deshade_epilogue_dev": [_vp, _vp, _vp, ctypes.c_uint64, _i32, _i32, _i32, _vp, _vp],
@@ -294,7 +298,8 @@ class TGVDeshadeProcessor:
                              iteration_finished_callback=None, add_background_back=False,
                              log_domain=False, data_term=DATA_L1, two_d=False,
                              state_precision=STATE_FP32, dct_mode=DCT_FP32,
-                             poisson_eigen=EIGEN_REFERENCE, tau=None, sigma=None):
+                             poisson_eigen=EIGEN_REFERENCE, tau=None, sigma=None,
+                             iteration_kernel=KERNEL_AUTO, z_chunk=0):
         """TGVDeshadeProcessor::processTGV2L1GPUCuda (TGVDeshadeProcessor.cpp:122-166; the
         GUI overload with mask, callback and add-back: :285-314).
 
@@ -310,7 +315,8 @@ class TGVDeshadeProcessor:
                            geometry=GEOMETRY_2D if two_d else GEOMETRY_3D,
                            state_precision=state_precision, dct_mode=dct_mode,
                            poisson_eigen=poisson_eigen,
-                           paint_iteration_interval=paint_iteration_interval)
+                           paint_iteration_interval=paint_iteration_interval,
+                           iteration_kernel=iteration_kernel, z_chunk=z_chunk)
         if tau is not None:
             p.tau = tau
         if sigma is not None:
@@ -376,6 +382,13 @@ class Context:
     def poisson_integrate_dev(self, vx_ptr, vy_ptr, vz_ptr, l_ptr, stream=None):
         _check(lib().tgvdct_poisson_integrate_dev(self._ctx, vx_ptr, vy_ptr, vz_ptr, l_ptr,
                                                   stream), allow_stop=False)
+
+    def poisson_solve_dev(self, rhs_ptr, l_ptr, stream=None):
+        _check(lib().tgvdct_poisson_solve_dev(self._ctx, rhs_ptr, l_ptr, stream),
+               allow_stop=False)
+
+    def check_device_error(self, stream=None):
+        _check(lib().tgvdct_check_device_error(self._ctx, stream), allow_stop=False)
 
     def process_dev(self, f_ptr, u_ptr, l_ptr, r_ptr, mask_ptr=None,
                     set_negative_values_to_zero=True, add_background_back=False,

@@ -33,6 +33,7 @@ UNITS = {
     "dct_kernels.cu": [],
     "capi.cu": [],
     "noalloc.cu": [],
+    "dct_tc.cu": [],
 }
 
 

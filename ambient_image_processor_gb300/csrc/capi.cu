@@ -59,6 +59,27 @@ void validate(const tgvdct_params* p) {
     TGV_REQUIRE(std::isfinite(p->tau) && p->tau > 0.f, "tau must be > 0");
     TGV_REQUIRE(std::isfinite(p->sigma) && p->sigma > 0.f, "sigma must be > 0");
     TGV_REQUIRE(std::isfinite(p->theta), "theta must be finite");
+    TGV_REQUIRE(p->iteration_kernel >= TGVDCT_KERNEL_AUTO &&
+                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED,
+                "unknown iteration kernel");
+    TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
+}
+
+int kernel_of(const tgvdct_params& p) {
+    return p.iteration_kernel == TGVDCT_KERNEL_TWO_PASS ? TGV_KERNEL_TWO_PASS : TGV_KERNEL_FUSED;
+}
+
+// Planes per block of the fused kernel: enough blocks to fill the GPU a few
+// times over, few enough that the one-plane prologue of each chunk stays small.
+int auto_zchunk(const tgvdct_params& p) {
+    if (p.z_chunk > 0) return (int)p.z_chunk;
+    const long long tiles = (long long)((p.width + 31) / 32) * ((p.height + 7) / 8);
+    const long long target_blocks = 152LL * 3 * 4;  // ~4 waves of 3 blocks per SM
+    long long chunks = (target_blocks + tiles - 1) / tiles;
+    if (chunks < 1) chunks = 1;
+    long long z = ((long long)p.depth + chunks - 1) / chunks;
+    if (z < 16) z = 16;
+    return (int)z;
 }
 
 void check_device() {
@@ -175,7 +196,10 @@ void create_into(const tgvdct_params* p, tgvdct_context** out) {
     c->st.D = (int)p->depth;
     c->st.three = p->geometry == TGVDCT_GEOMETRY_3D;
     c->st.precision = p->state_precision;
-    const size_t bytes = tgv_state_bytes(c->st.W, c->st.H, c->st.D, c->st.three, c->st.precision);
+    c->st.kernel = kernel_of(*p);
+    c->st.zchunk = auto_zchunk(*p);
+    const size_t bytes = tgv_state_bytes(c->st.W, c->st.H, c->st.D, c->st.three, c->st.precision,
+                                         c->st.kernel);
     cudaError_t e = cudaMalloc(&c->state_block, bytes);
     if (e != cudaSuccess) {
         delete c;
@@ -257,6 +281,10 @@ tgvdct_status with_plan(uint32_t w, uint32_t h, uint32_t d, Body&& body) {
         } pg{plan};
         body(plan, (size_t)w * h * d);
         TGV_CUDA(cudaStreamSynchronize(0));
+        if (!dct_tc_check(plan, 0)) {
+            set_error("a tensor-core DCT pass timed out waiting on its pipeline");
+            return TGVDCT_ERR_CUDA;
+        }
         return TGVDCT_OK;
     });
 }
@@ -303,7 +331,8 @@ void tgvdct_params_init(tgvdct_params* p) {
 size_t tgvdct_workspace_bytes(const tgvdct_params* p) {
     if (!p) return 0;
     return tgv_state_bytes((int)p->width, (int)p->height, (int)p->depth,
-                           p->geometry == TGVDCT_GEOMETRY_3D, p->state_precision) +
+                           p->geometry == TGVDCT_GEOMETRY_3D, p->state_precision,
+                           kernel_of(*p)) +
            dct_plan_bytes((int)p->width, (int)p->height, (int)p->depth);
 }
 
@@ -327,9 +356,11 @@ tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p) {
                         p->depth == ctx->prm.depth,
                     "set_params cannot change the shape");
         TGV_REQUIRE(p->geometry == ctx->prm.geometry &&
-                        p->state_precision == ctx->prm.state_precision,
-                    "set_params cannot change geometry or state precision");
+                        p->state_precision == ctx->prm.state_precision &&
+                        kernel_of(*p) == kernel_of(ctx->prm),
+                    "set_params cannot change geometry, state precision or iteration kernel");
         ctx->prm = *p;
+        ctx->st.zchunk = auto_zchunk(*p);
         return TGVDCT_OK;
     });
 }
@@ -543,6 +574,29 @@ tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* c, const float* v_x_d
                     "null device buffer");
         poisson_integrate(plan_of(c), v_x_dev, v_y_dev, v_z_dev, l_dev, c->prm.dct_mode,
                           c->prm.poisson_eigen, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* c, const float* rhs_dev, float* l_dev,
+                                       void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(rhs_dev && l_dev, "null device buffer");
+        poisson_solve(plan_of(c), rhs_dev, l_dev, c->prm.dct_mode, c->prm.poisson_eigen,
+                      (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_check_device_error(tgvdct_context* c, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        if (c->plan && !dct_tc_check(c->plan, (cudaStream_t)stream)) {
+            set_error("a tensor-core DCT pass timed out waiting on its pipeline");
+            return TGVDCT_ERR_CUDA;
+        }
+        TGV_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
         return TGVDCT_OK;
     });
 }

@@ -39,20 +39,33 @@ struct Error {
     } while (0)
 
 // ---- TGV2 loop ---------------------------------------------------------------
+// The fields an iteration reads with a stencil: ubar, vbar, p, q.  p (3 or 2
+// components) and q (6 or 3) are stored in the state precision's element type.
+struct TgvStencilFields {
+    float* ubar = nullptr;
+    float* vbar[3] = {nullptr, nullptr, nullptr};
+    void* p[3] = {nullptr, nullptr, nullptr};
+    void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
+};
+
+enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2 };
+
 // Device state of one volume.  Fields are planar (structure of arrays), x fastest.
-// p (3 or 2 components) and q (6 or 3) are stored in the state precision's
-// element type; everything else in FP32.
+// The two-pass kernels update set[0] in place.  The fused kernel reads set[cur]
+// and writes set[cur ^ 1] (its halo recompute reads neighbours another block may
+// already have advanced), so it needs the second set.
 struct TgvState {
     int W = 0, H = 0, D = 0;
     bool three = true;       // 3-D operators (also for D == 1) vs the 2-D launcher
     int precision = TGVDCT_STATE_FP32;
+    int kernel = TGV_KERNEL_FUSED;
+    int zchunk = 32;         // planes per block of the fused kernel
     float* u = nullptr;
-    float* ubar = nullptr;
     float* f = nullptr;      // private copy of the input (log-domain runs rewrite it)
     float* v[3] = {nullptr, nullptr, nullptr};
-    float* vbar[3] = {nullptr, nullptr, nullptr};
-    void* p[3] = {nullptr, nullptr, nullptr};
-    void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
+    TgvStencilFields set[2];
+    int cur = 0;
+    const TgvStencilFields& now() const { return set[cur]; }
 };
 
 struct TgvStep {
@@ -60,15 +73,15 @@ struct TgvStep {
     int data_term;
 };
 
-size_t tgv_state_bytes(int W, int H, int D, bool three, int precision);
+size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kernel);
 // Carves the state out of `base` (aligned to 256 bytes per field).
 void tgv_state_bind(TgvState& s, char* base);
 // u = ubar = f, p = q = v = vbar = 0.
-void tgv_state_init(const TgvState& s, cudaStream_t st);
-// One primal-dual iteration: the dual pass, then the primal pass.
-void tgv_iterate(const TgvState& s, const TgvStep& k, cudaStream_t st);
+void tgv_state_init(TgvState& s, cudaStream_t st);
+// One primal-dual iteration (advances s.cur for the fused kernel).
+void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.
-int tgv_kernels_per_iteration();
+int tgv_kernels_per_iteration(const TgvState& s);
 
 // ---- Poisson integration -------------------------------------------------------
 // Per-shape cosine tables and scratch of the Poisson integration.
@@ -80,7 +93,26 @@ struct DctPlan {
     float* eig[3] = {nullptr, nullptr, nullptr};   // 4 sin^2(pi k / 2N)
     float* tmp[2] = {nullptr, nullptr};            // two V-sized scratch volumes
     void* block = nullptr;                         // owning allocation (null for views)
+    // tensor-core operands (sides <= 256): per axis, forward and inverse matrices
+    // as BF16 hi/lo pairs and as TF32-rounded FP32, row-major N x N
+    uint16_t* bf_hi[2][3] = {};                    // [fwd, inv][axis]
+    uint16_t* bf_lo[2][3] = {};
+    float* tf[2][3] = {};
+    int* dev_err = nullptr;                        // set by a tensor-core pass whose wait timed out
+    void* tc_block = nullptr;
 };
+// Tensor-core passes need every side <= 256.
+bool dct_tc_supported(const DctPlan* p);
+// Prepares the tensor-core operands of a plan (allocates them once).
+void dct_plan_prepare_tc(DctPlan* p);
+// Reads (and clears) the device error flag of the tensor-core passes; synchronises.
+bool dct_tc_check(DctPlan* p, cudaStream_t st);
+// One separable pass on the tensor cores; epi: 0 none, 1 scale, 2/3 Poisson division
+// (reference / accurate eigenvalues) on the last forward pass; div: the operand is
+// the divergence of (vx, vy, vz) (x pass).
+void pass_tc(DctPlan* p, int axis, bool inverse, const float* in, float* out, int epi, float scale,
+             bool div, const float* vx, const float* vy, const float* vz, int dct_mode,
+             cudaStream_t st);
 DctPlan* dct_plan_create(int W, int H, int D);
 void dct_plan_destroy(DctPlan* p);
 size_t dct_plan_bytes(int W, int H, int D);
@@ -88,6 +120,9 @@ size_t dct_plan_bytes(int W, int H, int D);
 // l = DCT-III( DCT-II(div v) / eigenvalue ) with the reference's scale factors.
 void poisson_integrate(DctPlan* plan, const float* vx, const float* vy, const float* vz,
                        float* l, int dct_mode, int eigen_mode, cudaStream_t st);
+// l = DCT-III( DCT-II(rhs) / eigenvalue ): the Poisson solve of a given right-hand side.
+void poisson_solve(DctPlan* plan, const float* rhs, float* l, int dct_mode, int eigen_mode,
+                   cudaStream_t st);
 // The separate steps of the reference's CudaImageOperationsProcessor.
 void divergence(DctPlan* plan, const float* vx, const float* vy, const float* vz, float* out,
                 cudaStream_t st);

@@ -425,6 +425,7 @@ DctPlan* dct_plan_create(int W, int H, int D) {
 
 void dct_plan_destroy(DctPlan* p) {
     if (!p) return;
+    if (p->tc_block) cudaFree(p->tc_block);
     cudaFree(p->block);
     delete p;
 }
@@ -436,29 +437,51 @@ void divergence(DctPlan* p, const float* vx, const float* vy, const float* vz, f
     TGV_CHECK_LAUNCH();
 }
 
-void cosine_transform(DctPlan* p, const float* in, float* out, int dct_mode, cudaStream_t st) {
-    TGV_REQUIRE(dct_mode == TGVDCT_DCT_FP32, "this DCT mode is not built");
-    if (p->D == 1) {
-        pass(p, 0, p->fwd[0], in, p->tmp[0], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->fwd[1], p->tmp[0], out, EPI_SCALE, 8.f, A_PLAIN, 0, 0, 0, st);
+// A separable pass on the CUDA cores (FP32) or the tensor cores (dct_tc.cu).
+void any_pass(DctPlan* p, int axis, bool inverse, const float* in, float* out, int epi, float scale,
+              int dct_mode, cudaStream_t st) {
+    if (dct_mode == TGVDCT_DCT_FP32) {
+        pass(p, axis, inverse ? p->inv[axis] : p->fwd[axis], in, out, epi, scale, A_PLAIN, 0, 0, 0,
+             st);
     } else {
-        pass(p, 0, p->fwd[0], in, p->tmp[0], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->fwd[1], p->tmp[0], p->tmp[1], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 2, p->fwd[2], p->tmp[1], out, EPI_SCALE, 8.f, A_PLAIN, 0, 0, 0, st);
+        pass_tc(p, axis, inverse, in, out, epi, scale, false, nullptr, nullptr, nullptr, dct_mode,
+                st);
+    }
+}
+
+void check_mode(DctPlan* p, int dct_mode) {
+    TGV_REQUIRE(dct_mode == TGVDCT_DCT_FP32 || dct_mode == TGVDCT_DCT_TF32 ||
+                    dct_mode == TGVDCT_DCT_BF16X3,
+                "unknown DCT mode");
+    if (dct_mode != TGVDCT_DCT_FP32 && !dct_tc_supported(p)) {
+        set_error("tensor-core DCT modes need every side <= 256");
+        throw Error{TGVDCT_ERR_UNSUPPORTED};
+    }
+}
+
+void cosine_transform(DctPlan* p, const float* in, float* out, int dct_mode, cudaStream_t st) {
+    check_mode(p, dct_mode);
+    if (p->D == 1) {
+        any_pass(p, 0, false, in, p->tmp[0], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, false, p->tmp[0], out, EPI_SCALE, 8.f, dct_mode, st);
+    } else {
+        any_pass(p, 0, false, in, p->tmp[0], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, false, p->tmp[0], p->tmp[1], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, false, p->tmp[1], out, EPI_SCALE, 8.f, dct_mode, st);
     }
 }
 
 void inverse_cosine_transform(DctPlan* p, const float* in, float* out, int dct_mode,
                               cudaStream_t st) {
-    TGV_REQUIRE(dct_mode == TGVDCT_DCT_FP32, "this DCT mode is not built");
+    check_mode(p, dct_mode);
     const float s = (float)(1.0 / ((double)p->W * p->H * p->D * 8.0));
     if (p->D == 1) {
-        pass(p, 0, p->inv[0], in, p->tmp[0], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->inv[1], p->tmp[0], out, EPI_SCALE, s, A_PLAIN, 0, 0, 0, st);
+        any_pass(p, 0, true, in, p->tmp[0], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, p->tmp[0], out, EPI_SCALE, s, dct_mode, st);
     } else {
-        pass(p, 0, p->inv[0], in, p->tmp[0], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->inv[1], p->tmp[0], p->tmp[1], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 2, p->inv[2], p->tmp[1], out, EPI_SCALE, s, A_PLAIN, 0, 0, 0, st);
+        any_pass(p, 0, true, in, p->tmp[0], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, p->tmp[0], p->tmp[1], EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, true, p->tmp[1], out, EPI_SCALE, s, dct_mode, st);
     }
 }
 
@@ -470,25 +493,49 @@ void solve_poisson(DctPlan* p, const float* in, float* out, int eigen_mode, cuda
     TGV_CHECK_LAUNCH();
 }
 
+void poisson_solve(DctPlan* p, const float* rhs, float* l, int dct_mode, int eigen_mode,
+                   cudaStream_t st) {
+    check_mode(p, dct_mode);
+    const int epi = eigen_mode == TGVDCT_EIGEN_ACCURATE ? EPI_POISSON_ACC : EPI_POISSON_REF;
+    const float s = (float)(1.0 / ((double)p->W * p->H * p->D * 8.0));
+    float* t0 = p->tmp[0];
+    float* t1 = p->tmp[1];
+    any_pass(p, 0, false, rhs, t0, EPI_NONE, 1.f, dct_mode, st);
+    if (p->D == 1) {
+        any_pass(p, 1, false, t0, t1, epi, 1.f, dct_mode, st);
+        any_pass(p, 0, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, t0, l, EPI_SCALE, s, dct_mode, st);
+    } else {
+        any_pass(p, 1, false, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, false, t1, t0, epi, 1.f, dct_mode, st);
+        any_pass(p, 0, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, true, t0, l, EPI_SCALE, s, dct_mode, st);
+    }
+}
+
 void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float* vz, float* l,
                        int dct_mode, int eigen_mode, cudaStream_t st) {
-    TGV_REQUIRE(dct_mode == TGVDCT_DCT_FP32, "this DCT mode is not built");
+    check_mode(p, dct_mode);
     const int epi = eigen_mode == TGVDCT_EIGEN_ACCURATE ? EPI_POISSON_ACC : EPI_POISSON_REF;
     const float s = (float)(1.0 / ((double)p->W * p->H * p->D * 8.0));
     float* t0 = p->tmp[0];
     float* t1 = p->tmp[1];
     // forward: x (divergence fused into the operand load), y, z (+ Poisson division)
-    pass(p, 0, p->fwd[0], nullptr, t0, EPI_NONE, 1.f, A_DIVERGENCE, vx, vy, vz, st);
+    if (dct_mode == TGVDCT_DCT_FP32)
+        pass(p, 0, p->fwd[0], nullptr, t0, EPI_NONE, 1.f, A_DIVERGENCE, vx, vy, vz, st);
+    else
+        pass_tc(p, 0, false, nullptr, t0, EPI_NONE, 1.f, true, vx, vy, vz, dct_mode, st);
     if (p->D == 1) {
-        pass(p, 1, p->fwd[1], t0, t1, epi, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 0, p->inv[0], t1, t0, EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->inv[1], t0, l, EPI_SCALE, s, A_PLAIN, 0, 0, 0, st);
+        any_pass(p, 1, false, t0, t1, epi, 1.f, dct_mode, st);
+        any_pass(p, 0, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, t0, l, EPI_SCALE, s, dct_mode, st);
     } else {
-        pass(p, 1, p->fwd[1], t0, t1, EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 2, p->fwd[2], t1, t0, epi, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 0, p->inv[0], t0, t1, EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 1, p->inv[1], t1, t0, EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
-        pass(p, 2, p->inv[2], t0, l, EPI_SCALE, s, A_PLAIN, 0, 0, 0, st);
+        any_pass(p, 1, false, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, false, t1, t0, epi, 1.f, dct_mode, st);
+        any_pass(p, 0, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 1, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, true, t0, l, EPI_SCALE, s, dct_mode, st);
     }
 }
 

@@ -42,8 +42,11 @@ WORKLOADS = {
 # algorithmic bytes per voxel-iteration of one TGV2 iteration (read f, u, ubar, v3,
 # vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
 ALGO_BYTES = {0: 140, 1: 104, 2: 104}
-# bytes the two-pass FP32 iteration moves (dual 13 loads + 9 stores, primal 14 + 8)
-PASS_BYTES = {"two_pass": {0: 176, 1: 140, 2: 140}}
+# bytes an iteration moves: two-pass (dual 13 loads + 9 stores, primal 14 + 8) and
+# fused (18 loads + 17 stores, halo re-reads served by L2)
+PASS_BYTES = {"two_pass": {0: 176, 1: 140, 2: 140}, "fused": {0: 140, 1: 104, 2: 104}}
+KERNELS = {"fused": 2, "two_pass": 1}
+KERNEL_NAMES = {"fused": "tgv_fused_kernel", "two_pass": "tgv_dual_kernel + tgv_primal_kernel"}
 PREC_NAMES = {0: "fp32", 1: "bf16_dual", 2: "fx16_dual"}
 
 
@@ -193,7 +196,8 @@ def run_ours(args):
     f_host = make_input(args.workload)
     prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iters,
                              state_precision=args.precision, dct_mode=pkg.DCT_FP32,
-                             poisson_eigen=args.eigen)
+                             poisson_eigen=args.eigen, iteration_kernel=KERNELS[args.kernel],
+                             z_chunk=args.z_chunk)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     dev = torch.device("cuda", local)
@@ -233,7 +237,8 @@ def run_ours(args):
     # ---- roofline of the iteration kernels: iterations alone, events on the stream
     n_prof = args.profile_iterations
     prm_it = pkg.default_params(width=w, height=h, depth=d, iteration_count=n_prof,
-                                state_precision=args.precision)
+                                state_precision=args.precision,
+                                iteration_kernel=KERNELS[args.kernel], z_chunk=args.z_chunk)
     ctx.set_params(prm_it)
     vx, vy, vz = (torch.empty_like(f) for _ in range(3))
 
@@ -249,7 +254,7 @@ def run_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     it_ms = e0.elapsed_time(e1) / n_prof
-    launches_per_it = 2
+    launches_per_it = 1 if args.kernel == "fused" else 2
     launch_ms = it_ms / launches_per_it
     peak, peak_kind = hbm_peak()
     algo = ALGO_BYTES[args.precision]
@@ -258,7 +263,7 @@ def run_ours(args):
     # ---- e2e through the host-buffer C-ABI call (reference-facing)
     ctx.set_params(prm)
     e2e_ms = None
-    if rank == 0 or True:
+    if not args.no_e2e:
         fh = np.ascontiguousarray(f_host)
         uo, lo, ro = (np.empty_like(fh) for _ in range(3))
         times = []
@@ -273,7 +278,7 @@ def run_ours(args):
             if k > 0:
                 times.append(time.perf_counter() - t0)
         e2e_ms = 1e3 * float(np.median(times))
-    e2e_value = world * V * iters / (e2e_ms * 1e-3)
+    e2e_value = world * V * iters / (e2e_ms * 1e-3) if e2e_ms else None
 
     line = None
     if rank == 0:
@@ -293,7 +298,7 @@ def run_ours(args):
             "config": {"workload": args.workload, "shape_dhw": [d, h, w], "iterations": iters,
                        "state_precision": PREC_NAMES[args.precision], "dct": "fp32",
                        "poisson_eigen": "accurate" if args.eigen else "reference",
-                       "pass_structure": "two_pass",
+                       "pass_structure": args.kernel,
                        "l2": "state of 1.6 GB per replica, larger than L2",
                        "parallelism": f"replicas{world}"},
             "clocks": clocks.summary(),
@@ -303,9 +308,9 @@ def run_ours(args):
             "gpu_launches": gpu_launches * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "tgv_dual_kernel + tgv_primal_kernel (one iteration)",
+                         "kernel": KERNEL_NAMES[args.kernel] + " (one iteration)",
                          "algorithmic_bytes_per_voxel_iter": algo,
-                         "moved_bytes_per_voxel_iter": PASS_BYTES["two_pass"][args.precision],
+                         "moved_bytes_per_voxel_iter": PASS_BYTES[args.kernel][args.precision],
                          "iteration_ms": it_ms, "launch_ms": launch_ms,
                          "peak_source": peak_kind},
             "cpu_baseline": cpu,
@@ -326,11 +331,14 @@ def main():
     ap.add_argument("--workload", default="deshade_256x256x192", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
     ap.add_argument("--eigen", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--kernel", default="fused", choices=sorted(KERNELS))
+    ap.add_argument("--z-chunk", type=int, default=0)
     ap.add_argument("--iterations", type=int, default=0, help="override the iteration count")
     ap.add_argument("--profile-iterations", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample-iterations", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)

@@ -76,6 +76,17 @@ typedef enum tgvdct_dct_mode {
                               products, FP32 accumulation */
 } tgvdct_dct_mode;
 
+typedef enum tgvdct_iteration_kernel {
+    TGVDCT_KERNEL_AUTO = 0,     /* the fused single pass */
+    /* two coalesced passes per iteration (dual, then primal), every field updated
+       in place: 176 bytes per voxel-iteration in FP32 */
+    TGVDCT_KERNEL_TWO_PASS = 1,
+    /* one pass per iteration: z-marching tiles that recompute the one-voxel halo
+       of the dual fields on chip; the stencil-read fields are double-buffered:
+       140 bytes per voxel-iteration in FP32 */
+    TGVDCT_KERNEL_FUSED = 2
+} tgvdct_iteration_kernel;
+
 typedef enum tgvdct_poisson_eigen {
     /* 6 - 2cospi(kx/W) - 2cospi(ky/H) - 2cospi(kz/D) with FP32 cosines summed in
        FP64, as solve_poisson_in_cosine_domain.cu:48-53 computes it. */
@@ -102,6 +113,8 @@ typedef struct tgvdct_params {
     uint32_t paint_iteration_interval; /* callback cadence; 0 = never */
     int32_t callback_on_device;        /* 0: callback gets host copies (reference
                                           behaviour); 1: device pointers */
+    int32_t iteration_kernel;          /* tgvdct_iteration_kernel */
+    int32_t z_chunk;                   /* planes per block of the fused kernel; 0 = auto */
 } tgvdct_params;
 
 /* Called after iteration `iteration_index` when iteration_index > 0 and
@@ -199,6 +212,19 @@ tgvdct_status tgvdct_integrate_image_gradients_poisson_cosine_transform(
 tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* ctx, const float* v_x_dev,
                                            const float* v_y_dev, const float* v_z_dev,
                                            float* l_dev, void* stream);
+
+/* The DCT Poisson solve of a given right-hand side on a context's plan: l =
+   iDCT(DCT(rhs) / eigenvalue), DC set to zero, i.e. the reference's
+   cosineTransform -> solvePoissonInCosineDomain -> inverseCosineTransform chain
+   (CudaImageOperationsProcessor.cpp:240-284, solve_poisson_in_cosine_domain.cu)
+   without its three host round trips.  Uses the context's dct_mode and
+   poisson_eigen; device buffers, stream-ordered. */
+tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* ctx, const float* rhs_dev, float* l_dev,
+                                       void* stream);
+/* Reads and clears the device error flag of the tensor-core DCT passes of a context
+   (set when one of their bounded waits timed out); synchronises the stream.
+   Returns TGVDCT_ERR_CUDA if the flag was set. */
+tgvdct_status tgvdct_check_device_error(tgvdct_context* ctx, void* stream);
 
 /* Allocation-free form of tgvdct_poisson_integrate_dev.  It has no counterpart in
    the reference.  It is for callers that must not allocate device memory while

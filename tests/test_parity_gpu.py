@@ -172,3 +172,62 @@ def test_state_precision_error_vs_fp64(gpu_lib, prec):
 def test_bad_arguments_raise(gpu_lib):
     with pytest.raises(pkg.TgvdctError):
         pkg.tgv2_l1_deshade_launch(np.zeros((2, 3, 4), np.float32), 1.0, 5, 0, -1, None, 0.0, 1.0)
+
+
+@pytest.mark.parametrize("prec", [pkg.STATE_FP32, pkg.STATE_FX16_DUAL, pkg.STATE_BF16_DUAL])
+@pytest.mark.parametrize("shape,z_chunk,two_d,data_term", [
+    ((37, 45, 70), 5, False, pkg.DATA_L1),
+    ((19, 8, 33), 0, False, pkg.DATA_L2),
+    ((1, 50, 41), 0, False, pkg.DATA_L1),
+    ((1, 50, 41), 0, True, pkg.DATA_L1),
+    ((4, 1, 9), 1, False, pkg.DATA_L1),
+    ((3, 5, 1), 2, False, pkg.DATA_L2),
+])
+def test_fused_kernel_equals_two_pass(gpu_lib, prec, shape, z_chunk, two_d, data_term):
+    # same update sequence, one pass with on-chip halo recompute vs two in-place passes
+    f = tissue_phantom_3d(*shape, seed=12)
+    if two_d:
+        f = f[0]
+    kw = dict(state_precision=prec, data_term=data_term, two_d=two_d,
+              set_negative_values_to_zero=False)
+    a = pkg.TGVDeshadeProcessor.processTGV2L1GPUCuda(f, 0.9, 2.0, 1.0, 40,
+                                                     iteration_kernel=pkg.KERNEL_TWO_PASS, **kw)
+    b = pkg.TGVDeshadeProcessor.processTGV2L1GPUCuda(f, 0.9, 2.0, 1.0, 40,
+                                                     iteration_kernel=pkg.KERNEL_FUSED,
+                                                     z_chunk=z_chunk, **kw)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+# Tensor-core DCT modes against the reference's FP64 results.  BF16x3 keeps ~16
+# significant bits per product; one TF32 product keeps ~11.
+TC_TOL = {pkg.DCT_BF16X3: 3e-5, pkg.DCT_TF32: 3e-3}
+
+
+@pytest.mark.parametrize("mode", [pkg.DCT_BF16X3, pkg.DCT_TF32])
+@pytest.mark.parametrize("tag", ["10x12x16", "1x18x24", "5x7x1", "1x1x9", "3x1x1", "4x4x4"])
+def test_tensor_core_dct_vs_fp64_reference(gpu_lib, mode, tag):
+    g = load_golden(f"dct_{tag}_f64")
+    x = g["x"].astype(np.float32)
+    tol = TC_TOL[mode]
+    assert rel_l2(pkg.cosine_transform_kernel_launch(x, mode), g["cosine_transform"]) < tol
+    assert rel_l2(pkg.inverse_cosine_transform_kernel_launch(x, mode),
+                  g["inverse_cosine_transform"]) < tol
+    l = pkg.TGVDeshadeProcessor.integrate_image_gradients_poisson_cosine_transform(
+        g["v_x"], g["v_y"], g["v_z"], dct_mode=mode, poisson_eigen=pkg.EIGEN_ACCURATE)
+    # l is a smoothed difference of v: its error is bounded relative to v, not to l
+    vmax = max(np.abs(g[k]).max() for k in ("v_x", "v_y", "v_z"))
+    assert rel_l2(l, g["integrate"]) < 4 * tol or np.abs(l - g["integrate"]).max() < tol * vmax
+
+
+@pytest.mark.parametrize("mode", [pkg.DCT_FP32, pkg.DCT_BF16X3, pkg.DCT_TF32])
+@pytest.mark.parametrize("shape", [(40, 72, 136), (1, 200, 256), (256, 16, 24)])
+def test_dct_round_trip_and_vs_oracle(gpu_lib, mode, shape):
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(shape).astype(np.float32)
+    y = pkg.inverse_cosine_transform_kernel_launch(pkg.cosine_transform_kernel_launch(x, mode),
+                                                   mode)
+    assert rel_l2(y, x) < (2e-5 if mode != pkg.DCT_TF32 else 5e-3)
+    ref = oracle.cosine_transform(x.astype(np.float64))
+    assert rel_l2(pkg.cosine_transform_kernel_launch(x, mode), ref) < (
+        1e-6 if mode == pkg.DCT_FP32 else TC_TOL[mode])
