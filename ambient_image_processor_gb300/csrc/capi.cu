@@ -60,13 +60,17 @@ void validate(const tgvdct_params* p) {
     TGV_REQUIRE(std::isfinite(p->sigma) && p->sigma > 0.f, "sigma must be > 0");
     TGV_REQUIRE(std::isfinite(p->theta), "theta must be finite");
     TGV_REQUIRE(p->iteration_kernel >= TGVDCT_KERNEL_AUTO &&
-                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED,
+                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED_REGISTER,
                 "unknown iteration kernel");
     TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
 }
 
 int kernel_of(const tgvdct_params& p) {
-    return p.iteration_kernel == TGVDCT_KERNEL_TWO_PASS ? TGV_KERNEL_TWO_PASS : TGV_KERNEL_FUSED;
+    switch (p.iteration_kernel) {
+        case TGVDCT_KERNEL_TWO_PASS: return TGV_KERNEL_TWO_PASS;
+        case TGVDCT_KERNEL_FUSED_REGISTER: return TGV_KERNEL_FUSED_REGISTER;
+        default: return TGV_KERNEL_FUSED;
+    }
 }
 
 // Planes per block of the fused kernel: enough blocks to fill the GPU a few
@@ -183,6 +187,19 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
     }
     c->iterations_run = n_it;
     return false;
+}
+
+// Reads and clears the TGV kernels' device error flag (a pipeline wait timed out).
+void check_tgv_flag(tgvdct_context* c, cudaStream_t s) {
+    if (!c->st.err) return;
+    int h = 0;
+    TGV_CUDA(cudaMemcpyAsync(&h, c->st.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TGV_CUDA(cudaStreamSynchronize(s));
+    if (h) {
+        TGV_CUDA(cudaMemsetAsync(c->st.err, 0, sizeof(int), s));
+        set_error("a TGV iteration kernel timed out waiting on its load pipeline");
+        throw Error{TGVDCT_ERR_CUDA};
+    }
 }
 
 void create_into(const tgvdct_params* p, tgvdct_context** out) {
@@ -428,7 +445,7 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch(const float* f_host, uint32_t width,
         TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_z_host, c->st.v[2], n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaStreamSynchronize(s));
+        check_tgv_flag(c, s);
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -465,7 +482,7 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t wid
         TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaStreamSynchronize(s));
+        check_tgv_flag(c, s);
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -494,7 +511,7 @@ tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, ui
         TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
         run_loop(c, s, false, [](uint32_t) { return false; });
         TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaStreamSynchronize(s));
+        check_tgv_flag(c, s);
         return TGVDCT_OK;
     });
 }
@@ -592,6 +609,7 @@ tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* c, const float* rhs_dev, 
 tgvdct_status tgvdct_check_device_error(tgvdct_context* c, void* stream) {
     return guarded([&] {
         TGV_REQUIRE(c != nullptr, "null context");
+        check_tgv_flag(c, (cudaStream_t)stream);
         if (c->plan && !dct_tc_check(c->plan, (cudaStream_t)stream)) {
             set_error("a tensor-core DCT pass timed out waiting on its pipeline");
             return TGVDCT_ERR_CUDA;
@@ -651,7 +669,11 @@ tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host
         TGV_CUDA(cudaMemcpyAsync(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaStreamSynchronize(s));
+        check_tgv_flag(c, s);
+        if (c->plan && !dct_tc_check(c->plan, s)) {
+            set_error("a tensor-core DCT pass timed out waiting on its pipeline");
+            return TGVDCT_ERR_CUDA;
+        }
         return c->iterations_run < p->iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }

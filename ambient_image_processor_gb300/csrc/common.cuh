@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 
 #include "tgvdct.h"
@@ -48,7 +49,7 @@ struct TgvStencilFields {
     void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
 };
 
-enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2 };
+enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
 
 // Device state of one volume.  Fields are planar (structure of arrays), x fastest.
 // The two-pass kernels update set[0] in place.  The fused kernel reads set[cur]
@@ -65,6 +66,11 @@ struct TgvState {
     float* v[3] = {nullptr, nullptr, nullptr};
     TgvStencilFields set[2];
     int cur = 0;
+    // tensor maps of the TMA-pipelined fused kernel, one argument block per parity
+    // (built on first use; the fused kernel falls back to register prefetch for
+    // shapes the TMA stride rules exclude)
+    std::shared_ptr<void> tma_cache;
+    int* err = nullptr;      // device flag raised by a pipeline wait that timed out
     const TgvStencilFields& now() const { return set[cur]; }
 };
 
@@ -82,6 +88,8 @@ void tgv_state_init(TgvState& s, cudaStream_t st);
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.
 int tgv_kernels_per_iteration(const TgvState& s);
+// Whether the fused kernel of this state runs the TMA pipeline.
+bool tgv_uses_tma(const TgvState& s);
 
 // ---- Poisson integration -------------------------------------------------------
 // Per-shape cosine tables and scratch of the Poisson integration.

@@ -43,7 +43,7 @@ namespace {
 constexpr int TC_M = 128;        // lines per CTA (MMA M)
 constexpr int TC_THREADS = 256;  // 8 warps
 constexpr int ROW_BYTES = 128;   // K chunk per stage and row
-constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s
+constexpr uint64_t WAIT_LIMIT_NS = 200000000ull;  // 200 ms
 
 struct TcArgs {
     const float* in;
@@ -243,6 +243,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dct_tc_kernel(TcArgs g) {
     __shared__ uint64_t bar_free[2];
     __shared__ uint32_t tmem_base_s;
 
+    // an earlier pass timed out: do nothing more (one read shared by the block)
+    if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)g.err : 0)) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int batch = blockIdx.y;
     const long long line0 = (long long)blockIdx.x * TC_M;

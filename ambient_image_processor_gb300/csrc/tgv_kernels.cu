@@ -22,6 +22,11 @@
 // follows the reference's operation order (explicit fmaf where it calls fmaf, no
 // other contraction: this file is compiled with -fmad=false), so in FP32 the
 // result differs from the reference's float code only by the rounding of norm3df.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
 #include "common.cuh"
 
 namespace tgvdct {
@@ -52,16 +57,20 @@ struct Dual<TGVDCT_STATE_BF16_DUAL> {
 // 16-bit fixed point: value = code * (alpha / 32767).  After the projections every
 // component of p satisfies |p_c| <= |p| <= alpha1 and every component of q
 // satisfies |q_c| <= alpha0, so the code range covers the field exactly.
+// Conversions use the 1.5 * 2^23 bias: for |c| < 2^22 the float 12582912 + c holds
+// c in its low mantissa bits, so an integer add and a float add (full-rate
+// instructions) replace the slower int<->float conversion instructions, with the
+// same round-to-nearest-even result.
 template <>
 struct Dual<TGVDCT_STATE_FX16_DUAL> {
     using T = int16_t;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float dec) {
-        return (float)p[i] * dec;
+        const float c = __int_as_float(0x4B400000 + (int)p[i]) - 12582912.f;  // exact
+        return c * dec;
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float enc) {
-        float c = rintf(v * enc);
-        c = fminf(fmaxf(c, -32767.f), 32767.f);
-        p[i] = (T)(int)c;
+        const float c = fminf(fmaxf(v * enc, -32767.f), 32767.f);
+        p[i] = (T)__float_as_int(c + 12582912.f);  // low 16 bits: the rounded code
     }
 };
 
@@ -581,6 +590,463 @@ __global__ void __launch_bounds__(fused_threads<TY>())
     }
 }
 
+// ---- fused single pass, TMA pipeline -------------------------------------------------
+//
+// Same tile decomposition and update sequence as tgv_fused_kernel, software-
+// pipelined across planes.  Step t of a block computes, in one phase,
+//   the primal update at plane t                (needs p_new(t), p_new(t-1), q_new(t), q_new(t+1))
+//   the dual update p_new(t+1) on the -x/-y rim (ubar, vbar, p of planes t+1, t+2)
+//   the dual update q_new(t+2) on the +x/+y rim (vbar, q of planes t+1, t+2)
+// and ends with the block's single barrier; p_new lives in a 2-deep and q_new in a
+// 3-deep shared-memory ring.  The stencil fields (ubar, vbar, p, q) of every plane
+// arrive through the tensor memory accelerator: one thread issues 13 box loads
+// (tile plus one-voxel halo) per plane into a ring of NS stages, completing on the
+// stage's mbarrier (expect_tx); step t reads planes t+1 and t+2, so NS - 2 planes are
+// in flight while it computes.  The tile fields u, f, v (read only at a thread's
+// own voxel) are loaded into registers one plane ahead.  Interior voxels are one
+// warp per tile row (aligned, coalesced stores); three halo warps take the rim.
+namespace tma {
+
+constexpr int TX = 32, TY = 8;
+constexpr int EXW = TX + 2, EYH = TY + 2, NE = EXW * EYH;  // 34 x 10 positions
+constexpr int NTHREADS = 352;                              // 8 interior + 3 halo warps
+constexpr int PRODUCER = 256;                              // first halo thread issues TMA
+constexpr uint64_t WAIT_NS = 200000000ull;  // 200 ms: a plane normally lands in microseconds
+
+__host__ __device__ constexpr int a128(int b) { return (b + 127) / 128 * 128; }
+
+template <int PREC>
+struct Geo {
+    static constexpr int DES = PREC == TGVDCT_STATE_FP32 ? 4 : 2;  // dual element bytes
+    static constexpr int XO_F = 4, BW_F = TX + 8;                  // FP32 boxes: x0-4 .. x0+35
+    static constexpr int XO_D = DES == 4 ? 4 : 8;                  // 16-bit boxes: x0-8 .. x0+39
+    static constexpr int BW_D = DES == 4 ? TX + 8 : TX + 16;
+    static constexpr int BOX_F = a128(BW_F * EYH * 4);
+    static constexpr int BOX_D = a128(BW_D * EYH * DES);
+    // stage: ubar, vbar[3] | p[3], q[6]
+    static constexpr int OFF_P = 4 * BOX_F;
+    static constexpr int OFF_Q = OFF_P + 3 * BOX_D;
+    static constexpr int STAGE = OFF_Q + 6 * BOX_D;
+    // bytes the TMA delivers per plane (what expect_tx must announce)
+    static constexpr uint32_t tx_bytes(bool three) {
+        const int nc = three ? 3 : 2, nq = three ? 6 : 3;
+        return (uint32_t)((1 + nc) * BW_F * EYH * 4 + (nc + nq) * BW_D * EYH * DES);
+    }
+};
+
+struct alignas(64) Maps {
+    CUtensorMap ub, vb[3], p[3], q[6];  // q in kernel slot order
+};
+
+template <class T>
+struct Args {
+    Maps maps;
+    int W, H, D, zchunk;
+    size_t WH;
+    const float* f;
+    float* u;
+    float* v[3];
+    float* ubar_out;
+    float* vbar_out[3];
+    T* p_out[3];
+    T* q_out[6];  // state order: xx yy zz xy xz yz
+    float tau, sigma, theta, tau_lambda, alpha0, alpha1;
+    float penc, pdec, qenc, qdec;
+    int skip_bz;
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mtest(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ bool mwait(uint64_t* bar, uint32_t parity, int* err) {
+    if (mtest(bar, parity)) return true;
+    uint64_t t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    while (true) {
+        if (mtest(bar, parity)) return true;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > WAIT_NS) {
+            atomicExch(err, 1);
+            return false;
+        }
+        __nanosleep(32);
+    }
+}
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(su32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(su32(bar))
+        : "memory");
+}
+
+}  // namespace tma
+
+// p <- proj_{alpha1}(p + sigma (g - vb)), the reference's tgv_kernel_part22 arithmetic.
+// The division by max(1, |p|/alpha1) is skipped when that factor is 1 (x / 1 == x).
+template <bool THREE>
+__device__ __forceinline__ void dual_p_update(const float* g, const float* vb, float* p,
+                                              float sigma, float alpha1) {
+    p[0] = __fmaf_rn(sigma, g[0] - vb[0], p[0]);
+    p[1] = __fmaf_rn(sigma, g[1] - vb[1], p[1]);
+    float nrm;
+    if constexpr (THREE) {
+        p[2] = __fmaf_rn(sigma, g[2] - vb[2], p[2]);
+        nrm = norm3df(p[0], p[1], p[2]);
+    } else {
+        nrm = sqrtf(p[0] * p[0] + p[1] * p[1]);
+    }
+    nrm = fmaxf(1.f, nrm / alpha1);
+    if (nrm > 1.f) {
+        p[0] = p[0] / nrm;
+        p[1] = p[1] / nrm;
+        if constexpr (THREE) p[2] = p[2] / nrm;
+    }
+}
+
+// q <- proj_{alpha0}(q + sigma E vbar); xm/ym/zm: vbar at x-1 / y-1 / z-1 (0 outside);
+// q in slot order xx yy xy zz xz yz (tgv_kernel_part5 arithmetic)
+template <bool THREE>
+__device__ __forceinline__ void dual_q_update(const float* vb, const float* xm, const float* ym,
+                                              const float* zm, float* q, float sigma,
+                                              float alpha0) {
+    const float exx = xm[0] - vb[0];
+    const float eyy = ym[1] - vb[1];
+    const float exy = ((xm[1] - vb[1]) + (ym[0] - vb[0])) * 0.5f;
+    q[0] = __fmaf_rn(sigma, exx, q[0]);
+    q[1] = __fmaf_rn(sigma, eyy, q[1]);
+    q[2] = __fmaf_rn(sigma, exy, q[2]);
+    float sq = q[0] * q[0] + q[1] * q[1] + 2.f * q[2] * q[2];
+    if constexpr (THREE) {
+        const float ezz = zm[2] - vb[2];
+        const float exz = ((xm[2] - vb[2]) + (zm[0] - vb[0])) * 0.5f;
+        const float eyz = ((ym[2] - vb[2]) + (zm[1] - vb[1])) * 0.5f;
+        q[3] = __fmaf_rn(sigma, ezz, q[3]);
+        q[4] = __fmaf_rn(sigma, exz, q[4]);
+        q[5] = __fmaf_rn(sigma, eyz, q[5]);
+        sq = sq + q[3] * q[3] + 2.f * q[4] * q[4] + 2.f * q[5] * q[5];
+    }
+    const float qn = fmaxf(1.f, sqrtf(sq) / alpha0);
+    constexpr int NQ = THREE ? 6 : 3;
+    if (qn > 1.f) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) q[k] = q[k] / qn;
+    }
+}
+
+template <int PREC, bool THREE, int DATA, int NS>
+__global__ void __launch_bounds__(tma::NTHREADS, 2)
+    tgv_fused_tma_kernel(const __grid_constant__ tma::Args<typename Dual<PREC>::T> a) {
+    using namespace tma;
+    using S = Dual<PREC>;
+    using G = Geo<PREC>;
+    using T = typename S::T;
+    constexpr int NC = THREE ? 3 : 2, NQ = THREE ? 6 : 3;
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+    uint8_t* stages = smem;                                  // NS x STAGE
+    float* sP = (float*)(smem + NS * G::STAGE);              // [2][3][NE]
+    float* sQ = sP + 2 * 3 * NE;                             // [3][6][NE]
+    __shared__ uint64_t full[NS];
+
+    // a pipeline wait of an earlier block or launch timed out: do nothing more
+    // (one read, shared by the whole block, so every thread takes the same branch)
+    if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
+    const int tid = threadIdx.x;
+    int ex, ey;
+    bool interior = false, active = true;
+    if (tid < 256) {
+        ex = (tid & 31) + 1;
+        ey = (tid >> 5) + 1;
+        interior = true;
+    } else if (tid < 256 + NE - TX * TY) {
+        const int h = tid - 256;
+        if (h < EXW) { ex = h; ey = 0; }
+        else if (h < 2 * EXW) { ex = h - EXW; ey = EYH - 1; }
+        else if (h < 2 * EXW + TY) { ex = 0; ey = 1 + (h - 2 * EXW); }
+        else { ex = EXW - 1; ey = 1 + (h - 2 * EXW - TY); }
+    } else {
+        ex = 0;
+        ey = 0;
+        active = false;
+    }
+    const int e = ey * EXW + ex;
+    const int x0 = (int)blockIdx.x * TX, y0 = (int)blockIdx.y * TY;
+    const int x = x0 - 1 + ex, y = y0 - 1 + ey;
+    const bool in_dom = active && x >= 0 && x < a.W && y >= 0 && y < a.H;
+    const bool in_rp = in_dom && ex < EXW - 1 && ey < EYH - 1;
+    const bool in_rq = in_dom && ex >= 1 && ey >= 1;
+    interior = interior && in_dom;
+    const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
+    const int D = a.D;
+    const int z0 = (int)blockIdx.z * a.zchunk;
+    const int z1 = min(D, z0 + a.zchunk);
+    const int pbase = max(z0 - 1, 0);  // first plane this block loads; slots count from it
+    const int plast = min(D - 1, z1);  // last plane this block reads
+    const size_t col = in_dom ? (size_t)y * a.W + x : 0;
+
+    const int of = ey * G::BW_F + ex + G::XO_F - 1;  // offset in FP32 stencil boxes
+    const int od = ey * G::BW_D + ex + G::XO_D - 1;  // offset in dual boxes
+    auto st_of = [&](int plane) { return stages + ((plane - pbase) % NS) * G::STAGE; };
+    // field views of a stage (st: the stage's base)
+    auto fb = [&](const uint8_t* st, int field) -> const float* {  // 0 ubar, 1-3 vbar
+        return (const float*)(st + field * G::BOX_F);
+    };
+    auto pb = [&](const uint8_t* st, int c) -> const T* {
+        return (const T*)(st + G::OFF_P + c * G::BOX_D);
+    };
+    auto qb = [&](const uint8_t* st, int k) -> const T* {
+        return (const T*)(st + G::OFF_Q + k * G::BOX_D);
+    };
+    auto Pslot = [&](int plane) { return sP + (plane & 1) * 3 * NE; };  // [3][NE]
+    auto Qslot = [&](int plane) { return sQ + (plane % 3) * 6 * NE; };  // [6][NE]
+    auto dec_p = [&](T v) { T t[1] = {v}; return S::ld(t, 0, a.pdec); };
+    auto dec_q = [&](T v) { T t[1] = {v}; return S::ld(t, 0, a.qdec); };
+    auto rq_p = [&](float v) {
+        if constexpr (PREC == TGVDCT_STATE_FP32) return v;
+        T t[1];
+        S::st(t, 0, v, a.penc);
+        return S::ld(t, 0, a.pdec);
+    };
+    auto rq_q = [&](float v) {
+        if constexpr (PREC == TGVDCT_STATE_FP32) return v;
+        T t[1];
+        S::st(t, 0, v, a.qenc);
+        return S::ld(t, 0, a.qdec);
+    };
+    auto issue = [&](int plane) {  // producer thread only
+        if (plane < 0 || plane > plast) return;
+        uint8_t* st = st_of(plane);
+        uint64_t* bar = &full[(plane - pbase) % NS];
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
+                     "r"(G::tx_bytes(THREE))
+                     : "memory");
+        const int xf = x0 - G::XO_F, xd = x0 - G::XO_D, yb = y0 - 1;
+        tma_load(st, &a.maps.ub, xf, yb, plane, bar);
+        for (int c = 0; c < NC; ++c) tma_load(st + (1 + c) * G::BOX_F, &a.maps.vb[c], xf, yb, plane, bar);
+        for (int c = 0; c < NC; ++c) tma_load(st + G::OFF_P + c * G::BOX_D, &a.maps.p[c], xd, yb, plane, bar);
+        for (int k = 0; k < NQ; ++k) tma_load(st + G::OFF_Q + k * G::BOX_D, &a.maps.q[k], xd, yb, plane, bar);
+    };
+    bool ok = true;
+    int waited_upto = pbase - 1;  // every plane <= this one has landed
+    auto wait_plane = [&](int plane) {
+        if (plane < 0 || plane > plast || plane <= waited_upto) return;
+        const int j = (plane - pbase) / NS;
+        if (!mwait(&full[(plane - pbase) % NS], j & 1, a.err)) ok = false;
+        else waited_upto = plane;
+    };
+    // p_new over R_p from stage sz (plane z) and sn (plane z+1, or null past the volume):
+    // ubar(z) own/+x/+y, ubar(z+1) own, vbar(z) own, p(z)
+    auto dual_p_at = [&](const uint8_t* sz, const uint8_t* sn) {
+        const float* ub = fb(sz, 0);
+        const float u0 = ub[of];
+        float g[3] = {xl ? ub[of + 1] - u0 : 0.f, yl ? ub[of + G::BW_F] - u0 : 0.f, 0.f};
+        if constexpr (THREE) g[2] = sn ? fb(sn, 0)[of] - u0 : 0.f;
+        float vb[3] = {fb(sz, 1)[of], fb(sz, 2)[of], THREE ? fb(sz, 3)[of] : 0.f};
+        float pp[3];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) pp[c] = dec_p(pb(sz, c)[od]);
+        dual_p_update<THREE>(g, vb, pp, a.sigma, a.alpha1);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) pp[c] = rq_p(pp[c]);
+        return make_float3(pp[0], pp[1], THREE ? pp[2] : 0.f);
+    };
+    // q_new over R_q from stage sz (plane z) and sm (plane z-1, or null below the
+    // volume): vbar(z) own/-x/-y, vbar(z-1) own, q(z); written to ring slot out
+    auto dual_q_at = [&](const uint8_t* sz, const uint8_t* sm, float* out) {
+        float vb[3], xm[3], ym[3], zm[3], q[6];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const float* box = fb(sz, 1 + c);
+            vb[c] = box[of];
+            xm[c] = x > 0 ? box[of - 1] : 0.f;
+            ym[c] = y > 0 ? box[of - G::BW_F] : 0.f;
+            zm[c] = (THREE && sm) ? fb(sm, 1 + c)[of] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) q[k] = dec_q(qb(sz, k)[od]);
+        dual_q_update<THREE>(vb, xm, ym, zm, q, a.sigma, a.alpha0);
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) out[k * NE + e] = rq_q(q[k]);
+    };
+    float tu = 0.f, tf = 0.f, tv[3] = {0.f, 0.f, 0.f};  // u, f, v of the next primal plane
+    auto load_tile = [&](int z) {
+        if (interior && z < z1) {
+            const size_t i = (size_t)z * a.WH + col;
+            tu = a.u[i];
+            tf = a.f[i];
+            for (int c = 0; c < NC; ++c) tv[c] = a.v[c][i];
+        }
+    };
+
+    if (tid == 0) {
+        for (int k = 0; k < NS; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[k])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == PRODUCER)
+        for (int k = 0; k < NS; ++k) issue(pbase + k);
+    int issued_upto = pbase + NS - 1;  // meaningful in the producer only
+    load_tile(z0);
+
+    // ---- prologue: p_new(z0-1) own, p_new(z0) over R_p, q_new(z0), q_new(z0+1) over R_q
+    wait_plane(z0 - 1);
+    wait_plane(z0);
+    if (z0 + 1 < D) wait_plane(z0 + 1);
+    float p_prev[3] = {0.f, 0.f, 0.f};
+    if (ok) {
+        const uint8_t* s0 = st_of(z0);
+        const uint8_t* s1 = z0 + 1 < D ? st_of(z0 + 1) : nullptr;
+        const uint8_t* sm = z0 > 0 ? st_of(z0 - 1) : nullptr;
+        if constexpr (THREE) {
+            if (interior && z0 > 0) {  // p_new(z0 - 1) at this column
+                const float3 pp = dual_p_at(sm, s0);
+                p_prev[0] = pp.x;
+                p_prev[1] = pp.y;
+                p_prev[2] = pp.z;
+            }
+        }
+        if (in_rp) {
+            const float3 pp = dual_p_at(s0, s1);
+            float* Pz = Pslot(z0);
+            Pz[e] = pp.x;
+            Pz[NE + e] = pp.y;
+            if constexpr (THREE) Pz[2 * NE + e] = pp.z;
+        }
+        if (in_rq) {
+            dual_q_at(s0, sm, Qslot(z0));
+            if (s1) dual_q_at(s1, s0, Qslot(z0 + 1));
+        }
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && tid == PRODUCER) {
+        // planes z0-1 and z0 are no longer read: their slots take the next planes
+        if (z0 > 0) issue(++issued_upto);
+        issue(++issued_upto);
+    }
+
+    // ring positions of plane t + 1 (stage) and of plane t (p ring) / t (q ring)
+    int slot1 = (z0 + 1 - pbase) % NS;
+    int pslot = z0 & 1, qslot = z0 % 3;
+    for (int t = z0; t < z1 && ok; ++t) {
+        const bool p_next = t + 1 < z1;                  // p_new(t+1) feeds primal(t+1)
+        const bool q_next = t + 2 <= z1 && t + 2 < D;    // q_new(t+2) feeds primal(t+1)
+        if (p_next || q_next) wait_plane(min(t + 2, plast));
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        const int slot2 = slot1 + 1 == NS ? 0 : slot1 + 1;
+        const uint8_t* S1 = stages + slot1 * G::STAGE;   // plane t + 1
+        const uint8_t* S2 = stages + slot2 * G::STAGE;   // plane t + 2
+        const float* Pt = sP + pslot * 3 * NE;           // p_new(t)
+        float* Pn = sP + (pslot ^ 1) * 3 * NE;           // p_new(t + 1)
+        const int q1 = qslot + 1 == 3 ? 0 : qslot + 1, q2 = q1 + 1 == 3 ? 0 : q1 + 1;
+        const float* Qt = sQ + qslot * 6 * NE;           // q_new(t)
+        const float* Qn = sQ + q1 * 6 * NE;              // q_new(t + 1)
+        float* Qnn = sQ + q2 * 6 * NE;                   // q_new(t + 2)
+        const float pu = tu, pf = tf, pv0 = tv[0], pv1 = tv[1], pv2 = tv[2];
+        load_tile(t + 1);
+        // ---- duals for the next planes
+        float3 pn = make_float3(0.f, 0.f, 0.f);
+        if (in_rp && p_next) pn = dual_p_at(S1, t + 2 < D ? S2 : nullptr);
+        if (in_rq && q_next) dual_q_at(S2, S1, Qnn);
+        // ---- primal at (x, y, t)
+        if (interior) {
+            const size_t i = (size_t)t * a.WH + col;
+            float pv[3] = {Pt[e], Pt[NE + e], THREE ? Pt[2 * NE + e] : 0.f};
+            const float bx = (x > 0 ? Pt[e - 1] : 0.f) - pv[0];
+            const float by = (y > 0 ? Pt[NE + e - EXW] : 0.f) - pv[1];
+            float div = bx + by;
+            if constexpr (THREE) {
+                const float bz = p_prev[2] - pv[2];
+                if (!a.skip_bz) div = div + bz;
+            }
+            float uu = pu - a.tau * div;
+            if constexpr (DATA == TGVDCT_DATA_L1) {
+                const float umf = uu - pf;
+                if (umf > a.tau_lambda) uu = uu - a.tau_lambda;
+                else if (umf < -a.tau_lambda) uu = uu + a.tau_lambda;
+                else uu = pf;
+            } else {
+                uu = (uu + a.tau_lambda * pf) / (1.f + a.tau_lambda);
+            }
+            a.u[i] = uu;
+            a.ubar_out[i] = uu + a.theta * (uu - pu);
+            const bool has_next = t + 1 < D;
+            const float qxx = Qt[e], qyy = Qt[NE + e], qxy = Qt[2 * NE + e];
+            float d[3];
+            d[0] = (xl ? Qt[e + 1] - qxx : 0.f) + (yl ? Qt[2 * NE + e + EXW] - qxy : 0.f);
+            d[1] = (yl ? Qt[NE + e + EXW] - qyy : 0.f) + (xl ? Qt[2 * NE + e + 1] - qxy : 0.f);
+            d[2] = 0.f;
+            float qzz = 0.f, qxz = 0.f, qyz = 0.f;
+            if constexpr (THREE) {
+                qzz = Qt[3 * NE + e];
+                qxz = Qt[4 * NE + e];
+                qyz = Qt[5 * NE + e];
+                d[0] = d[0] + (has_next ? Qn[4 * NE + e] - qxz : 0.f);
+                d[1] = d[1] + (has_next ? Qn[5 * NE + e] - qyz : 0.f);
+                d[2] = ((has_next ? Qn[3 * NE + e] - qzz : 0.f) +
+                        (xl ? Qt[4 * NE + e + 1] - qxz : 0.f)) +
+                       (yl ? Qt[5 * NE + e + EXW] - qyz : 0.f);
+            }
+            const float vo[3] = {pv0, pv1, pv2};
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const float vn = vo[c] - a.tau * (d[c] - pv[c]);
+                a.v[c][i] = vn;
+                a.vbar_out[c][i] = vn + a.theta * (vn - vo[c]);
+                S::st(a.p_out[c], i, pv[c], a.penc);
+            }
+            S::st(a.q_out[0], i, qxx, a.qenc);
+            S::st(a.q_out[1], i, qyy, a.qenc);
+            S::st(a.q_out[3], i, qxy, a.qenc);
+            if constexpr (THREE) {
+                S::st(a.q_out[2], i, qzz, a.qenc);
+                S::st(a.q_out[4], i, qxz, a.qenc);
+                S::st(a.q_out[5], i, qyz, a.qenc);
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) p_prev[c] = pv[c];
+        }
+        // p_new(t+1) goes to the other slot of the p ring (primal(t-1) read it before
+        // the last barrier)
+        if (in_rp && p_next) {
+            Pn[e] = pn.x;
+            Pn[NE + e] = pn.y;
+            if constexpr (THREE) Pn[2 * NE + e] = pn.z;
+        }
+        __syncthreads();
+        if (tid == PRODUCER) issue(++issued_upto);  // plane t+1 is dead: its slot takes t+1+NS
+        slot1 = slot2;
+        pslot ^= 1;
+        qslot = q1;
+    }
+    // On an error exit, let every load this block issued land before the block's
+    // shared memory goes away (bounded waits; the flag is already raised).
+    if (!ok && tid == PRODUCER) {
+        for (int pl = max(waited_upto + 1, 0); pl <= min(issued_upto, plast); ++pl) {
+            const int j = (pl - pbase) / NS;
+            mwait(&full[(pl - pbase) % NS], j & 1, a.err);
+        }
+    }
+    __syncthreads();
+}
+
 size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2; }
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -663,6 +1129,138 @@ void launch_fused(const FusedArgs<typename Dual<PREC>::T>& a, int D, cudaStream_
     TGV_CHECK_LAUNCH();
 }
 
+// ---- TMA launch plumbing -----------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TGV_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                                  cudaEnableDefault, &q));
+        TGV_REQUIRE(q == cudaDriverEntryPointSuccess && ptr, "cuTensorMapEncodeTiled unavailable");
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+    }
+    return fn;
+}
+
+void encode_box(CUtensorMap* m, const void* base, int es, const TgvState& s, int bw, int bh) {
+    const cuuint64_t dims[3] = {(cuuint64_t)s.W, (cuuint64_t)s.H, (cuuint64_t)s.D};
+    const cuuint64_t strides[2] = {(cuuint64_t)s.W * es, (cuuint64_t)s.W * s.H * es};
+    const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUtensorMapDataType dt =
+        es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    const CUresult r = tensor_map_encoder()(m, dt, 3, const_cast<void*>(base), dims, strides, box,
+                                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                            CU_TENSOR_MAP_SWIZZLE_NONE,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    TGV_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected a state field");
+}
+
+// TMA needs 16-byte row and plane strides: width a multiple of 4 (FP32 fields) and
+// of 8 (16-bit dual fields).
+bool tma_shape_ok(const TgvState& s) {
+    const int need = s.precision == TGVDCT_STATE_FP32 ? 4 : 8;
+    return s.W % need == 0 && s.kernel == TGV_KERNEL_FUSED;
+}
+
+template <int PREC>
+struct TmaCache {
+    tma::Args<typename Dual<PREC>::T> args[2];  // [cur]: reads set cur, writes set cur ^ 1
+};
+
+template <int PREC>
+constexpr int tma_stages() {
+    return PREC == TGVDCT_STATE_FP32 ? 3 : 4;
+}
+
+template <int PREC>
+size_t tma_smem_bytes() {
+    // stages + the p_new ring (2 x 3 fields) and the q_new ring (3 x 6 fields)
+    return (size_t)tma_stages<PREC>() * tma::Geo<PREC>::STAGE + 24 * tma::NE * 4 + 128;
+}
+
+template <int PREC>
+TmaCache<PREC>* tma_cache(TgvState& s) {
+    if (!s.tma_cache) {
+        using T = typename Dual<PREC>::T;
+        using G = tma::Geo<PREC>;
+        auto c = std::make_shared<TmaCache<PREC>>();
+        const int NC = s.three ? 3 : 2, NQ = s.three ? 6 : 3;
+        const int qmap[6] = {0, 1, 3, 2, 4, 5};  // kernel slot -> state order
+        for (int cur = 0; cur < 2; ++cur) {
+            tma::Args<T>& a = c->args[cur];
+            std::memset(&a, 0, sizeof(a));
+            const TgvStencilFields& I = s.set[cur];
+            const TgvStencilFields& O = s.set[cur ^ 1];
+            encode_box(&a.maps.ub, I.ubar, 4, s, G::BW_F, tma::EYH);
+            for (int c2 = 0; c2 < NC; ++c2) {
+                encode_box(&a.maps.vb[c2], I.vbar[c2], 4, s, G::BW_F, tma::EYH);
+                encode_box(&a.maps.p[c2], I.p[c2], G::DES, s, G::BW_D, tma::EYH);
+            }
+            for (int k = 0; k < NQ; ++k)
+                encode_box(&a.maps.q[k], I.q[qmap[k]], G::DES, s, G::BW_D, tma::EYH);
+            a.f = s.f;
+            a.W = s.W;
+            a.H = s.H;
+            a.D = s.D;
+            a.WH = (size_t)s.W * s.H;
+            a.u = s.u;
+            a.ubar_out = O.ubar;
+            for (int c2 = 0; c2 < 3; ++c2) {
+                a.v[c2] = s.v[c2];
+                a.vbar_out[c2] = O.vbar[c2];
+                a.p_out[c2] = (T*)O.p[c2];
+            }
+            for (int k = 0; k < 6; ++k) a.q_out[k] = (T*)O.q[k];
+        }
+        s.tma_cache = c;
+    }
+    return (TmaCache<PREC>*)s.tma_cache.get();
+}
+
+template <int PREC, bool THREE, int DATA>
+void launch_tma(const tma::Args<typename Dual<PREC>::T>& a, cudaStream_t st) {
+    constexpr int NS = tma_stages<PREC>();
+    auto kern = tgv_fused_tma_kernel<PREC, THREE, DATA, NS>;
+    const size_t smem = tma_smem_bytes<PREC>();
+    static bool configured = false;
+    if (!configured) {
+        TGV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    const dim3 grid(ceil_div(a.W, tma::TX), ceil_div(a.H, tma::TY), ceil_div(a.D, a.zchunk));
+    kern<<<grid, tma::NTHREADS, smem, st>>>(a);
+    TGV_CHECK_LAUNCH();
+}
+
+template <int PREC>
+void iterate_tma(TgvState& s, const TgvStep& k, int* err, cudaStream_t st) {
+    auto a = tma_cache<PREC>(s)->args[s.cur];  // copy; the step parameters change per call
+    a.zchunk = s.three ? (s.zchunk > 0 ? s.zchunk : s.D) : 1;
+    a.tau = k.tau;
+    a.sigma = k.sigma;
+    a.theta = k.theta;
+    a.tau_lambda = k.tau * k.lambda;
+    a.alpha0 = k.alpha0;
+    a.alpha1 = k.alpha1;
+    a.penc = 32767.f / k.alpha1;
+    a.pdec = k.alpha1 / 32767.f;
+    a.qenc = 32767.f / k.alpha0;
+    a.qdec = k.alpha0 / 32767.f;
+    a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
+    a.err = err;
+    if (s.three) {
+        if (k.data_term == TGVDCT_DATA_L1) launch_tma<PREC, true, TGVDCT_DATA_L1>(a, st);
+        else launch_tma<PREC, true, TGVDCT_DATA_L2>(a, st);
+    } else {
+        if (k.data_term == TGVDCT_DATA_L1) launch_tma<PREC, false, TGVDCT_DATA_L1>(a, st);
+        else launch_tma<PREC, false, TGVDCT_DATA_L2>(a, st);
+    }
+    s.cur ^= 1;
+}
+
 template <int PREC>
 void iterate_fused(TgvState& s, const TgvStep& k, cudaStream_t st) {
     using T = typename Dual<PREC>::T;
@@ -716,9 +1314,9 @@ size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kerne
     const size_t n = (size_t)W * H * D;
     const size_t f32 = align256(n * 4), dual = align256(n * elem_bytes(precision));
     const int ncomp = three ? 3 : 2, nq = three ? 6 : 3;
-    const int sets = kernel == TGV_KERNEL_FUSED ? 2 : 1;
-    // u, f, v + per set: ubar, vbar, p, q
-    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq));
+    const int sets = kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
+    // u, f, v + per set: ubar, vbar, p, q; plus a device error flag
+    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq)) + 256;
 }
 
 void tgv_state_bind(TgvState& s, char* base) {
@@ -734,7 +1332,8 @@ void tgv_state_bind(TgvState& s, char* base) {
     s.u = (float*)take(f32);
     s.f = (float*)take(f32);
     for (int k = 0; k < 3; ++k) s.v[k] = k < ncomp ? (float*)take(f32) : nullptr;
-    const int sets = s.kernel == TGV_KERNEL_FUSED ? 2 : 1;
+    const int sets = s.kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
+    s.tma_cache.reset();
     // q order: xx yy zz xy xz yz; the 2-D launcher keeps xx yy xy
     const int order2[3] = {0, 1, 3};
     for (int t = 0; t < 2; ++t) {
@@ -746,6 +1345,7 @@ void tgv_state_bind(TgvState& s, char* base) {
         for (int k = 0; k < ncomp; ++k) F.p[k] = (void*)take(dual);
         for (int k = 0; k < nq; ++k) F.q[s.three ? k : order2[k]] = (void*)take(dual);
     }
+    s.err = (int*)take(256);
     s.cur = 0;
 }
 
@@ -763,9 +1363,20 @@ void tgv_state_init(TgvState& s, cudaStream_t st) {
     }
     for (int k = 0; k < 6; ++k)
         if (F.q[k]) TGV_CUDA(cudaMemsetAsync(F.q[k], 0, n * e, st));
+    TGV_CUDA(cudaMemsetAsync(s.err, 0, sizeof(int), st));
 }
 
+bool tgv_uses_tma(const TgvState& s) { return tma_shape_ok(s); }
+
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
+    if (tma_shape_ok(s)) {
+        TGV_REQUIRE(s.err != nullptr, "TMA kernel needs a device error flag");
+        switch (s.precision) {
+            case TGVDCT_STATE_FP32: iterate_tma<TGVDCT_STATE_FP32>(s, k, s.err, st); return;
+            case TGVDCT_STATE_BF16_DUAL: iterate_tma<TGVDCT_STATE_BF16_DUAL>(s, k, s.err, st); return;
+            case TGVDCT_STATE_FX16_DUAL: iterate_tma<TGVDCT_STATE_FX16_DUAL>(s, k, s.err, st); return;
+        }
+    }
     if (s.kernel == TGV_KERNEL_TWO_PASS) {
         switch (s.precision) {
             case TGVDCT_STATE_FP32: iterate_two_pass<TGVDCT_STATE_FP32>(s, k, st); return;
@@ -782,6 +1393,6 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     TGV_REQUIRE(false, "unknown state precision");
 }
 
-int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL_FUSED ? 1 : 2; }
+int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL_TWO_PASS ? 2 : 1; }
 
 }  // namespace tgvdct

@@ -82,9 +82,13 @@ typedef enum tgvdct_iteration_kernel {
        in place: 176 bytes per voxel-iteration in FP32 */
     TGVDCT_KERNEL_TWO_PASS = 1,
     /* one pass per iteration: z-marching tiles that recompute the one-voxel halo
-       of the dual fields on chip; the stencil-read fields are double-buffered:
-       140 bytes per voxel-iteration in FP32 */
-    TGVDCT_KERNEL_FUSED = 2
+       of the dual fields on chip, input planes streamed in by TMA; the
+       stencil-read fields are double-buffered: 140 bytes per voxel-iteration */
+    TGVDCT_KERNEL_FUSED = 2,
+    /* the fused pass with the input planes staged through registers instead of
+       the TMA pipeline (the fused kernel uses it by itself when the width is not a
+       multiple of 4, or of 8 with 16-bit dual fields) */
+    TGVDCT_KERNEL_FUSED_REGISTER = 3
 } tgvdct_iteration_kernel;
 
 typedef enum tgvdct_poisson_eigen {

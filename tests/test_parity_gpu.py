@@ -175,16 +175,22 @@ def test_bad_arguments_raise(gpu_lib):
 
 
 @pytest.mark.parametrize("prec", [pkg.STATE_FP32, pkg.STATE_FX16_DUAL, pkg.STATE_BF16_DUAL])
+@pytest.mark.parametrize("kernel", [pkg.KERNEL_FUSED, pkg.KERNEL_FUSED_REGISTER])
 @pytest.mark.parametrize("shape,z_chunk,two_d,data_term", [
-    ((37, 45, 70), 5, False, pkg.DATA_L1),
+    ((37, 45, 72), 5, False, pkg.DATA_L1),   # width % 8 == 0: the TMA pipeline
+    ((37, 45, 70), 5, False, pkg.DATA_L1),   # width % 4 != 0: register prefetch
+    ((19, 8, 64), 0, False, pkg.DATA_L2),
     ((19, 8, 33), 0, False, pkg.DATA_L2),
-    ((1, 50, 41), 0, False, pkg.DATA_L1),
+    ((6, 17, 40), 1, False, pkg.DATA_L1),
+    ((1, 50, 40), 0, False, pkg.DATA_L1),
+    ((1, 50, 40), 0, True, pkg.DATA_L1),
     ((1, 50, 41), 0, True, pkg.DATA_L1),
     ((4, 1, 9), 1, False, pkg.DATA_L1),
-    ((3, 5, 1), 2, False, pkg.DATA_L2),
+    ((3, 5, 8), 2, False, pkg.DATA_L2),
 ])
-def test_fused_kernel_equals_two_pass(gpu_lib, prec, shape, z_chunk, two_d, data_term):
-    # same update sequence, one pass with on-chip halo recompute vs two in-place passes
+def test_fused_kernels_equal_two_pass(gpu_lib, prec, kernel, shape, z_chunk, two_d, data_term):
+    # same update sequence: one pass with on-chip halo recompute (TMA-fed or
+    # register-fed) vs two in-place passes, so the results are bit-identical
     f = tissue_phantom_3d(*shape, seed=12)
     if two_d:
         f = f[0]
@@ -193,7 +199,7 @@ def test_fused_kernel_equals_two_pass(gpu_lib, prec, shape, z_chunk, two_d, data
     a = pkg.TGVDeshadeProcessor.processTGV2L1GPUCuda(f, 0.9, 2.0, 1.0, 40,
                                                      iteration_kernel=pkg.KERNEL_TWO_PASS, **kw)
     b = pkg.TGVDeshadeProcessor.processTGV2L1GPUCuda(f, 0.9, 2.0, 1.0, 40,
-                                                     iteration_kernel=pkg.KERNEL_FUSED,
+                                                     iteration_kernel=kernel,
                                                      z_chunk=z_chunk, **kw)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
