@@ -79,6 +79,8 @@ _SIGS = {
                                          _flt, _flt, _f32p, _f32p, _f32p],
     "tgvdct_tgv2_denoise_launch": [_f32p, _u32, _u32, _u32, _i32, _flt, _u32, _flt, _flt, _f32p],
     "tgvdct_tgv2_run_dev": [_vp, _vp, _vp, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+    "tgvdct_tgv2_forward_checkpointed_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _vp],
+    "tgvdct_tgv2_backward_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_divergence_launch": [_f32p, _f32p, _vp, _u32, _u32, _u32, _f32p],
     "tgvdct_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
     "tgvdct_inverse_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
@@ -378,6 +380,18 @@ class Context:
                 callback=None) -> int:
         return _check(lib().tgvdct_tgv2_run_dev(self._ctx, f_ptr, u_ptr, vx_ptr, vy_ptr, vz_ptr,
                                                 callback or CALLBACK(), None, stream))
+
+    def forward_checkpointed_dev(self, f_ptr, u_ptr, vx_ptr, vy_ptr, vz_ptr, checkpoint_every,
+                                 stream=None):
+        _check(lib().tgvdct_tgv2_forward_checkpointed_dev(self._ctx, f_ptr, u_ptr, vx_ptr, vy_ptr,
+                                                          vz_ptr, checkpoint_every, stream),
+               allow_stop=False)
+
+    def backward_dev(self, grad_u_ptr, grad_vx_ptr, grad_vy_ptr, grad_vz_ptr, grad_f_ptr,
+                     grad_params_ptr, stream=None):
+        _check(lib().tgvdct_tgv2_backward_dev(self._ctx, grad_u_ptr, grad_vx_ptr, grad_vy_ptr,
+                                              grad_vz_ptr, grad_f_ptr, grad_params_ptr, stream),
+               allow_stop=False)
 
     def poisson_integrate_dev(self, vx_ptr, vy_ptr, vz_ptr, l_ptr, stream=None):
         _check(lib().tgvdct_poisson_integrate_dev(self._ctx, vx_ptr, vy_ptr, vz_ptr, l_ptr,

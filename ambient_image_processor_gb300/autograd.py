@@ -1,0 +1,76 @@
+"""PyTorch autograd over the CUDA TGV2 loop and its hand-written reverse mode.
+
+``tgv_denoise(f, alpha0, alpha1, lam, iterations)`` runs the TGV2 primal-dual loop
+(the reference's tgv2_l1_deshade_launch / tgv2_l2_launch iteration, 3-D operators)
+on a CUDA tensor and returns (u, v): the denoised image and the bias gradient
+field.  Gradients flow to f and to alpha0, alpha1 and lambda (pass them as
+tensors with requires_grad) for bilevel parameter learning.  The forward keeps a
+checkpoint of the full state every ``checkpoint_every`` iterations; backward
+recomputes each segment from its checkpoint and runs the adjoint iteration (the
+transposed difference operators and the Jacobians of the projections and of the
+prox) from the last iteration to the first.  All compute runs in libtgvdct; torch
+provides device memory and the stream.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import DATA_L1, Context, default_params
+
+
+def _as_float(x):
+    return float(x.detach().item()) if isinstance(x, torch.Tensor) else float(x)
+
+
+class TGVDenoiseFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, f, alpha0, alpha1, lam, iterations, checkpoint_every, data_term):
+        if not f.is_cuda:
+            raise ValueError("f must be a CUDA tensor")
+        f = f.detach().contiguous().to(torch.float32)
+        shape = tuple(f.shape)
+        vol = f if f.dim() == 3 else f.reshape((1,) + shape)
+        d, h, w = vol.shape
+        prm = default_params(width=w, height=h, depth=d, lambda_=_as_float(lam),
+                             alpha0=_as_float(alpha0), alpha1=_as_float(alpha1),
+                             iteration_count=int(iterations), data_term=int(data_term))
+        tgv = Context(prm)
+        u = torch.empty_like(vol)
+        v = torch.empty((3,) + tuple(vol.shape), dtype=torch.float32, device=vol.device)
+        stream = torch.cuda.current_stream(vol.device).cuda_stream
+        tgv.forward_checkpointed_dev(vol.data_ptr(), u.data_ptr(), v[0].data_ptr(),
+                                     v[1].data_ptr(), v[2].data_ptr(), int(checkpoint_every),
+                                     stream)
+        ctx.tgv = tgv
+        ctx.shape = shape
+        ctx.vol_shape = tuple(vol.shape)
+        ctx.param_like = [p if isinstance(p, torch.Tensor) else None for p in (alpha0, alpha1, lam)]
+        return u.reshape(shape), v.reshape((3,) + shape)
+
+    @staticmethod
+    def backward(ctx, grad_u, grad_v):
+        tgv = ctx.tgv
+        dev = grad_u.device if grad_u is not None else grad_v.device
+        gu = grad_u.contiguous().to(torch.float32).reshape(ctx.vol_shape) if grad_u is not None else None
+        gv = grad_v.contiguous().to(torch.float32).reshape((3,) + ctx.vol_shape) if grad_v is not None else None
+        gf = torch.empty(ctx.vol_shape, dtype=torch.float32, device=dev)
+        gp = torch.empty(3, dtype=torch.float64, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        tgv.backward_dev(gu.data_ptr() if gu is not None else None,
+                         gv[0].data_ptr() if gv is not None else None,
+                         gv[1].data_ptr() if gv is not None else None,
+                         gv[2].data_ptr() if gv is not None else None,
+                         gf.data_ptr(), gp.data_ptr(), stream)
+        outs = []
+        # gp: d/dlambda, d/dalpha0, d/dalpha1; inputs: alpha0, alpha1, lam
+        for like, g in zip(ctx.param_like, (gp[1], gp[2], gp[0])):
+            outs.append(None if like is None else g.to(like.dtype).reshape(like.shape))
+        return (gf.reshape(ctx.shape), outs[0], outs[1], outs[2], None, None, None)
+
+
+def tgv_denoise(f, alpha0=2.0, alpha1=1.0, lam=1.0, iterations=100, checkpoint_every=20,
+                data_term=DATA_L1):
+    """(u, v) after `iterations` TGV2 iterations from u = ubar = f; differentiable in f,
+    alpha0, alpha1 and lam (tensors) through the checkpointed reverse mode."""
+    return TGVDenoiseFunction.apply(f, alpha0, alpha1, lam, iterations, checkpoint_every,
+                                    data_term)

@@ -34,6 +34,9 @@ UNITS = {
     "capi.cu": [],
     "noalloc.cu": [],
     "dct_tc.cu": [],
+    # the adjoint recomputes forward predicates (prox branch, projection activity)
+    # and must round exactly like tgv_kernels.cu
+    "adjoint.cu": ["-fmad=false"],
 }
 
 

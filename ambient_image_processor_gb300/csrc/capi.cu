@@ -27,6 +27,16 @@ struct tgvdct_context {
     size_t host_cb_count = 0;
     // device scratch for the per-callback deshade of tgvdct_process_dev
     float* cb_dev = nullptr;
+    // reverse mode: checkpoints of the last checkpointed forward run, the states of
+    // one recomputed segment, and the adjoint state with its scratch fields
+    void* ckpt_block = nullptr;
+    size_t ckpt_bytes = 0;
+    uint32_t ckpt_every = 0, ckpt_K = 0, ckpt_count = 0;
+    bool have_ckpt = false;
+    void* seg_block = nullptr;
+    size_t seg_bytes = 0;
+    void* adj_block = nullptr;
+    size_t adj_bytes = 0;
 };
 
 namespace {
@@ -230,11 +240,37 @@ void create_into(const tgvdct_params* p, tgvdct_context** out) {
 
 void destroy_ctx(tgvdct_context* c) {
     if (!c) return;
+    if (c->ckpt_block) cudaFree(c->ckpt_block);
+    if (c->seg_block) cudaFree(c->seg_block);
+    if (c->adj_block) cudaFree(c->adj_block);
     if (c->state_block) cudaFree(c->state_block);
     if (c->cb_dev) cudaFree(c->cb_dev);
     if (c->host_cb) cudaFreeHost(c->host_cb);
     dct_plan_destroy(c->plan);
     delete c;
+}
+
+// (re)allocates a context-owned device block of at least `bytes`
+void ensure_block(void** block, size_t* have, size_t bytes) {
+    if (*have >= bytes && *block) return;
+    if (*block) cudaFree(*block);
+    *block = nullptr;
+    *have = 0;
+    TGV_CUDA(cudaMalloc(block, bytes));
+    *have = bytes;
+}
+
+TgvFullDev full_state_at(void* block, size_t index, size_t n) {
+    TgvFullDev d;
+    tgv_full_state_bind(d, (char*)block + index * tgv_full_state_bytes(n), n);
+    return d;
+}
+
+void require_reverse_mode(const tgvdct_context* c) {
+    if (c->prm.state_precision != TGVDCT_STATE_FP32 || c->prm.geometry != TGVDCT_GEOMETRY_3D) {
+        set_error("the reverse mode needs FP32 state and 3-D geometry");
+        throw Error{TGVDCT_ERR_UNSUPPORTED};
+    }
 }
 
 struct CtxGuard {
@@ -408,6 +444,89 @@ tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* c, const float* f_dev, float* 
                 TGV_CUDA(cudaMemsetAsync(v_z_dev, 0, n * 4, s));
         }
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const float* f_dev,
+                                                   float* u_dev, float* v_x_dev,
+                                                   float* v_y_dev, float* v_z_dev,
+                                                   uint32_t checkpoint_every, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(f_dev && u_dev && v_x_dev && v_y_dev && v_z_dev, "null device buffer");
+        TGV_REQUIRE(checkpoint_every >= 1, "checkpoint_every must be >= 1");
+        require_reverse_mode(c);
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t n = voxels(c->prm);
+        const uint32_t K = c->prm.iteration_count;
+        const uint32_t count = (K + checkpoint_every - 1) / checkpoint_every;
+        c->have_ckpt = false;
+        ensure_block(&c->ckpt_block, &c->ckpt_bytes,
+                     (size_t)(count ? count : 1) * tgv_full_state_bytes(n));
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
+        tgv_state_init(c->st, s);
+        const TgvStep k = step_of(c->prm);
+        for (uint32_t it = 0; it < K; ++it) {
+            if (it % checkpoint_every == 0)
+                tgv_save_state(c->st, full_state_at(c->ckpt_block, it / checkpoint_every, n), s);
+            tgv_iterate(c->st, k, s);
+        }
+        c->iterations_run = K;
+        TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
+        float* vo[3] = {v_x_dev, v_y_dev, v_z_dev};
+        for (int a = 0; a < 3; ++a)
+            TGV_CUDA(cudaMemcpyAsync(vo[a], c->st.v[a], n * 4, cudaMemcpyDeviceToDevice, s));
+        c->ckpt_every = checkpoint_every;
+        c->ckpt_K = K;
+        c->ckpt_count = count;
+        c->have_ckpt = true;
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_dev,
+                                       const float* grad_v_x_dev, const float* grad_v_y_dev,
+                                       const float* grad_v_z_dev, float* grad_f_dev,
+                                       double* grad_params_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(grad_f_dev && grad_params_dev, "null device buffer");
+        TGV_REQUIRE(c->have_ckpt, "no checkpointed forward run on this context");
+        require_reverse_mode(c);
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t n = voxels(c->prm);
+        const uint32_t every = c->ckpt_every, K = c->ckpt_K;
+        ensure_block(&c->seg_block, &c->seg_bytes, (size_t)(every + 1) * tgv_full_state_bytes(n));
+        const size_t field = (n * 4 + 255) & ~size_t(255);
+        ensure_block(&c->adj_block, &c->adj_bytes, tgv_full_state_bytes(n) + 4 * field);
+        TgvFullDev A = full_state_at(c->adj_block, 0, n);
+        float* scratch = (float*)((char*)c->adj_block + tgv_full_state_bytes(n));
+        float* uta = scratch;
+        float* va[3] = {(float*)((char*)scratch + field), (float*)((char*)scratch + 2 * field),
+                        (float*)((char*)scratch + 3 * field)};
+        tgv_full_state_zero(A, n, s);
+        if (grad_u_dev) TGV_CUDA(cudaMemcpyAsync(A.u, grad_u_dev, n * 4, cudaMemcpyDeviceToDevice, s));
+        const float* gv[3] = {grad_v_x_dev, grad_v_y_dev, grad_v_z_dev};
+        for (int a = 0; a < 3; ++a)
+            if (gv[a]) TGV_CUDA(cudaMemcpyAsync(A.v[a], gv[a], n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemsetAsync(grad_f_dev, 0, n * 4, s));
+        TGV_CUDA(cudaMemsetAsync(grad_params_dev, 0, 3 * sizeof(double), s));
+        const TgvStep k = step_of(c->prm);
+        for (int seg = (int)c->ckpt_count - 1; seg >= 0; --seg) {
+            const uint32_t k0 = (uint32_t)seg * every, k1 = k0 + every < K ? k0 + every : K;
+            TGV_CUDA(cudaMemcpyAsync(full_state_at(c->seg_block, 0, n).u,
+                                     full_state_at(c->ckpt_block, seg, n).u,
+                                     tgv_full_state_bytes(n), cudaMemcpyDeviceToDevice, s));
+            for (uint32_t it = k0; it < k1; ++it)
+                tgv_step_fp32(c->st, k, full_state_at(c->seg_block, it - k0, n),
+                              full_state_at(c->seg_block, it - k0 + 1, n), s);
+            for (uint32_t it = k1; it-- > k0;)
+                tgv_adjoint_iteration(c->st, k, full_state_at(c->seg_block, it - k0, n),
+                                      full_state_at(c->seg_block, it - k0 + 1, n), A, uta, va,
+                                      grad_f_dev, grad_params_dev, s);
+        }
+        tgv_adjoint_finish(grad_f_dev, A, n, s);
+        return TGVDCT_OK;
     });
 }
 

@@ -91,6 +91,34 @@ int tgv_kernels_per_iteration(const TgvState& s);
 // Whether the fused kernel of this state runs the TMA pipeline.
 bool tgv_uses_tma(const TgvState& s);
 
+// ---- reverse mode (adjoint.cu) ---------------------------------------------------------
+// One full FP32 state of the loop: 17 contiguous V-sized fields.
+struct TgvFullDev {
+    float* u = nullptr;
+    float* ubar = nullptr;
+    float* v[3] = {nullptr, nullptr, nullptr};
+    float* vbar[3] = {nullptr, nullptr, nullptr};
+    float* p[3] = {nullptr, nullptr, nullptr};
+    float* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
+};
+size_t tgv_full_state_bytes(size_t n);
+void tgv_full_state_bind(TgvFullDev& s, char* base, size_t n);
+void tgv_full_state_zero(const TgvFullDev& s, size_t n, cudaStream_t st);
+// Copies the loop's current state (u, v and the current stencil set) into `out`.
+void tgv_save_state(const TgvState& s, const TgvFullDev& out, cudaStream_t st);
+// One FP32 iteration from `in` to `out` (distinct buffers), the same arithmetic as
+// every forward kernel (they agree bit for bit).
+void tgv_step_fp32(const TgvState& s, const TgvStep& k, const TgvFullDev& in,
+                   const TgvFullDev& out, cudaStream_t st);
+// Adjoint of the iteration S_k -> S_{k+1}: A holds the adjoint of S_{k+1} on entry
+// and of S_k on return; accumulates d/df into grad_f and d/d(lambda, alpha0, alpha1)
+// into gp[0..2]; uta and va are scratch (1 + 3 fields).
+void tgv_adjoint_iteration(const TgvState& s, const TgvStep& k, const TgvFullDev& Sk,
+                           const TgvFullDev& Sk1, const TgvFullDev& A, float* uta,
+                           float* const* va, float* grad_f, double* gp, cudaStream_t st);
+// grad_f += a(u_0) + a(ubar_0) (the loop starts from u = ubar = f).
+void tgv_adjoint_finish(float* grad_f, const TgvFullDev& A, size_t n, cudaStream_t st);
+
 // ---- Poisson integration -------------------------------------------------------
 // Per-shape cosine tables and scratch of the Poisson integration.
 struct DctPlan {

@@ -74,28 +74,39 @@ struct Dual<TGVDCT_STATE_FX16_DUAL> {
     }
 };
 
+// Fields of the two-pass kernels.  The dual pass reads ubar, vbar, p_in, q_in and
+// writes p, q; the primal pass reads p, q (the new duals), u_in, f, v_in and writes
+// u, ubar_out, v, vbar_out.  The forward loop passes the same buffers for in and out
+// (every field read at the voxel that writes it); the adjoint's segment recompute
+// passes one stored state as input and the next as output.
 template <class T>
 struct TgvArgs {
     int W, H, D;
     size_t WH;
-    const float* __restrict__ f;
-    float* __restrict__ u;
-    float* __restrict__ ubar;
-    float* __restrict__ v0;
-    float* __restrict__ v1;
-    float* __restrict__ v2;
-    float* __restrict__ vb0;
-    float* __restrict__ vb1;
-    float* __restrict__ vb2;
-    T* __restrict__ p0;
-    T* __restrict__ p1;
-    T* __restrict__ p2;
-    T* __restrict__ qxx;
-    T* __restrict__ qyy;
-    T* __restrict__ qzz;
-    T* __restrict__ qxy;
-    T* __restrict__ qxz;
-    T* __restrict__ qyz;
+    const float* f;
+    const float* u_in;
+    float* u;
+    const float* ubar;     // input ubar
+    float* ubar_out;
+    const float* v_in[3];
+    float* v0;
+    float* v1;
+    float* v2;
+    const float* vb0;      // input vbar
+    const float* vb1;
+    const float* vb2;
+    float* vbo[3];         // output vbar
+    const T* pin[3];
+    const T* qin[6];       // xx yy zz xy xz yz
+    T* p0;
+    T* p1;
+    T* p2;
+    T* qxx;
+    T* qyy;
+    T* qzz;
+    T* qxy;
+    T* qxz;
+    T* qyz;
     float tau, sigma, theta, tau_lambda, alpha0, alpha1;
     float penc, pdec, qenc, qdec;
     int skip_bz;  // L2 data term with depth == 1 drops B_z p (tgv_cuda/tgv2_l2.cu:39-42)
@@ -119,13 +130,13 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     const float gx = (x + 1 < a.W) ? a.ubar[i + 1] - ub : 0.f;
     const float gy = (y + 1 < a.H) ? a.ubar[i + W] - ub : 0.f;
     const float vbx = a.vb0[i], vby = a.vb1[i];
-    float px = __fmaf_rn(a.sigma, gx - vbx, S::ld(a.p0, i, a.pdec));
-    float py = __fmaf_rn(a.sigma, gy - vby, S::ld(a.p1, i, a.pdec));
+    float px = __fmaf_rn(a.sigma, gx - vbx, S::ld(a.pin[0], i, a.pdec));
+    float py = __fmaf_rn(a.sigma, gy - vby, S::ld(a.pin[1], i, a.pdec));
     float pz = 0.f, vbz = 0.f, nrm;
     if constexpr (THREE) {
         const float gz = (z + 1 < a.D) ? a.ubar[i + WH] - ub : 0.f;
         vbz = a.vb2[i];
-        pz = __fmaf_rn(a.sigma, gz - vbz, S::ld(a.p2, i, a.pdec));
+        pz = __fmaf_rn(a.sigma, gz - vbz, S::ld(a.pin[2], i, a.pdec));
         nrm = norm3df(px, py, pz);
     } else {
         nrm = sqrtf(px * px + py * py);  // tgv2_common_2d.cu:113
@@ -144,9 +155,9 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     const float exx = vbx_x - vbx;
     const float eyy = vby_y - vby;
     const float exy = ((vby_x - vby) + (vbx_y - vbx)) * 0.5f;  // tgv2_common.cu:191-199
-    float qxx = __fmaf_rn(a.sigma, exx, S::ld(a.qxx, i, a.qdec));
-    float qyy = __fmaf_rn(a.sigma, eyy, S::ld(a.qyy, i, a.qdec));
-    float qxy = __fmaf_rn(a.sigma, exy, S::ld(a.qxy, i, a.qdec));
+    float qxx = __fmaf_rn(a.sigma, exx, S::ld(a.qin[0], i, a.qdec));
+    float qyy = __fmaf_rn(a.sigma, eyy, S::ld(a.qin[1], i, a.qdec));
+    float qxy = __fmaf_rn(a.sigma, exy, S::ld(a.qin[3], i, a.qdec));
     float s = qxx * qxx + qyy * qyy + 2.f * qxy * qxy;
     float qzz = 0.f, qxz = 0.f, qyz = 0.f;
     if constexpr (THREE) {
@@ -158,9 +169,9 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
         const float ezz = vbz_z - vbz;
         const float exz = ((vbz_x - vbz) + (vbx_z - vbx)) * 0.5f;
         const float eyz = ((vbz_y - vbz) + (vby_z - vby)) * 0.5f;
-        qzz = __fmaf_rn(a.sigma, ezz, S::ld(a.qzz, i, a.qdec));
-        qxz = __fmaf_rn(a.sigma, exz, S::ld(a.qxz, i, a.qdec));
-        qyz = __fmaf_rn(a.sigma, eyz, S::ld(a.qyz, i, a.qdec));
+        qzz = __fmaf_rn(a.sigma, ezz, S::ld(a.qin[2], i, a.qdec));
+        qxz = __fmaf_rn(a.sigma, exz, S::ld(a.qin[4], i, a.qdec));
+        qyz = __fmaf_rn(a.sigma, eyz, S::ld(a.qin[5], i, a.qdec));
         s = s + qzz * qzz + 2.f * qxz * qxz + 2.f * qyz * qyz;  // tgv2_common.cu:255-261
     }
     const float qn = fmaxf(1.f, sqrtf(s) / a.alpha0);
@@ -198,7 +209,7 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
         const float bz = (z > 0 ? S::ld(a.p2, i - WH, a.pdec) : 0.f) - pzi;
         if (!a.skip_bz) div = div + bz;
     }
-    const float uo = a.u[i];
+    const float uo = a.u_in[i];
     const float fi = a.f[i];
     float uu = uo - a.tau * div;
     if constexpr (DATA == TGVDCT_DATA_L1) {
@@ -210,7 +221,7 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
         uu = (uu + a.tau_lambda * fi) / (1.f + a.tau_lambda);
     }
     a.u[i] = uu;
-    a.ubar[i] = uu + a.theta * (uu - uo);
+    a.ubar_out[i] = uu + a.theta * (uu - uo);
 
     // div q with Neumann forward differences          (tgv2_common.cu:290-318)
     const float qxx = S::ld(a.qxx, i, a.qdec);
@@ -240,22 +251,22 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
 
     // v <- v - tau (div q - p), vbar                     (tgv2_common.cu:338-347)
     {
-        const float vo = a.v0[i];
+        const float vo = a.v_in[0][i];
         const float vn = vo - a.tau * (dx - pxi);
         a.v0[i] = vn;
-        a.vb0[i] = vn + a.theta * (vn - vo);
+        a.vbo[0][i] = vn + a.theta * (vn - vo);
     }
     {
-        const float vo = a.v1[i];
+        const float vo = a.v_in[1][i];
         const float vn = vo - a.tau * (dy - pyi);
         a.v1[i] = vn;
-        a.vb1[i] = vn + a.theta * (vn - vo);
+        a.vbo[1][i] = vn + a.theta * (vn - vo);
     }
     if constexpr (THREE) {
-        const float vo = a.v2[i];
+        const float vo = a.v_in[2][i];
         const float vn = vo - a.tau * (dz - pzi);
         a.v2[i] = vn;
-        a.vb2[i] = vn + a.theta * (vn - vo);
+        a.vbo[2][i] = vn + a.theta * (vn - vo);
     }
 }
 
@@ -1051,32 +1062,42 @@ size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 template <int PREC>
-TgvArgs<typename Dual<PREC>::T> make_args(const TgvState& s, const TgvStep& k) {
+TgvArgs<typename Dual<PREC>::T> make_args(const TgvState& s, const TgvStep& k,
+                                          const TgvStencilFields& I, const float* u_in,
+                                          float* const* v_in, const TgvStencilFields& O,
+                                          float* u_out, float* const* v_out) {
     using T = typename Dual<PREC>::T;
-    const TgvStencilFields& F = s.set[0];
     TgvArgs<T> a;
     a.W = s.W;
     a.H = s.H;
     a.D = s.D;
     a.WH = (size_t)s.W * s.H;
     a.f = s.f;
-    a.u = s.u;
-    a.ubar = F.ubar;
-    a.v0 = s.v[0];
-    a.v1 = s.v[1];
-    a.v2 = s.v[2];
-    a.vb0 = F.vbar[0];
-    a.vb1 = F.vbar[1];
-    a.vb2 = F.vbar[2];
-    a.p0 = (T*)F.p[0];
-    a.p1 = (T*)F.p[1];
-    a.p2 = (T*)F.p[2];
-    a.qxx = (T*)F.q[0];
-    a.qyy = (T*)F.q[1];
-    a.qzz = (T*)F.q[2];
-    a.qxy = (T*)F.q[3];
-    a.qxz = (T*)F.q[4];
-    a.qyz = (T*)F.q[5];
+    a.u_in = u_in;
+    a.u = u_out;
+    a.ubar = I.ubar;
+    a.ubar_out = O.ubar;
+    for (int c = 0; c < 3; ++c) {
+        a.v_in[c] = v_in[c];
+        a.vbo[c] = O.vbar[c];
+        a.pin[c] = (const T*)I.p[c];
+    }
+    for (int c = 0; c < 6; ++c) a.qin[c] = (const T*)I.q[c];
+    a.v0 = v_out[0];
+    a.v1 = v_out[1];
+    a.v2 = v_out[2];
+    a.vb0 = I.vbar[0];
+    a.vb1 = I.vbar[1];
+    a.vb2 = I.vbar[2];
+    a.p0 = (T*)O.p[0];
+    a.p1 = (T*)O.p[1];
+    a.p2 = (T*)O.p[2];
+    a.qxx = (T*)O.q[0];
+    a.qyy = (T*)O.q[1];
+    a.qzz = (T*)O.q[2];
+    a.qxy = (T*)O.q[3];
+    a.qxz = (T*)O.q[4];
+    a.qyz = (T*)O.q[5];
     a.tau = k.tau;
     a.sigma = k.sigma;
     a.theta = k.theta;
@@ -1092,8 +1113,8 @@ TgvArgs<typename Dual<PREC>::T> make_args(const TgvState& s, const TgvStep& k) {
 }
 
 template <int PREC>
-void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
-    const auto a = make_args<PREC>(s, k);
+void launch_two_pass(const TgvState& s, const TgvStep& k,
+                     const TgvArgs<typename Dual<PREC>::T>& a, cudaStream_t st) {
     const dim3 block(BX, BY, 1);
     const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
     if (s.three) {
@@ -1112,6 +1133,14 @@ void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
     TGV_CHECK_LAUNCH();
 }
 
+template <int PREC>
+void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
+    const TgvStencilFields& F = s.set[0];
+    float* const v[3] = {s.v[0], s.v[1], s.v[2]};
+    const auto a = make_args<PREC>(s, k, F, s.u, v, F, s.u, v);
+    launch_two_pass<PREC>(s, k, a, st);
+}
+
 constexpr int FUSED_TY = 8;
 
 template <int PREC, bool THREE, int DATA>
@@ -1128,6 +1157,7 @@ void launch_fused(const FusedArgs<typename Dual<PREC>::T>& a, int D, cudaStream_
     kern<<<grid, fused_threads<TY>(), smem, st>>>(a);
     TGV_CHECK_LAUNCH();
 }
+
 
 // ---- TMA launch plumbing -----------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -1367,6 +1397,43 @@ void tgv_state_init(TgvState& s, cudaStream_t st) {
 }
 
 bool tgv_uses_tma(const TgvState& s) { return tma_shape_ok(s); }
+
+namespace {
+TgvStencilFields stencil_view(const TgvFullDev& d) {
+    TgvStencilFields F;
+    F.ubar = d.ubar;
+    for (int c = 0; c < 3; ++c) F.vbar[c] = d.vbar[c], F.p[c] = d.p[c];
+    for (int c = 0; c < 6; ++c) F.q[c] = d.q[c];
+    return F;
+}
+}  // namespace
+
+void tgv_step_fp32(const TgvState& s, const TgvStep& k, const TgvFullDev& in,
+                   const TgvFullDev& out, cudaStream_t st) {
+    TGV_REQUIRE(s.precision == TGVDCT_STATE_FP32 && s.three,
+                "the reverse mode needs FP32 state and 3-D geometry");
+    float* const vi[3] = {in.v[0], in.v[1], in.v[2]};
+    float* const vo[3] = {out.v[0], out.v[1], out.v[2]};
+    const auto a = make_args<TGVDCT_STATE_FP32>(s, k, stencil_view(in), in.u, vi,
+                                                stencil_view(out), out.u, vo);
+    launch_two_pass<TGVDCT_STATE_FP32>(s, k, a, st);
+}
+
+void tgv_save_state(const TgvState& s, const TgvFullDev& out, cudaStream_t st) {
+    TGV_REQUIRE(s.precision == TGVDCT_STATE_FP32 && s.three,
+                "the reverse mode needs FP32 state and 3-D geometry");
+    const size_t b = (size_t)s.W * s.H * s.D * 4;
+    const TgvStencilFields& F = s.now();
+    TGV_CUDA(cudaMemcpyAsync(out.u, s.u, b, cudaMemcpyDeviceToDevice, st));
+    TGV_CUDA(cudaMemcpyAsync(out.ubar, F.ubar, b, cudaMemcpyDeviceToDevice, st));
+    for (int c = 0; c < 3; ++c) {
+        TGV_CUDA(cudaMemcpyAsync(out.v[c], s.v[c], b, cudaMemcpyDeviceToDevice, st));
+        TGV_CUDA(cudaMemcpyAsync(out.vbar[c], F.vbar[c], b, cudaMemcpyDeviceToDevice, st));
+        TGV_CUDA(cudaMemcpyAsync(out.p[c], F.p[c], b, cudaMemcpyDeviceToDevice, st));
+    }
+    for (int c = 0; c < 6; ++c)
+        TGV_CUDA(cudaMemcpyAsync(out.q[c], F.q[c], b, cudaMemcpyDeviceToDevice, st));
+}
 
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     if (tma_shape_ok(s)) {

@@ -186,6 +186,28 @@ tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* ctx, const float* f_dev, float
                                   float* v_x_dev, float* v_y_dev, float* v_z_dev,
                                   tgvdct_iteration_callback callback, void* user, void* stream);
 
+/* ---- reverse mode (no counterpart in the reference) ------------------------ */
+/* The loop of tgvdct_tgv2_run_dev (iteration_count iterations from u = ubar = f),
+   keeping a copy of the full state every `checkpoint_every` iterations on the
+   context for tgvdct_tgv2_backward_dev.  Needs FP32 state and 3-D geometry.
+   Device memory: ceil(K / checkpoint_every) states of 17 fields. */
+tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* ctx, const float* f_dev,
+                                                   float* u_dev, float* v_x_dev,
+                                                   float* v_y_dev, float* v_z_dev,
+                                                   uint32_t checkpoint_every, void* stream);
+/* Gradient of a loss through the last checkpointed forward run of this context:
+   given dL/du_K (and dL/dv_K, each may be NULL for zero), writes dL/df to
+   grad_f_dev and (dL/dlambda, dL/dalpha0, dL/dalpha1) as three doubles to
+   grad_params_dev.  Recomputes each segment from its checkpoint (checkpoint_every
+   + 1 further states of device memory) and runs the adjoint iteration backwards:
+   the transposes of the difference operators and the Jacobians of the
+   projections and of the prox (taken on the branch the forward run took).
+   The context's f (from the forward call) and parameters must be unchanged. */
+tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* ctx, const float* grad_u_dev,
+                                       const float* grad_v_x_dev, const float* grad_v_y_dev,
+                                       const float* grad_v_z_dev, float* grad_f_dev,
+                                       double* grad_params_dev, void* stream);
+
 /* ---- Poisson integration of v (DCT-II / DCT-III) -------------------------- */
 /* Each replaces the host-in/host-out launcher of the same name:
    divergence_kernel_launch (cuda_image_operations/divergence.cu:59-61; depth == 1

@@ -56,6 +56,9 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = [p, p, p, _u, _u, _u, p]
             fn = getattr(L, f"oracle_deshade_epilogue_{suf}")
             fn.argtypes = [p, p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
+        vp = ctypes.c_void_p
+        L.oracle_tgv2_gradient_f64.argtypes = [_f64p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d,
+                                               ctypes.c_int, vp, vp, vp, vp, _f64p, _f64p, vp]
         _lib = L
     return _lib
 
@@ -165,6 +168,29 @@ def process_tgv2_l1(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *,
     l = integrate_poisson_dct(vx, vy, vz)
     r, _ = deshade_epilogue(u, l, None, set_negative_values_to_zero, False)
     return u, l, r
+
+
+def tgv2_gradient(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=10, *, grad_u=None,
+                  grad_v=None, data_term="l1", tau=0.0, sigma=0.0, theta=1.0):
+    """FP64 reverse mode of the 3-D loop: returns (u_K, dL/df, dL/d(lambda, alpha0, alpha1))
+    for the loss gradient grad_u = dL/du_K (and grad_v = (dL/dv_x, dL/dv_y, dL/dv_z))."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    w, h, d = _shape3(f)
+    gf = np.empty_like(f)
+    gp = np.zeros(3)
+    u = np.empty_like(f)
+
+    def ptr(a):
+        return None if a is None else np.ascontiguousarray(a, np.float64).ctypes.data_as(
+            ctypes.c_void_p)
+
+    keep = [None if a is None else np.ascontiguousarray(a, np.float64)
+            for a in ([grad_u] + list(grad_v or (None, None, None)))]
+    dt = 0 if data_term in ("l1", 0) else 1
+    lib().oracle_tgv2_gradient_f64(f, w, h, d, lambda_, alpha0, alpha1, iterations, tau, sigma,
+                                   theta, dt, *[ptr(a) for a in keep], gf, gp,
+                                   u.ctypes.data_as(ctypes.c_void_p))
+    return u, gf, gp
 
 
 # ---------------------------------------------------------------------------

@@ -1,5 +1,6 @@
 // TEST INFRASTRUCTURE — extern "C" entry points of the CPU oracle (tgv_oracle.hpp),
 // loaded by tests/ and bench.py's CPU-baseline leg through ctypes.  Not product code.
+#include "tgv_adjoint.hpp"
 #include "tgv_oracle.hpp"
 
 #ifdef _OPENMP
@@ -77,5 +78,25 @@ ORACLE_TYPED(float, f32)
 ORACLE_TYPED(double, f64)
 
 #undef ORACLE_TYPED
+
+// FP64 reverse mode through K iterations (tgv_adjoint.hpp).  gu / gv* may be null.
+// grad_params: d/dlambda, d/dalpha0, d/dalpha1.
+void oracle_tgv2_gradient_f64(const double* f, unsigned w, unsigned h, unsigned d, double lambda,
+                              double alpha0, double alpha1, unsigned K, double tau, double sigma,
+                              double theta, int data_term, const double* gu, const double* gvx,
+                              const double* gvy, const double* gvz, double* grad_f,
+                              double* grad_params, double* u_out) {
+    oracle::StepParams k;
+    k.tau = tau > 0 ? tau : oracle::default_step();
+    k.sigma = sigma > 0 ? sigma : oracle::default_step();
+    k.theta = theta;
+    k.lambda = lambda;
+    k.alpha0 = alpha0;
+    k.alpha1 = alpha1;
+    k.data_term = data_term;
+    k.skip_bz = data_term == oracle::L2 && d == 1;
+    const double* gv[3] = {gvx, gvy, gvz};
+    oracle::tgv2_gradient<double>(f, dims(w, h, d), k, K, gu, gv, grad_f, grad_params, u_out);
+}
 
 }  // extern "C"

@@ -1,0 +1,150 @@
+"""The CUDA reverse mode against the FP64 unrolled oracle gradient and against
+central finite differences of the CUDA forward loop."""
+import numpy as np
+import pytest
+
+import ambient_image_processor_gb300 as pkg
+import oracle
+from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _tensors(*arrays):
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in arrays]
+
+
+@pytest.mark.parametrize("alphas", [(2.0, 1.0), (0.01, 0.05)])
+@pytest.mark.parametrize("shape,data_term,K,every", [
+    ((6, 10, 12), pkg.DATA_L1, 15, 4),
+    ((7, 9, 16), pkg.DATA_L2, 12, 5),
+    ((1, 20, 24), pkg.DATA_L1, 16, 16),
+    ((1, 20, 24), pkg.DATA_L2, 9, 2),
+])
+def test_adjoint_matches_fp64_oracle(gpu_lib, alphas, shape, data_term, K, every):
+    import torch
+    from ambient_image_processor_gb300.autograd import tgv_denoise
+
+    rng = np.random.default_rng(3)
+    f = np.log(tissue_phantom_3d(*shape, seed=13, noise=0.05))
+    target = f + 0.05 * rng.standard_normal(shape)
+    cv = [0.01 * rng.standard_normal(shape) for _ in range(3)]
+    a0, a1 = alphas
+    lam = 1.1
+    ft, tt = _tensors(f, target)
+    ft.requires_grad_(True)
+    p = [torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+         for x in (a0, a1, lam)]
+    u, v = tgv_denoise(ft, p[0], p[1], p[2], K, every, data_term)
+    loss = 0.5 * ((u - tt) ** 2).sum() + sum((v[c] * _tensors(cv[c])[0]).sum() for c in range(3))
+    loss.backward()
+    uo = u.detach().cpu().numpy().astype(np.float64)
+    # the FP64 oracle's gradient of the same loss at the same point
+    _, gf, gp = oracle.tgv2_gradient(f.astype(np.float64), lam, a0, a1, K,
+                                     grad_u=uo - target, grad_v=cv,
+                                     data_term="l1" if data_term == pkg.DATA_L1 else "l2")
+    assert rel_l2(ft.grad.cpu().numpy(), gf) < 1e-3
+    got = [p[2].grad.item(), p[0].grad.item(), p[1].grad.item()]  # lambda, alpha0, alpha1
+    for g, ref in zip(got, gp):
+        assert abs(g - ref) <= 1e-3 * max(abs(ref), 1e-2 * np.abs(gf).sum()), (got, gp)
+
+
+def test_adjoint_checkpoint_stride_does_not_change_the_gradient(gpu_lib):
+    import torch
+    from ambient_image_processor_gb300.autograd import tgv_denoise
+
+    f = np.log(tissue_phantom_3d(9, 12, 20, seed=14))
+    grads = []
+    for every in (1, 3, 7, 30):
+        ft = _tensors(f)[0].requires_grad_(True)
+        lam = torch.tensor(1.0, device="cuda", requires_grad=True)
+        u, v = tgv_denoise(ft, 2.0, 1.0, lam, 30, every)
+        (u ** 2).sum().backward()
+        grads.append((ft.grad.cpu().numpy(), lam.grad.item()))
+    for g, l in grads[1:]:
+        assert np.array_equal(g, grads[0][0]) and l == pytest.approx(grads[0][1], rel=1e-6)
+
+
+def test_adjoint_finite_differences_96cube(gpu_lib):
+    """The 96^3 adjoint workload: 5-class phantom with noise 0.05, K = 200, checkpoints
+    every 20, loss = 1/2 |u_K - clean|^2, central differences with h = 1e-3.
+    Single input voxels are differenced through the FP64 forward loop (the oracle): in
+    FP32 the rounding flips a 1e-3 perturbation leaves across the volume are ~10% of a
+    single voxel's signal.  The three scalars, and one random direction over all
+    voxels, are differenced through the CUDA forward loop (loss summed in FP64).
+    The denoiser uses the L2 data term: with the L1 prox the loss has kinks closer
+    than h = 1e-3 (test_adjoint_oracle.py checks the L1 adjoint at smaller h)."""
+    import torch
+    from ambient_image_processor_gb300.autograd import tgv_denoise
+
+    noisy, clean, _ = tissue_phantom_3d(96, 96, 96, bias=False, noise=0.05, rician=False, seed=4,
+                                        return_parts=True)
+    K, every, h = 200, 20, 1e-3
+    a0, a1, lam = 2.0, 1.0, 1.0
+    ft, ct = _tensors(noisy, clean)
+    ft.requires_grad_(True)
+    p = [torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+         for x in (a0, a1, lam)]
+    u, _ = tgv_denoise(ft, p[0], p[1], p[2], K, every, pkg.DATA_L2)
+    (0.5 * ((u - ct) ** 2).sum()).backward()
+    gf = ft.grad.cpu().numpy().astype(np.float64)
+    scale = np.sqrt(np.mean(gf ** 2))
+
+    # 16 seeded voxels, FP64 forward
+    f64, c64 = noisy.astype(np.float64), clean.astype(np.float64)
+
+    def loss64(fa):
+        uu = oracle.tgv2_deshade(fa, lam, a0, a1, K, data_term="l2", dtype=np.float64)[0]
+        return 0.5 * float(np.sum((uu - c64) ** 2))
+
+    rng = np.random.default_rng(44)
+    for j in rng.choice(noisy.size, 16, replace=False):
+        fp, fm = f64.copy(), f64.copy()
+        fp.flat[j] += h
+        fm.flat[j] -= h
+        fd = (loss64(fp) - loss64(fm)) / (2 * h)
+        assert abs(fd - gf.flat[j]) <= 1e-3 * max(abs(fd), scale), (j, fd, gf.flat[j])
+
+    # scalars and one random direction, CUDA forward
+    prm = pkg.default_params(width=96, height=96, depth=96, iteration_count=K,
+                             data_term=pkg.DATA_L2)
+    ctx = pkg.Context(prm)
+    uo = torch.empty_like(ct)
+    vx, vy, vz = (torch.empty_like(ct) for _ in range(3))
+
+    def loss(fa, a0_, a1_, lam_):
+        prm.alpha0, prm.alpha1, prm.lambda_ = a0_, a1_, lam_
+        ctx.set_params(prm)
+        ft2 = _tensors(fa)[0]
+        ctx.run_dev(ft2.data_ptr(), uo.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr())
+        torch.cuda.synchronize()
+        d = uo.double() - ct.double()
+        return 0.5 * float((d * d).sum())
+
+    # alpha0, alpha1, lambda: a 1e-3 step switches projections on or off at some voxels,
+    # so the h = 1e-3 quotient differs from the derivative by a few 1e-3 (FP64 and FP32
+    # alike); the FP64 quotient at h = 1e-6 is the derivative to ~1e-6
+    got = [p[2].grad.item(), p[0].grad.item(), p[1].grad.item()]  # lambda, alpha0, alpha1
+    base = [lam, a0, a1]
+
+    def loss64p(pv):
+        uu = oracle.tgv2_deshade(f64, pv[0], pv[1], pv[2], K, data_term="l2",
+                                 dtype=np.float64)[0]
+        return 0.5 * float(np.sum((uu - c64) ** 2))
+
+    for k in range(3):
+        for hh, tol, fn in ((1e-6, 1e-4, loss64p),
+                            (h, 1e-2, lambda pv: loss(noisy, pv[1], pv[2], pv[0]))):
+            bp, bm = list(base), list(base)
+            bp[k] += hh
+            bm[k] -= hh
+            fd = (fn(bp) - fn(bm)) / (2 * hh)
+            assert abs(fd - got[k]) <= tol * max(abs(fd), 1.0), (k, hh, fd, got[k])
+    # one random direction over all voxels (every projection near its switch feels a
+    # volume-wide step, so this one goes through FP64 at h = 1e-6 too)
+    delta = rng.choice([-1.0, 1.0], size=noisy.shape)
+    hh = 1e-6
+    fd = (loss64(f64 + hh * delta) - loss64(f64 - hh * delta)) / (2 * hh)
+    assert abs(fd - float(np.sum(gf * delta))) <= 1e-4 * abs(fd), (fd, np.sum(gf * delta))
