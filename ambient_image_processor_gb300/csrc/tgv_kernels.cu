@@ -629,19 +629,27 @@ __host__ __device__ constexpr int a128(int b) { return (b + 127) / 128 * 128; }
 template <int PREC>
 struct Geo {
     static constexpr int DES = PREC == TGVDCT_STATE_FP32 ? 4 : 2;  // dual element bytes
-    static constexpr int XO_F = 4, BW_F = TX + 8;                  // FP32 boxes: x0-4 .. x0+35
-    static constexpr int XO_D = DES == 4 ? 4 : 8;                  // 16-bit boxes: x0-8 .. x0+39
-    static constexpr int BW_D = DES == 4 ? TX + 8 : TX + 16;
+    // ubar / vbar boxes: x0-4 .. x0+35, rows y0-1 .. y0+8 (the dual steps read the
+    // +x/+y neighbours of ubar and the -x/-y neighbours of vbar)
+    static constexpr int XO_F = 4, BW_F = TX + 8;
+    // p is read only at R_p (x0-1 .. x0+31, y0-1 .. y0+7) and q only at R_q
+    // (x0 .. x0+32, y0 .. y0+8): nine rows each, x start and width rounded to 16 bytes
+    static constexpr int PQ_ROWS = TY + 1;
+    static constexpr int XO_P = DES == 4 ? 4 : 8;
+    static constexpr int BW_P = DES == 4 ? TX + 4 : TX + 8;  // x0-XO_P .. x0+31
+    static constexpr int BW_Q = DES == 4 ? TX + 4 : TX + 8;  // x0 .. x0+35 (x0+39)
     static constexpr int BOX_F = a128(BW_F * EYH * 4);
-    static constexpr int BOX_D = a128(BW_D * EYH * DES);
-    // stage: ubar, vbar[3] | p[3], q[6]
+    static constexpr int BOX_P = a128(BW_P * PQ_ROWS * DES);
+    static constexpr int BOX_Q = a128(BW_Q * PQ_ROWS * DES);
+    // stage: ubar, vbar[3] | p[3] | q[6]
     static constexpr int OFF_P = 4 * BOX_F;
-    static constexpr int OFF_Q = OFF_P + 3 * BOX_D;
-    static constexpr int STAGE = OFF_Q + 6 * BOX_D;
+    static constexpr int OFF_Q = OFF_P + 3 * BOX_P;
+    static constexpr int STAGE = OFF_Q + 6 * BOX_Q;
     // bytes the TMA delivers per plane (what expect_tx must announce)
     static constexpr uint32_t tx_bytes(bool three) {
         const int nc = three ? 3 : 2, nq = three ? 6 : 3;
-        return (uint32_t)((1 + nc) * BW_F * EYH * 4 + (nc + nq) * BW_D * EYH * DES);
+        return (uint32_t)((1 + nc) * BW_F * EYH * 4 + nc * BW_P * PQ_ROWS * DES +
+                          nq * BW_Q * PQ_ROWS * DES);
     }
 };
 
@@ -810,17 +818,18 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     const size_t col = in_dom ? (size_t)y * a.W + x : 0;
 
     const int of = ey * G::BW_F + ex + G::XO_F - 1;  // offset in FP32 stencil boxes
-    const int od = ey * G::BW_D + ex + G::XO_D - 1;  // offset in dual boxes
+    const int odp = ey * G::BW_P + ex + G::XO_P - 1;  // offset in p boxes (R_p only)
+    const int odq = (ey - 1) * G::BW_Q + ex - 1;      // offset in q boxes (R_q only)
     auto st_of = [&](int plane) { return stages + ((plane - pbase) % NS) * G::STAGE; };
     // field views of a stage (st: the stage's base)
     auto fb = [&](const uint8_t* st, int field) -> const float* {  // 0 ubar, 1-3 vbar
         return (const float*)(st + field * G::BOX_F);
     };
     auto pb = [&](const uint8_t* st, int c) -> const T* {
-        return (const T*)(st + G::OFF_P + c * G::BOX_D);
+        return (const T*)(st + G::OFF_P + c * G::BOX_P);
     };
     auto qb = [&](const uint8_t* st, int k) -> const T* {
-        return (const T*)(st + G::OFF_Q + k * G::BOX_D);
+        return (const T*)(st + G::OFF_Q + k * G::BOX_Q);
     };
     auto Pslot = [&](int plane) { return sP + (plane & 1) * 3 * NE; };  // [3][NE]
     auto Qslot = [&](int plane) { return sQ + (plane % 3) * 6 * NE; };  // [6][NE]
@@ -845,11 +854,11 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
                      "r"(G::tx_bytes(THREE))
                      : "memory");
-        const int xf = x0 - G::XO_F, xd = x0 - G::XO_D, yb = y0 - 1;
+        const int xf = x0 - G::XO_F, xp = x0 - G::XO_P, yb = y0 - 1;
         tma_load(st, &a.maps.ub, xf, yb, plane, bar);
         for (int c = 0; c < NC; ++c) tma_load(st + (1 + c) * G::BOX_F, &a.maps.vb[c], xf, yb, plane, bar);
-        for (int c = 0; c < NC; ++c) tma_load(st + G::OFF_P + c * G::BOX_D, &a.maps.p[c], xd, yb, plane, bar);
-        for (int k = 0; k < NQ; ++k) tma_load(st + G::OFF_Q + k * G::BOX_D, &a.maps.q[k], xd, yb, plane, bar);
+        for (int c = 0; c < NC; ++c) tma_load(st + G::OFF_P + c * G::BOX_P, &a.maps.p[c], xp, yb, plane, bar);
+        for (int k = 0; k < NQ; ++k) tma_load(st + G::OFF_Q + k * G::BOX_Q, &a.maps.q[k], x0, y0, plane, bar);
     };
     bool ok = true;
     int waited_upto = pbase - 1;  // every plane <= this one has landed
@@ -869,7 +878,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         float vb[3] = {fb(sz, 1)[of], fb(sz, 2)[of], THREE ? fb(sz, 3)[of] : 0.f};
         float pp[3];
 #pragma unroll
-        for (int c = 0; c < NC; ++c) pp[c] = dec_p(pb(sz, c)[od]);
+        for (int c = 0; c < NC; ++c) pp[c] = dec_p(pb(sz, c)[odp]);
         dual_p_update<THREE>(g, vb, pp, a.sigma, a.alpha1);
 #pragma unroll
         for (int c = 0; c < NC; ++c) pp[c] = rq_p(pp[c]);
@@ -888,7 +897,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             zm[c] = (THREE && sm) ? fb(sm, 1 + c)[of] : 0.f;
         }
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) q[k] = dec_q(qb(sz, k)[od]);
+        for (int k = 0; k < NQ; ++k) q[k] = dec_q(qb(sz, k)[odq]);
         dual_q_update<THREE>(vb, xm, ym, zm, q, a.sigma, a.alpha0);
 #pragma unroll
         for (int k = 0; k < NQ; ++k) out[k * NE + e] = rq_q(q[k]);
@@ -957,10 +966,6 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         const bool p_next = t + 1 < z1;                  // p_new(t+1) feeds primal(t+1)
         const bool q_next = t + 2 <= z1 && t + 2 < D;    // q_new(t+2) feeds primal(t+1)
         if (p_next || q_next) wait_plane(min(t + 2, plast));
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
-        }
         const int slot2 = slot1 + 1 == NS ? 0 : slot1 + 1;
         const uint8_t* S1 = stages + slot1 * G::STAGE;   // plane t + 1
         const uint8_t* S2 = stages + slot2 * G::STAGE;   // plane t + 2
@@ -970,6 +975,9 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         const float* Qt = sQ + qslot * 6 * NE;           // q_new(t)
         const float* Qn = sQ + q1 * 6 * NE;              // q_new(t + 1)
         float* Qnn = sQ + q2 * 6 * NE;                   // q_new(t + 2)
+        // A thread whose wait gave up skips the plane; the barrier below shares the
+        // outcome and the whole block leaves together.
+        if (ok) {
         const float pu = tu, pf = tf, pv0 = tv[0], pv1 = tv[1], pv2 = tv[2];
         load_tile(t + 1);
         // ---- duals for the next planes
@@ -1041,7 +1049,11 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             Pn[NE + e] = pn.y;
             if constexpr (THREE) Pn[2 * NE + e] = pn.z;
         }
-        __syncthreads();
+        }  // ok
+        // The block's one barrier per plane: the rings written above become readable,
+        // and the stage of plane t + 1 is no longer read.
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
         if (tid == PRODUCER) issue(++issued_upto);  // plane t+1 is dead: its slot takes t+1+NS
         slot1 = slot2;
         pslot ^= 1;
@@ -1202,7 +1214,7 @@ struct TmaCache {
 
 template <int PREC>
 constexpr int tma_stages() {
-    return PREC == TGVDCT_STATE_FP32 ? 3 : 4;
+    return PREC == TGVDCT_STATE_FP32 ? 4 : 5;
 }
 
 template <int PREC>
@@ -1227,10 +1239,10 @@ TmaCache<PREC>* tma_cache(TgvState& s) {
             encode_box(&a.maps.ub, I.ubar, 4, s, G::BW_F, tma::EYH);
             for (int c2 = 0; c2 < NC; ++c2) {
                 encode_box(&a.maps.vb[c2], I.vbar[c2], 4, s, G::BW_F, tma::EYH);
-                encode_box(&a.maps.p[c2], I.p[c2], G::DES, s, G::BW_D, tma::EYH);
+                encode_box(&a.maps.p[c2], I.p[c2], G::DES, s, G::BW_P, G::PQ_ROWS);
             }
             for (int k = 0; k < NQ; ++k)
-                encode_box(&a.maps.q[k], I.q[qmap[k]], G::DES, s, G::BW_D, tma::EYH);
+                encode_box(&a.maps.q[k], I.q[qmap[k]], G::DES, s, G::BW_Q, G::PQ_ROWS);
             a.f = s.f;
             a.W = s.W;
             a.H = s.H;

@@ -42,12 +42,9 @@ WORKLOADS = {
 # algorithmic bytes per voxel-iteration of one TGV2 iteration (read f, u, ubar, v3,
 # vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
 ALGO_BYTES = {0: 140, 1: 104, 2: 104}
-# bytes an iteration moves: two-pass (dual 13 loads + 9 stores, primal 14 + 8) and
-# fused (18 loads + 17 stores, halo re-reads served by L2)
-PASS_BYTES = {"two_pass": {0: 176, 1: 140, 2: 140}, "fused": {0: 140, 1: 104, 2: 104}}
 KERNELS = {"fused": 2, "two_pass": 1}
-KERNEL_NAMES = {"fused": "tgv_fused_kernel", "two_pass": "tgv_dual_kernel + tgv_primal_kernel"}
 PREC_NAMES = {0: "fp32", 1: "bf16_dual", 2: "fx16_dual"}
+DCT_MODES = {"fp32": 0, "tf32": 1, "bf16x3": 2}
 
 
 def env_int(name, default):
@@ -146,7 +143,7 @@ def run_reference_arm(args):
     f = make_input(args.workload)
     d, h, w, iters = WORKLOADS[args.workload]
     # bounded sample: a few iterations of the same volume per step
-    sample_it = args.cpu_sample_iterations
+    sample_it = args.ref_sample_iterations
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_reference(args, f, 1)
     rates, cores = [], 1
@@ -175,6 +172,97 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------------------------
+# DRAM bytes (read + write) of one launch of the fused TMA kernel on this workload,
+# FP32 state, from the ncu capture summarised in
+# profiles/tgv_fused_tma_kernel_deshade_256x256x192.md (dram__bytes_read.sum +
+# dram__bytes_write.sum).
+TRAFFIC_FUSED_FP32_256x256x192 = 920454400 + 808067328
+
+
+def time_iterations(pkg, torch, w, h, d, f, kernel, precision, n_it, stream):
+    """Milliseconds per iteration of the TGV loop alone (CUDA events on `stream`)."""
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=n_it,
+                             state_precision=precision, iteration_kernel=KERNELS[kernel])
+    u, vx, vy, vz = (torch.empty_like(f) for _ in range(4))
+    with pkg.Context(prm) as ctx:
+        def run():
+            ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr(),
+                        stream=stream.cuda_stream)
+        run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.check_device_error(stream.cuda_stream)
+    return e0.elapsed_time(e1) / n_it
+
+
+def time_dct_poisson(pkg, torch, stream, n=256, reps=10):
+    """The 256^3 DCT Poisson solve per precision mode: ms per solve and flop rate
+    (12 N^4 flops of the six contractions; three times that in tensor flops for BF16x3)."""
+    from ambient_image_processor_gb300.phantoms import cosine_modes_rhs
+    rhs = torch.from_numpy(cosine_modes_rhs(n, n, n, seed=3)).cuda()
+    out = torch.empty_like(rhs)
+    res = {}
+    for mode, name in ((pkg.DCT_FP32, "fp32"), (pkg.DCT_TF32, "tf32"), (pkg.DCT_BF16X3, "bf16x3")):
+        prm = pkg.default_params(width=n, height=n, depth=n, dct_mode=mode,
+                                 poisson_eigen=pkg.EIGEN_ACCURATE)
+        with pkg.Context(prm) as ctx:
+            for _ in range(3):
+                ctx.poisson_solve_dev(rhs.data_ptr(), out.data_ptr(), stream.cuda_stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                ctx.poisson_solve_dev(rhs.data_ptr(), out.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ctx.check_device_error(stream.cuda_stream)
+        ms = e0.elapsed_time(e1) / reps
+        flops = 12.0 * n ** 4
+        res[name] = {"ms": ms, "useful_tflops": flops / (ms * 1e-3) / 1e12,
+                     "hbm_gbs": 48.0 * n ** 3 / (ms * 1e-3) / 1e9}
+    return res
+
+
+def time_adjoint(pkg, torch, stream, n=96, K=200, every=20):
+    """Backward over forward time of the checkpointed reverse mode (96^3, K = 200)."""
+    from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
+    f = torch.from_numpy(tissue_phantom_3d(n, n, n, bias=False, noise=0.05, rician=False,
+                                           seed=4)).cuda()
+    prm = pkg.default_params(width=n, height=n, depth=n, iteration_count=K)
+    u, vx, vy, vz, gu, gf = (torch.empty_like(f) for _ in range(6))
+    gu.normal_()
+    gp = torch.empty(3, dtype=torch.float64, device=f.device)
+    sh = stream.cuda_stream
+    with pkg.Context(prm) as ctx:
+        calls = {
+            "forward": lambda: ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(),
+                                           vy.data_ptr(), vz.data_ptr(), stream=sh),
+            "forward_checkpointed": lambda: ctx.forward_checkpointed_dev(
+                f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr(), every,
+                sh),
+            "backward": lambda: ctx.backward_dev(gu.data_ptr(), None, None, None, gf.data_ptr(),
+                                                 gp.data_ptr(), sh),
+        }
+        for fn in calls.values():
+            fn()
+        torch.cuda.synchronize()
+        out = {}
+        for name, fn in calls.items():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out[name + "_ms"] = e0.elapsed_time(e1)
+    out["backward_over_forward"] = out["backward_ms"] / out["forward_ms"]
+    out["workload"] = f"{n}^3, K = {K}, checkpoints every {every}"
+    return out
+
+
 def run_ours(args):
     import torch
     import ambient_image_processor_gb300 as pkg
@@ -195,7 +283,7 @@ def run_ours(args):
     V = d * h * w
     f_host = make_input(args.workload)
     prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iters,
-                             state_precision=args.precision, dct_mode=pkg.DCT_FP32,
+                             state_precision=args.precision, dct_mode=DCT_MODES[args.dct],
                              poisson_eigen=args.eigen, iteration_kernel=KERNELS[args.kernel],
                              z_chunk=args.z_chunk)
     stream = torch.cuda.current_stream()
@@ -213,6 +301,7 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
+    # ---- the headline: whole deshades, input resident in HBM (state 1.6 GB > L2)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -227,41 +316,27 @@ def run_ours(args):
         torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
+    ctx.check_device_error(sh)
     ms = ev0.elapsed_time(ev1) / args.steps
     if dist is not None:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * V * iters / (ms * 1e-3)
+    ctx.close()
 
-    # ---- roofline of the iteration kernels: iterations alone, events on the stream
-    n_prof = args.profile_iterations
-    prm_it = pkg.default_params(width=w, height=h, depth=d, iteration_count=n_prof,
-                                state_precision=args.precision,
-                                iteration_kernel=KERNELS[args.kernel], z_chunk=args.z_chunk)
-    ctx.set_params(prm_it)
-    vx, vy, vz = (torch.empty_like(f) for _ in range(3))
-
-    def iters_only():
-        ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr(),
-                    stream=sh)
-
-    iters_only()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    iters_only()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    it_ms = e0.elapsed_time(e1) / n_prof
+    # ---- roofline of the iteration kernel, timed alone on its stream
+    it_ms = time_iterations(pkg, torch, w, h, d, f, args.kernel, args.precision,
+                            args.profile_iterations, stream)
     launches_per_it = 1 if args.kernel == "fused" else 2
-    launch_ms = it_ms / launches_per_it
     peak, peak_kind = hbm_peak()
     algo = ALGO_BYTES[args.precision]
-    achieved = algo * V / (it_ms * 1e-3) / 1e9  # GB/s of algorithmic bytes per iteration
+    achieved = algo * V / (it_ms * 1e-3) / 1e9  # algorithmic bytes of one iteration per second
+    traffic = (TRAFFIC_FUSED_FP32_256x256x192
+               if (args.kernel, args.precision, args.workload) == ("fused", 0, "deshade_256x256x192")
+               else None)
 
     # ---- e2e through the host-buffer C-ABI call (reference-facing)
-    ctx.set_params(prm)
     e2e_ms = None
     if not args.no_e2e:
         fh = np.ascontiguousarray(f_host)
@@ -282,6 +357,18 @@ def run_ours(args):
 
     line = None
     if rank == 0:
+        extra = {}
+        if not args.no_variants:
+            var = {}
+            for kernel, prec in (("two_pass", 0), ("fused", 0), ("two_pass", 2), ("fused", 2),
+                                 ("fused", 1)):
+                t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 40, stream)
+                var[f"{kernel}_{PREC_NAMES[prec]}"] = {
+                    "ms_per_iteration": t, "voxel_iters_per_s": V / (t * 1e-3),
+                    "algorithmic_gbs": ALGO_BYTES[prec] * V / (t * 1e-3) / 1e9}
+            extra["iteration_variants"] = var
+            extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
+            extra["adjoint"] = time_adjoint(pkg, torch, stream)
         cpu = None
         if not args.no_cpu_baseline:
             rate, cores, dt = cpu_reference(args, f_host, args.cpu_sample_iterations)
@@ -296,10 +383,10 @@ def run_ours(args):
             "dtype": "f32" if args.precision == 0 else "f32+" + PREC_NAMES[args.precision],
             "data": "synthetic",
             "config": {"workload": args.workload, "shape_dhw": [d, h, w], "iterations": iters,
-                       "state_precision": PREC_NAMES[args.precision], "dct": "fp32",
+                       "state_precision": PREC_NAMES[args.precision], "dct": args.dct,
                        "poisson_eigen": "accurate" if args.eigen else "reference",
-                       "pass_structure": args.kernel,
-                       "l2": "state of 1.6 GB per replica, larger than L2",
+                       "iteration_kernel": args.kernel,
+                       "l2": "inputs larger than L2 (TGV state 1.6 GB per replica)",
                        "parallelism": f"replicas{world}"},
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_value, "unit": "voxel-iter/s",
@@ -307,16 +394,16 @@ def run_ours(args):
                     "ms_per_step": e2e_ms},
             "gpu_launches": gpu_launches * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": KERNEL_NAMES[args.kernel] + " (one iteration)",
-                         "algorithmic_bytes_per_voxel_iter": algo,
-                         "moved_bytes_per_voxel_iter": PASS_BYTES[args.kernel][args.precision],
-                         "iteration_ms": it_ms, "launch_ms": launch_ms,
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": ("tgv_fused_tma_kernel" if args.kernel == "fused"
+                                    else "tgv_dual_kernel + tgv_primal_kernel"),
+                         "algorithmic_bytes_per_launch": algo * V / launches_per_it,
+                         "launch_ms": it_ms / launches_per_it,
                          "peak_source": peak_kind},
             "cpu_baseline": cpu,
         }
+        line.update(extra)
         print(json.dumps(line))
-    ctx.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -331,14 +418,19 @@ def main():
     ap.add_argument("--workload", default="deshade_256x256x192", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", type=int, default=0, choices=[0, 1, 2])
     ap.add_argument("--eigen", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--dct", default="fp32", choices=sorted(DCT_MODES))
     ap.add_argument("--kernel", default="fused", choices=sorted(KERNELS))
     ap.add_argument("--z-chunk", type=int, default=0)
     ap.add_argument("--iterations", type=int, default=0, help="override the iteration count")
     ap.add_argument("--profile-iterations", type=int, default=200)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-sample-iterations", type=int, default=4)
+    ap.add_argument("--cpu-sample-iterations", type=int, default=100,
+                    help="iterations of the CPU baseline sample in the ours line (~10 s)")
+    ap.add_argument("--ref-sample-iterations", type=int, default=24,
+                    help="iterations per step of the reference arm's CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
