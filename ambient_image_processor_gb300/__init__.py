@@ -82,6 +82,18 @@ _SIGS = {
     "tgvdct_tgv2_forward_checkpointed_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _u32, _vp],
     "tgvdct_tgv2_backward_dev": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_divergence_launch": [_f32p, _f32p, _vp, _u32, _u32, _u32, _f32p],
+    "tgvdct_divergence_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp],
+    "tgvdct_set_domain_mask_dev": [_vp, _vp, _vp],
+    "tgvdct_process_tgv2_l1_masked": [ctypes.POINTER(Params), _f32p, _f32p, _i32, _i32, _i32,
+                                      CALLBACK, _vp, _f32p, _f32p, _f32p],
+    "tgvdct_tgv2_l1_deshade_masked_launch": [_f32p, _f32p, _u32, _u32, _u32, _flt, _u32, _u32,
+                                             ctypes.c_int, CALLBACK, _vp, _flt, _flt, _f32p,
+                                             _f32p, _f32p, _vp],
+    "tgvdct_device_alloc": [ctypes.c_size_t, ctypes.POINTER(_vp)],
+    "tgvdct_device_free": [_vp],
+    "tgvdct_host_to_device": [_vp, _vp, ctypes.c_size_t],
+    "tgvdct_device_to_host": [_vp, _vp, ctypes.c_size_t],
+    "tgvdct_tgv2_run": [ctypes.POINTER(Params), _f32p, _f32p, _vp, _vp, _vp, CALLBACK, _vp],
     "tgvdct_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
     "tgvdct_inverse_cosine_transform_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
     "tgvdct_solve_poisson_in_cosine_domain_launch": [_f32p, _u32, _u32, _u32, _i32, _f32p],
@@ -338,6 +350,59 @@ class TGVDeshadeProcessor:
 
 
 # ---------------------------------------------------------------------------
+class TGVDeshadeMaskedProcessor:
+    """Mirror of the reference's TGVDeshadeMaskedProcessor
+    (tgv_deshade_masked/TGVDeshadeMaskedProcessor.h) over numpy images: the TGV loop
+    runs on the voxels with mask >= 1 only."""
+
+    @staticmethod
+    def processTGV2L1GPUCuda(input_image, lambda_, alpha0, alpha1, iteration_count,
+                             cuda_block_dimension=-1, paint_iteration_interval=0,
+                             iteration_finished_callback=None, mask=None,
+                             set_negative_values_to_zero=True, add_background_back=False, *,
+                             log_domain=False, state_precision=STATE_FP32, dct_mode=DCT_FP32,
+                             poisson_eigen=EIGEN_REFERENCE, iteration_kernel=KERNEL_AUTO,
+                             z_chunk=0):
+        """TGVDeshadeMaskedProcessor::processTGV2L1GPUCuda
+        (TGVDeshadeMaskedProcessor.cpp:77-212; 2-D operators when depth == 1, :214-330).
+        A missing mask means every voxel (the reference substitutes an all-ones mask).
+        Returns (denoised_image, shading_image, deshaded_image); the callback gets
+        (iteration_index, iteration_count, u, l, r)."""
+        f = _f32(input_image)
+        w, h, d = _dims(f)
+        m = np.ones_like(f) if mask is None else _f32(mask)
+        if m.shape != f.shape:
+            raise ValueError("mask shape differs from the image shape")
+        p = default_params(width=w, height=h, depth=d, lambda_=lambda_, alpha0=alpha0,
+                           alpha1=alpha1, iteration_count=iteration_count,
+                           state_precision=state_precision, dct_mode=dct_mode,
+                           poisson_eigen=poisson_eigen,
+                           paint_iteration_interval=paint_iteration_interval,
+                           iteration_kernel=iteration_kernel, z_chunk=z_chunk)
+        u, l, r = (np.empty_like(f) for _ in range(3))
+        cb, keep = _make_callback(iteration_finished_callback, f.shape, 3)
+        _check(lib().tgvdct_process_tgv2_l1_masked(ctypes.byref(p), f, m,
+                                                   int(set_negative_values_to_zero),
+                                                   int(add_background_back), int(log_domain), cb,
+                                                   None, u, l, r))
+        del keep
+        return u, l, r
+
+
+def tgv2_l1_deshade_masked_launch(f, mask, lambda_, iteration_count, alpha0, alpha1):
+    """tgv2_l1_deshade_masked_launch / _2d_launch (tgv_deshade_masked/): the masked loop.
+    Returns (u, v_x, v_y, v_z); v_z is zero when depth == 1."""
+    f = _f32(f)
+    m = _f32(mask)
+    w, h, d = _dims(f)
+    u, vx, vy, vz = (np.empty_like(f) for _ in range(4))
+    _check(lib().tgvdct_tgv2_l1_deshade_masked_launch(f, m, w, h, d, lambda_, iteration_count, 0,
+                                                      -1, CALLBACK(), None, alpha0, alpha1, u,
+                                                      vx, vy, vz.ctypes.data_as(_vp)))
+    return u, vx, vy, vz
+
+
+# ---------------------------------------------------------------------------
 class Context:
     """A device workspace for one volume shape (tgvdct_context).
 
@@ -400,6 +465,11 @@ class Context:
     def poisson_solve_dev(self, rhs_ptr, l_ptr, stream=None):
         _check(lib().tgvdct_poisson_solve_dev(self._ctx, rhs_ptr, l_ptr, stream),
                allow_stop=False)
+
+    def set_domain_mask_dev(self, mask_ptr, stream=None):
+        """Restrict the loop to voxels with mask >= 1 (None clears); see
+        tgvdct_set_domain_mask_dev."""
+        _check(lib().tgvdct_set_domain_mask_dev(self._ctx, mask_ptr, stream), allow_stop=False)
 
     def check_device_error(self, stream=None):
         _check(lib().tgvdct_check_device_error(self._ctx, stream), allow_stop=False)

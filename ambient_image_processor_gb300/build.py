@@ -3,7 +3,9 @@
 Every CUDA translation unit is compiled by nvcc for ``sm_103a`` only, in
 parallel, then linked into ``ambient_image_processor_gb300/_build/libtgvdct.so``.
 No cmake, no torch extension machinery: the library exposes plain ``extern "C"``
-symbols declared in ``include/tgvdct.h``.
+symbols declared in ``include/tgvdct.h``.  On top of it, g++ builds the host-only
+reference-signature layer ``libtgvdct_refapi.so`` (``include/tgvdct_reference_api.hpp``)
+and the terminal program ``tgv2_deshade_application``.
 
     python -m ambient_image_processor_gb300.build
 """
@@ -20,6 +22,9 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libtgvdct.so")
+REFAPI = os.path.join(PKG, "refapi")
+REFAPI_LIB = os.path.join(OUT, "libtgvdct_refapi.so")
+CLI = os.path.join(OUT, "tgv2_deshade_application")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
@@ -79,7 +84,23 @@ def build(verbose: bool = False, force: bool = False, jobs: int = 8) -> str:
                 print(r.stderr)
     if force or cmds or _stale(LIB, objs):
         _run([nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs])
+    build_host(force)
     return LIB
+
+
+def build_host(force: bool = False) -> None:
+    """The host-only C++ on top of libtgvdct.so (portable flags: x86_64 and aarch64)."""
+    cxx = os.environ.get("CXX", "g++")
+    flags = ["-O2", "-std=c++17", "-Wall", "-Wextra", "-I", INCLUDE, "-I", REFAPI]
+    link = ["-L", OUT, "-ltgvdct", "-Wl,-rpath,$ORIGIN"]
+    hdrs = [os.path.join(INCLUDE, "tgvdct.h"), os.path.join(INCLUDE, "tgvdct_reference_api.hpp"),
+            os.path.join(REFAPI, "metaimage.hpp"), __file__]
+    api_src = [os.path.join(REFAPI, "reference_api.cpp")]
+    if force or _stale(REFAPI_LIB, [*api_src, *hdrs, LIB]):
+        _run([cxx, *flags, "-fPIC", "-shared", "-o", REFAPI_LIB, *api_src, *link])
+    cli_src = [os.path.join(REFAPI, "tgv2_deshade_main.cpp"), os.path.join(REFAPI, "metaimage.cpp")]
+    if force or _stale(CLI, [*cli_src, *hdrs, LIB]):
+        _run([cxx, *flags, "-o", CLI, *cli_src, *link])
 
 
 if __name__ == "__main__":

@@ -27,6 +27,10 @@ struct tgvdct_context {
     size_t host_cb_count = 0;
     // device scratch for the per-callback deshade of tgvdct_process_dev
     float* cb_dev = nullptr;
+    // masked deshade: the caller's mask (weights of the epilogue) and the domain
+    // derived from it (voxels with mask >= 1 are iterated)
+    float* domain_mask = nullptr;
+    uint8_t* domain = nullptr;
     // reverse mode: checkpoints of the last checkpointed forward run, the states of
     // one recomputed segment, and the adjoint state with its scratch fields
     void* ckpt_block = nullptr;
@@ -245,6 +249,8 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->adj_block) cudaFree(c->adj_block);
     if (c->state_block) cudaFree(c->state_block);
     if (c->cb_dev) cudaFree(c->cb_dev);
+    if (c->domain_mask) cudaFree(c->domain_mask);
+    if (c->domain) cudaFree(c->domain);
     if (c->host_cb) cudaFreeHost(c->host_cb);
     dct_plan_destroy(c->plan);
     delete c;
@@ -271,6 +277,36 @@ void require_reverse_mode(const tgvdct_context* c) {
         set_error("the reverse mode needs FP32 state and 3-D geometry");
         throw Error{TGVDCT_ERR_UNSUPPORTED};
     }
+    if (c->domain) {
+        set_error("the reverse mode does not support a domain mask");
+        throw Error{TGVDCT_ERR_UNSUPPORTED};
+    }
+}
+
+void set_domain(tgvdct_context* c, const float* mask_dev, cudaStream_t s) {
+    const size_t n = voxels(c->prm);
+    if (!mask_dev) {
+        TGV_CUDA(cudaStreamSynchronize(s));
+        if (c->domain_mask) TGV_CUDA(cudaFree(c->domain_mask));
+        if (c->domain) TGV_CUDA(cudaFree(c->domain));
+        c->domain_mask = nullptr;
+        c->domain = nullptr;
+        c->st.domain = nullptr;
+        return;
+    }
+    if (!c->domain) {
+        if (cudaMalloc(&c->domain_mask, n * 4) != cudaSuccess ||
+            cudaMalloc(&c->domain, n) != cudaSuccess) {
+            cudaGetLastError();
+            if (c->domain_mask) cudaFree(c->domain_mask);
+            c->domain_mask = nullptr;
+            set_error("device allocation of the domain mask failed");
+            throw Error{TGVDCT_ERR_OOM};
+        }
+    }
+    TGV_CUDA(cudaMemcpyAsync(c->domain_mask, mask_dev, n * 4, cudaMemcpyDeviceToDevice, s));
+    build_domain(c->domain_mask, n, c->domain, s);
+    c->st.domain = c->domain;
 }
 
 struct CtxGuard {
@@ -295,6 +331,10 @@ void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_
     TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
     if (log_domain) log_inplace(c->st.f, n, s);
     DctPlan* plan = plan_of(c);
+    // The masked processor weights l and r by its mask and, without the background
+    // add-back, multiplies r by it once more (TGVDeshadeMaskedProcessor.cpp:186-211).
+    const bool masked = c->domain != nullptr;
+    if (masked) mask_dev = c->domain_mask;
     const bool mask_shading = mask_dev != nullptr;
     const bool stopped = run_loop(c, s, cb != nullptr, [&](uint32_t it) {
         // The GUI module deshades at every paint interval and hands u, l, r to its
@@ -304,14 +344,14 @@ void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_
         float* r = c->cb_dev + n;
         poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, l,
                           c->prm.dct_mode, c->prm.poisson_eigen, s);
-        deshade_epilogue(c->st.u, l, mask_dev, n, mask_shading, clamp, add_back, r, s);
+        deshade_epilogue(c->st.u, l, mask_dev, n, mask_shading, clamp, add_back, r, s, masked);
         return deliver(c, cb, user, it, c->st.u, l, r, nullptr, s) != 0;
     });
     (void)stopped;
     TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
     poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, l_dev,
                       c->prm.dct_mode, c->prm.poisson_eigen, s);
-    deshade_epilogue(u_dev, l_dev, mask_dev, n, mask_shading, clamp, add_back, r_dev, s);
+    deshade_epilogue(u_dev, l_dev, mask_dev, n, mask_shading, clamp, add_back, r_dev, s, masked);
     if (log_domain) {
         exp_inplace(u_dev, n, s);
         exp_inplace(l_dev, n, s);
@@ -606,6 +646,33 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t wid
     });
 }
 
+tgvdct_status tgvdct_tgv2_run(const tgvdct_params* p, const float* f_host, float* u_host,
+                             float* v_x_host, float* v_y_host, float* v_z_host,
+                             tgvdct_iteration_callback callback, void* user) {
+    return guarded([&] {
+        TGV_REQUIRE(p && f_host && u_host, "null host buffer");
+        CtxGuard g;
+        create_into(p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(*p);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        const bool stopped = run_loop(c, s, callback != nullptr, [&](uint32_t it) {
+            return deliver(c, callback, user, it, c->st.u, c->st.v[0], c->st.v[1],
+                           c->st.three ? c->st.v[2] : nullptr, s) != 0;
+        });
+        TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        float* vh[3] = {v_x_host, v_y_host, v_z_host};
+        for (int k = 0; k < 3; ++k) {
+            if (!vh[k]) continue;
+            if (k == 2 && !c->st.three) std::memset(vh[k], 0, n * 4);
+            else TGV_CUDA(cudaMemcpyAsync(vh[k], c->st.v[k], n * 4, cudaMemcpyDeviceToHost, s));
+        }
+        check_tgv_flag(c, s);
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
 tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, uint32_t height,
                                          uint32_t depth, int32_t data_term, float lambda,
                                          uint32_t iteration_count, float alpha0, float alpha1,
@@ -649,6 +716,63 @@ tgvdct_status tgvdct_divergence_launch(const float* dx, const float* dy, const f
         if (depth > 1) TGV_CUDA(cudaMemcpy(c.p, dz, n * 4, cudaMemcpyHostToDevice));
         divergence(plan, a.p, b.p, c.p, o.p, 0);
         TGV_CUDA(cudaMemcpy(out, o.p, n * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+tgvdct_status tgvdct_device_alloc(size_t bytes, void** out) {
+    return guarded([&] {
+        TGV_REQUIRE(out, "null output pointer");
+        *out = nullptr;
+        check_device();
+        const cudaError_t e = cudaMalloc(out, bytes ? bytes : 1);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            return TGVDCT_ERR_OOM;
+        }
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_device_free(void* p) {
+    return guarded([&] {
+        if (p) TGV_CUDA(cudaFree(p));
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_host_to_device(void* dst_dev, const void* src_host, size_t bytes) {
+    return guarded([&] {
+        TGV_REQUIRE(dst_dev && src_host, "null buffer");
+        TGV_CUDA(cudaMemcpy(dst_dev, src_host, bytes, cudaMemcpyHostToDevice));
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_device_to_host(void* dst_host, const void* src_dev, size_t bytes) {
+    return guarded([&] {
+        TGV_REQUIRE(dst_host && src_dev, "null buffer");
+        TGV_CUDA(cudaMemcpy(dst_host, src_dev, bytes, cudaMemcpyDeviceToHost));
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_divergence_dev(const float* dx_dev, const float* dy_dev,
+                                    const float* dz_dev, uint32_t width, uint32_t height,
+                                    uint32_t depth, float* out_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(width >= 1 && height >= 1 && depth >= 1, "width, height, depth must be >= 1");
+        TGV_REQUIRE(dx_dev && dy_dev && out_dev && (dz_dev || depth == 1), "null device buffer");
+        check_device();
+        DctPlan* plan = dct_plan_create((int)width, (int)height, (int)depth);
+        struct PlanGuard {
+            DctPlan* p;
+            ~PlanGuard() { dct_plan_destroy(p); }
+        } pg{plan};
+        divergence(plan, dx_dev, dy_dev, depth > 1 ? dz_dev : nullptr, out_dev,
+                   (cudaStream_t)stream);
+        TGV_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        return TGVDCT_OK;
     });
 }
 
@@ -759,10 +883,98 @@ tgvdct_status tgvdct_process_dev(tgvdct_context* c, const float* f_dev, const fl
     return guarded([&] {
         TGV_REQUIRE(c != nullptr, "null context");
         TGV_REQUIRE(f_dev && u_dev && l_dev && r_dev, "null device buffer");
+        TGV_REQUIRE(!(c->domain && mask_dev),
+                    "a context with a domain mask uses it in the epilogue; pass mask_dev = NULL");
         process_on_device(c, f_dev, mask_dev, set_negative_values_to_zero != 0,
                           add_background_back != 0, log_domain != 0, u_dev, l_dev, r_dev, callback,
                           user, (cudaStream_t)stream);
         return c->iterations_run < c->prm.iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_set_domain_mask_dev(tgvdct_context* c, const float* mask_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        set_domain(c, mask_dev, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_process_tgv2_l1_masked(const tgvdct_params* p, const float* f_host,
+                                            const float* mask_host,
+                                            int32_t set_negative_values_to_zero,
+                                            int32_t add_background_back, int32_t log_domain,
+                                            tgvdct_iteration_callback callback, void* user,
+                                            float* denoised_host, float* shading_host,
+                                            float* deshaded_host) {
+    return guarded([&] {
+        TGV_REQUIRE(p && f_host && mask_host && denoised_host && shading_host && deshaded_host,
+                    "null host buffer");
+        tgvdct_params q = *p;
+        if (q.depth == 1) q.geometry = TGVDCT_GEOMETRY_2D;  // TGVDeshadeMaskedProcessor.cpp:94-99
+        CtxGuard g;
+        create_into(&q, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(q);
+        DevBuf f(n), m(n), u(n), l(n), r(n);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(f.p, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        set_domain(c, m.p, s);
+        process_on_device(c, f.p, nullptr, set_negative_values_to_zero != 0,
+                          add_background_back != 0, log_domain != 0, u.p, l.p, r.p, callback,
+                          user, s);
+        TGV_CUDA(cudaMemcpyAsync(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
+        check_tgv_flag(c, s);
+        return c->iterations_run < q.iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
+    const float* f_host, const float* mask_host, uint32_t width, uint32_t height, uint32_t depth,
+    float lambda, uint32_t iteration_count, uint32_t paint_iteration_interval,
+    int cuda_block_dimension, tgvdct_iteration_callback callback, void* user, float alpha0,
+    float alpha1, float* u_host, float* v_x_host, float* v_y_host, float* v_z_host) {
+    (void)cuda_block_dimension;
+    return guarded([&] {
+        TGV_REQUIRE(f_host && mask_host && u_host && v_x_host && v_y_host, "null host buffer");
+        tgvdct_params p;
+        tgvdct_params_init(&p);
+        p.width = width;
+        p.height = height;
+        p.depth = depth;
+        p.lambda = lambda;
+        p.alpha0 = alpha0;
+        p.alpha1 = alpha1;
+        p.iteration_count = iteration_count;
+        p.paint_iteration_interval = paint_iteration_interval;
+        if (depth == 1) p.geometry = TGVDCT_GEOMETRY_2D;
+        CtxGuard g;
+        create_into(&p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(p);
+        DevBuf m(n);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        set_domain(c, m.p, s);
+        const bool stopped = run_loop(c, s, callback != nullptr, [&](uint32_t it) {
+            return deliver(c, callback, user, it, c->st.u, c->st.v[0], c->st.v[1],
+                           c->st.three ? c->st.v[2] : nullptr, s) != 0;
+        });
+        TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
+        if (v_z_host) {
+            if (c->st.three)
+                TGV_CUDA(cudaMemcpyAsync(v_z_host, c->st.v[2], n * 4, cudaMemcpyDeviceToHost, s));
+            else
+                std::memset(v_z_host, 0, n * 4);
+        }
+        check_tgv_flag(c, s);
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
 

@@ -71,6 +71,10 @@ struct TgvState {
     // shapes the TMA stride rules exclude)
     std::shared_ptr<void> tma_cache;
     int* err = nullptr;      // device flag raised by a pipeline wait that timed out
+    // Optional domain of the masked deshade: voxels with domain[i] == 0 are never
+    // updated and keep u = ubar = f, p = v = vbar = q = 0 (both sets of the fused
+    // kernels hold those values).  Null: every voxel is updated.
+    const uint8_t* domain = nullptr;
     const TgvStencilFields& now() const { return set[cur]; }
 };
 
@@ -82,8 +86,11 @@ struct TgvStep {
 size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kernel);
 // Carves the state out of `base` (aligned to 256 bytes per field).
 void tgv_state_bind(TgvState& s, char* base);
-// u = ubar = f, p = q = v = vbar = 0.
+// u = ubar = f, p = q = v = vbar = 0 (in both sets of the fused kernels when a
+// domain is set, so that skipped voxels read the same values from either set).
 void tgv_state_init(TgvState& s, cudaStream_t st);
+// domain[i] = mask[i] >= 1 (the masked processor's test, TGVDeshadeMaskedProcessor.cpp:347).
+void build_domain(const float* mask, size_t n, uint8_t* domain, cudaStream_t st);
 // One primal-dual iteration (advances s.cur for the fused kernel).
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.
@@ -169,7 +176,8 @@ void solve_poisson(DctPlan* plan, const float* in, float* out, int eigen_mode, c
 
 // ---- element-wise ------------------------------------------------------------
 void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,
-                      bool clamp, bool add_back, float* r, cudaStream_t st);
+                      bool clamp, bool add_back, float* r, cudaStream_t st,
+                      bool mask_again = false);
 void log_inplace(float* x, size_t n, cudaStream_t st);
 void exp_inplace(float* x, size_t n, cudaStream_t st);
 

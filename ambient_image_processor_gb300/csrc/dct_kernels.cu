@@ -317,9 +317,11 @@ __global__ void poisson_kernel(const float* __restrict__ in, float* __restrict__
     }
 }
 
+// mask_again: the masked processor multiplies r by the mask a second time when it
+// does not add the background back (TGVDeshadeMaskedProcessor.cpp:203-211).
 __global__ void epilogue_kernel(const float* __restrict__ u, float* __restrict__ l,
                                 const float* __restrict__ mask, size_t n, int mask_shading,
-                                int clamp, int add_back, float* __restrict__ r) {
+                                int clamp, int add_back, int mask_again, float* __restrict__ r) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const float ui = u[i];
@@ -332,6 +334,7 @@ __global__ void epilogue_kernel(const float* __restrict__ u, float* __restrict__
         }
         if (clamp && ri < 0.f) ri = 0.f;         // :91-92
         if (add_back && mask) ri = ri + ui * (1.f - mask[i]);  // :275-279
+        else if (mask_again && mask) ri = ri * mask[i];
         r[i] = ri;
     }
 }
@@ -540,9 +543,10 @@ void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float
 }
 
 void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,
-                      bool clamp, bool add_back, float* r, cudaStream_t st) {
+                      bool clamp, bool add_back, float* r, cudaStream_t st, bool mask_again) {
     epilogue_kernel<<<ew_grid(n), 256, 0, st>>>(u, l, mask, n, mask_shading ? 1 : 0,
-                                                clamp ? 1 : 0, add_back ? 1 : 0, r);
+                                                clamp ? 1 : 0, add_back ? 1 : 0,
+                                                mask_again ? 1 : 0, r);
     TGV_CHECK_LAUNCH();
 }
 

@@ -25,6 +25,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "common.cuh"
@@ -110,6 +111,7 @@ struct TgvArgs {
     float tau, sigma, theta, tau_lambda, alpha0, alpha1;
     float penc, pdec, qenc, qdec;
     int skip_bz;  // L2 data term with depth == 1 drops B_z p (tgv_cuda/tgv2_l2.cu:39-42)
+    const uint8_t* dom;  // masked deshade: update only voxels with dom[i] != 0 (null: all)
 };
 
 constexpr int BX = 32, BY = 8;
@@ -124,6 +126,8 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
+    // outside the masked deshade's domain nothing is updated (tgv2_masked_common.cu)
+    if (a.dom && !a.dom[i]) return;
 
     // p <- proj(p + sigma (F ubar - vbar))          (tgv2_common.cu:118-130)
     const float ub = a.ubar[i];
@@ -196,6 +200,7 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
     const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
+    if (a.dom && !a.dom[i]) return;
 
     // u <- prox(u - tau B.p), ubar                       (tgv2_l1.cu:39-52)
     const float pxi = S::ld(a.p0, i, a.pdec);
@@ -673,6 +678,7 @@ struct Args {
     float penc, pdec, qenc, qdec;
     int skip_bz;
     int* err;
+    const uint8_t* dom;  // masked deshade domain (null: every voxel)
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -870,7 +876,12 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     };
     // p_new over R_p from stage sz (plane z) and sn (plane z+1, or null past the volume):
     // ubar(z) own/+x/+y, ubar(z+1) own, vbar(z) own, p(z)
-    auto dual_p_at = [&](const uint8_t* sz, const uint8_t* sn) {
+    // a voxel outside the masked deshade's domain keeps p = q = 0 and u, v unchanged
+    auto live = [&](int plane) {
+        return a.dom == nullptr || a.dom[(size_t)plane * a.WH + col] != 0;
+    };
+    auto dual_p_at = [&](const uint8_t* sz, const uint8_t* sn, bool lv) {
+        if (!lv) return make_float3(0.f, 0.f, 0.f);
         const float* ub = fb(sz, 0);
         const float u0 = ub[of];
         float g[3] = {xl ? ub[of + 1] - u0 : 0.f, yl ? ub[of + G::BW_F] - u0 : 0.f, 0.f};
@@ -886,7 +897,12 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     };
     // q_new over R_q from stage sz (plane z) and sm (plane z-1, or null below the
     // volume): vbar(z) own/-x/-y, vbar(z-1) own, q(z); written to ring slot out
-    auto dual_q_at = [&](const uint8_t* sz, const uint8_t* sm, float* out) {
+    auto dual_q_at = [&](const uint8_t* sz, const uint8_t* sm, float* out, bool lv) {
+        if (!lv) {
+#pragma unroll
+            for (int k = 0; k < NQ; ++k) out[k * NE + e] = 0.f;
+            return;
+        }
         float vb[3], xm[3], ym[3], zm[3], q[6];
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
@@ -934,22 +950,22 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         const uint8_t* sm = z0 > 0 ? st_of(z0 - 1) : nullptr;
         if constexpr (THREE) {
             if (interior && z0 > 0) {  // p_new(z0 - 1) at this column
-                const float3 pp = dual_p_at(sm, s0);
+                const float3 pp = dual_p_at(sm, s0, live(z0 - 1));
                 p_prev[0] = pp.x;
                 p_prev[1] = pp.y;
                 p_prev[2] = pp.z;
             }
         }
         if (in_rp) {
-            const float3 pp = dual_p_at(s0, s1);
+            const float3 pp = dual_p_at(s0, s1, live(z0));
             float* Pz = Pslot(z0);
             Pz[e] = pp.x;
             Pz[NE + e] = pp.y;
             if constexpr (THREE) Pz[2 * NE + e] = pp.z;
         }
         if (in_rq) {
-            dual_q_at(s0, sm, Qslot(z0));
-            if (s1) dual_q_at(s1, s0, Qslot(z0 + 1));
+            dual_q_at(s0, sm, Qslot(z0), live(z0));
+            if (s1) dual_q_at(s1, s0, Qslot(z0 + 1), live(z0 + 1));
         }
     }
     ok = __syncthreads_and(ok);
@@ -982,8 +998,8 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         load_tile(t + 1);
         // ---- duals for the next planes
         float3 pn = make_float3(0.f, 0.f, 0.f);
-        if (in_rp && p_next) pn = dual_p_at(S1, t + 2 < D ? S2 : nullptr);
-        if (in_rq && q_next) dual_q_at(S2, S1, Qnn);
+        if (in_rp && p_next) pn = dual_p_at(S1, t + 2 < D ? S2 : nullptr, live(t + 1));
+        if (in_rq && q_next) dual_q_at(S2, S1, Qnn, live(t + 2));
         // ---- primal at (x, y, t)
         if (interior) {
             const size_t i = (size_t)t * a.WH + col;
@@ -1004,8 +1020,12 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             } else {
                 uu = (uu + a.tau_lambda * pf) / (1.f + a.tau_lambda);
             }
-            a.u[i] = uu;
-            a.ubar_out[i] = uu + a.theta * (uu - pu);
+            // outside the domain the stored state is already the frozen one
+            const bool lt = live(t);
+            if (lt) {
+                a.u[i] = uu;
+                a.ubar_out[i] = uu + a.theta * (uu - pu);
+            }
             const bool has_next = t + 1 < D;
             const float qxx = Qt[e], qyy = Qt[NE + e], qxy = Qt[2 * NE + e];
             float d[3];
@@ -1024,20 +1044,22 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
                        (yl ? Qt[5 * NE + e + EXW] - qyz : 0.f);
             }
             const float vo[3] = {pv0, pv1, pv2};
+            if (lt) {
 #pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                const float vn = vo[c] - a.tau * (d[c] - pv[c]);
-                a.v[c][i] = vn;
-                a.vbar_out[c][i] = vn + a.theta * (vn - vo[c]);
-                S::st(a.p_out[c], i, pv[c], a.penc);
-            }
-            S::st(a.q_out[0], i, qxx, a.qenc);
-            S::st(a.q_out[1], i, qyy, a.qenc);
-            S::st(a.q_out[3], i, qxy, a.qenc);
-            if constexpr (THREE) {
-                S::st(a.q_out[2], i, qzz, a.qenc);
-                S::st(a.q_out[4], i, qxz, a.qenc);
-                S::st(a.q_out[5], i, qyz, a.qenc);
+                for (int c = 0; c < NC; ++c) {
+                    const float vn = vo[c] - a.tau * (d[c] - pv[c]);
+                    a.v[c][i] = vn;
+                    a.vbar_out[c][i] = vn + a.theta * (vn - vo[c]);
+                    S::st(a.p_out[c], i, pv[c], a.penc);
+                }
+                S::st(a.q_out[0], i, qxx, a.qenc);
+                S::st(a.q_out[1], i, qyy, a.qenc);
+                S::st(a.q_out[3], i, qxy, a.qenc);
+                if constexpr (THREE) {
+                    S::st(a.q_out[2], i, qzz, a.qenc);
+                    S::st(a.q_out[4], i, qxz, a.qenc);
+                    S::st(a.q_out[5], i, qyz, a.qenc);
+                }
             }
 #pragma unroll
             for (int c = 0; c < NC; ++c) p_prev[c] = pv[c];
@@ -1121,6 +1143,7 @@ TgvArgs<typename Dual<PREC>::T> make_args(const TgvState& s, const TgvStep& k,
     a.qenc = 32767.f / k.alpha0;
     a.qdec = k.alpha0 / 32767.f;
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
+    a.dom = s.domain;
     return a;
 }
 
@@ -1147,7 +1170,7 @@ void launch_two_pass(const TgvState& s, const TgvStep& k,
 
 template <int PREC>
 void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
-    const TgvStencilFields& F = s.set[0];
+    const TgvStencilFields& F = s.now();  // in place on the current set
     float* const v[3] = {s.v[0], s.v[1], s.v[2]};
     const auto a = make_args<PREC>(s, k, F, s.u, v, F, s.u, v);
     launch_two_pass<PREC>(s, k, a, st);
@@ -1293,6 +1316,7 @@ void iterate_tma(TgvState& s, const TgvStep& k, int* err, cudaStream_t st) {
     a.qdec = k.alpha0 / 32767.f;
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
     a.err = err;
+    a.dom = s.domain;
     if (s.three) {
         if (k.data_term == TGVDCT_DATA_L1) launch_tma<PREC, true, TGVDCT_DATA_L1>(a, st);
         else launch_tma<PREC, true, TGVDCT_DATA_L2>(a, st);
@@ -1405,7 +1429,33 @@ void tgv_state_init(TgvState& s, cudaStream_t st) {
     }
     for (int k = 0; k < 6; ++k)
         if (F.q[k]) TGV_CUDA(cudaMemsetAsync(F.q[k], 0, n * e, st));
+    // masked runs skip the voxels outside the domain, so the second set must hold
+    // the frozen values as well
+    const TgvStencilFields& G = s.set[1];
+    if (s.domain && G.ubar) {
+        TGV_CUDA(cudaMemcpyAsync(G.ubar, s.f, n * 4, cudaMemcpyDeviceToDevice, st));
+        for (int k = 0; k < 3; ++k) {
+            if (G.vbar[k]) TGV_CUDA(cudaMemsetAsync(G.vbar[k], 0, n * 4, st));
+            if (G.p[k]) TGV_CUDA(cudaMemsetAsync(G.p[k], 0, n * e, st));
+        }
+        for (int k = 0; k < 6; ++k)
+            if (G.q[k]) TGV_CUDA(cudaMemsetAsync(G.q[k], 0, n * e, st));
+    }
     TGV_CUDA(cudaMemsetAsync(s.err, 0, sizeof(int), st));
+}
+
+namespace {
+__global__ void domain_kernel(const float* mask, size_t n, uint8_t* domain) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        domain[i] = mask[i] >= 1.f ? 1 : 0;
+}
+}  // namespace
+
+void build_domain(const float* mask, size_t n, uint8_t* domain, cudaStream_t st) {
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+    domain_kernel<<<blocks, 256, 0, st>>>(mask, n, domain);
+    TGV_CHECK_LAUNCH();
 }
 
 bool tgv_uses_tma(const TgvState& s) { return tma_shape_ok(s); }
@@ -1456,7 +1506,9 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
             case TGVDCT_STATE_FX16_DUAL: iterate_tma<TGVDCT_STATE_FX16_DUAL>(s, k, s.err, st); return;
         }
     }
-    if (s.kernel == TGV_KERNEL_TWO_PASS) {
+    // The register-staged fused kernel has no domain support: a masked run whose
+    // shape rules out TMA uses the two-pass kernels in place on the current set.
+    if (s.kernel == TGV_KERNEL_TWO_PASS || s.domain) {
         switch (s.precision) {
             case TGVDCT_STATE_FP32: iterate_two_pass<TGVDCT_STATE_FP32>(s, k, st); return;
             case TGVDCT_STATE_BF16_DUAL: iterate_two_pass<TGVDCT_STATE_BF16_DUAL>(s, k, st); return;

@@ -139,6 +139,15 @@ void tgvdct_params_init(tgvdct_params* p);
 /* Bytes of device memory a context for these parameters allocates. */
 size_t tgvdct_workspace_bytes(const tgvdct_params* p);
 
+/* ---- device buffers for hosts without a CUDA runtime of their own ---------- */
+/* cudaMalloc / cudaFree / blocking cudaMemcpy on the current device, for callers
+   (FFI bindings, the reference-signature C++ layer) that hand device buffers to
+   the _dev entry points without linking the CUDA runtime themselves. */
+tgvdct_status tgvdct_device_alloc(size_t bytes, void** out);
+tgvdct_status tgvdct_device_free(void* p);
+tgvdct_status tgvdct_host_to_device(void* dst_dev, const void* src_host, size_t bytes);
+tgvdct_status tgvdct_device_to_host(void* dst_host, const void* src_dev, size_t bytes);
+
 /* ---- contexts (device workspace of one shape) --------------------------- */
 tgvdct_status tgvdct_create(const tgvdct_params* p, tgvdct_context** out);
 tgvdct_status tgvdct_destroy(tgvdct_context* ctx);
@@ -172,6 +181,16 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t wid
                                                tgvdct_iteration_callback callback, void* user,
                                                float alpha0, float alpha1, float* u_host,
                                                float* v_x_host, float* v_y_host);
+
+/* General host-buffer form of the loop: every parameter of tgvdct_params (data
+   term, geometry, steps, precision), host f in, host u out; v_x/v_y/v_z_host may
+   each be NULL (not copied out; v_z is zero for 2-D geometry).  With a callback,
+   it is called as in tgvdct_tgv2_l1_deshade_launch (host copies).  Backs the
+   reference-signature tgv2_l1_launch / tgv2_l2_launch (tgv_cuda/tgv2_l1.cu:64-72,
+   tgv_cuda/tgv2_l2.cu:60-68), whose iteration callback sees u. */
+tgvdct_status tgvdct_tgv2_run(const tgvdct_params* p, const float* f_host, float* u_host,
+                             float* v_x_host, float* v_y_host, float* v_z_host,
+                             tgvdct_iteration_callback callback, void* user);
 
 /* Replaces tgv2_l1_launch / tgv2_l2_launch (tgv_cuda/tgv2_l1.cu:64-72,
    tgv_cuda/tgv2_l2.cu:60-68): the TGV filter's denoise loop, u only. */
@@ -218,6 +237,13 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* ctx, const float* grad_u_
 tgvdct_status tgvdct_divergence_launch(const float* dx, const float* dy, const float* dz,
                                        uint32_t width, uint32_t height, uint32_t depth,
                                        float* out);
+/* Device form of divergence_kernel_launch with is_host_data == false
+   (divergence.cu:59-61, whose inputs are device buffers): out_dev = B_x dx +
+   B_y dy (+ B_z dz when depth > 1), the negated backward differences.
+   Synchronises the stream before returning. */
+tgvdct_status tgvdct_divergence_dev(const float* dx_dev, const float* dy_dev,
+                                    const float* dz_dev, uint32_t width, uint32_t height,
+                                    uint32_t depth, float* out_dev, void* stream);
 tgvdct_status tgvdct_cosine_transform_launch(const float* in, uint32_t width, uint32_t height,
                                              uint32_t depth, int32_t dct_mode, float* out);
 tgvdct_status tgvdct_inverse_cosine_transform_launch(const float* in, uint32_t width,
@@ -303,6 +329,40 @@ tgvdct_status tgvdct_process_dev(tgvdct_context* ctx, const float* f_dev, const 
                                  int32_t set_negative_values_to_zero, int32_t add_background_back,
                                  int32_t log_domain, float* u_dev, float* l_dev, float* r_dev,
                                  tgvdct_iteration_callback callback, void* user, void* stream);
+
+/* ---- masked deshade (tgv_deshade_masked/) ---------------------------------- */
+/* Restricts the TGV loop of a context to the voxels whose mask value is >= 1
+   (TGVDeshadeMaskedProcessor::buildMaskIndices, TGVDeshadeMaskedProcessor.cpp:337-385):
+   the others are never updated and keep u = f and p = v = q = 0, and the
+   difference operators at updated voxels read those values, as the reference's
+   masked kernels do (tgv2_masked_common.cu, tgv_masked_common.cu).  The mask is
+   copied; with a mask set, tgvdct_process_dev also applies the masked processor's
+   epilogue (l and r weighted by the mask, then the background add-back or a second
+   multiply of r by the mask; its mask_dev argument must be NULL).  NULL clears.
+   The reverse mode refuses a context with a mask. */
+tgvdct_status tgvdct_set_domain_mask_dev(tgvdct_context* ctx, const float* mask_dev, void* stream);
+
+/* Replaces TGVDeshadeMaskedProcessor::processTGV2L1GPUCuda
+   (TGVDeshadeMaskedProcessor.cpp:77-212, 2-D :214-330): the masked loop (2-D
+   operators when depth == 1, whatever p->geometry says, as the reference chooses),
+   the Poisson integration of v, and the masked epilogue.  Host buffers. */
+tgvdct_status tgvdct_process_tgv2_l1_masked(const tgvdct_params* p, const float* f_host,
+                                            const float* mask_host,
+                                            int32_t set_negative_values_to_zero,
+                                            int32_t add_background_back, int32_t log_domain,
+                                            tgvdct_iteration_callback callback, void* user,
+                                            float* denoised_host, float* shading_host,
+                                            float* deshaded_host);
+
+/* Replaces tgv2_l1_deshade_masked_launch<float> (tgv_deshade_masked/tgv2_l1_deshade_masked.cu)
+   and tgv2_l1_deshade_masked_2d_launch (depth == 1): the masked loop alone.  The
+   mask replaces the reference's index lists (voxels with mask >= 1; the face lists
+   follow from the shape).  v_z_host may be NULL; it is zero when depth == 1. */
+tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
+    const float* f_host, const float* mask_host, uint32_t width, uint32_t height, uint32_t depth,
+    float lambda, uint32_t iteration_count, uint32_t paint_iteration_interval,
+    int cuda_block_dimension, tgvdct_iteration_callback callback, void* user, float alpha0,
+    float alpha1, float* u_host, float* v_x_host, float* v_y_host, float* v_z_host);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,12 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = [p, p, p, _u, _u, _u, p]
             fn = getattr(L, f"oracle_deshade_epilogue_{suf}")
             fn.argtypes = [p, p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
+            fn = getattr(L, f"oracle_masked_deshade_epilogue_{suf}")
+            fn.argtypes = [p, p, p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
+            fn = getattr(L, f"oracle_tgv2_deshade_masked_{suf}")
+            fn.argtypes = [p, p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int,
+                           ctypes.c_int, p, p, p, p]
+            fn.restype = _u
         vp = ctypes.c_void_p
         L.oracle_tgv2_gradient_f64.argtypes = [_f64p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d,
                                                ctypes.c_int, vp, vp, vp, vp, _f64p, _f64p, vp]
@@ -170,6 +176,50 @@ def process_tgv2_l1(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *,
     return u, l, r
 
 
+def tgv2_deshade_masked(f, mask, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *,
+                        tau=0.0, sigma=0.0, theta=1.0, data_term="l1", two_d=None,
+                        dtype=np.float64):
+    """The masked loop: only voxels with mask >= 1 are updated.  two_d defaults to
+    depth == 1, the choice TGVDeshadeMaskedProcessor makes.  Returns (u, v_x, v_y, v_z)."""
+    f = np.ascontiguousarray(f, dtype=dtype)
+    mask = np.ascontiguousarray(mask, dtype=dtype)
+    w, h, d = _shape3(f)
+    if two_d is None:
+        two_d = d == 1
+    u = np.empty_like(f)
+    vx, vy, vz = np.empty_like(f), np.empty_like(f), np.empty_like(f)
+    dt = 0 if data_term in ("l1", 0) else 1
+    getattr(lib(), f"oracle_tgv2_deshade_masked_{_dt(dtype)}")(
+        f, mask, w, h, d, lambda_, alpha0, alpha1, iterations, tau, sigma, theta, dt,
+        int(two_d), u, vx, vy, vz)
+    return u, vx, vy, vz
+
+
+def masked_deshade_epilogue(u, l, mask, set_negative_values_to_zero=True,
+                            add_background_back=False):
+    """The masked processor's tail: returns (r, l * mask)."""
+    u = np.ascontiguousarray(u)
+    l = np.array(l, dtype=u.dtype, copy=True, order="C")
+    mask = np.ascontiguousarray(mask, dtype=u.dtype)
+    r = np.empty_like(u)
+    getattr(lib(), f"oracle_masked_deshade_epilogue_{_dt(u.dtype)}")(
+        u, l, mask, int(set_negative_values_to_zero), int(add_background_back), u.size, r)
+    return r, l
+
+
+def process_tgv2_l1_masked(f, mask, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *,
+                           set_negative_values_to_zero=True, add_background_back=False,
+                           tau=0.0, sigma=0.0, dtype=np.float64):
+    """TGVDeshadeMaskedProcessor::processTGV2L1GPUCuda (TGVDeshadeMaskedProcessor.cpp:77-330):
+    the masked loop (2-D operators when depth == 1), the Poisson-DCT integration of v,
+    then the masked epilogue.  Returns (u, l, r)."""
+    u, vx, vy, vz = tgv2_deshade_masked(f, mask, lambda_, alpha0, alpha1, iterations, tau=tau,
+                                        sigma=sigma, dtype=dtype)
+    l = integrate_poisson_dct(vx, vy, vz)
+    r, l = masked_deshade_epilogue(u, l, mask, set_negative_values_to_zero, add_background_back)
+    return u, l, r
+
+
 def tgv2_gradient(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=10, *, grad_u=None,
                   grad_v=None, data_term="l1", tau=0.0, sigma=0.0, theta=1.0):
     """FP64 reverse mode of the 3-D loop: returns (u_K, dL/df, dL/d(lambda, alpha0, alpha1))
@@ -215,6 +265,11 @@ def ref() -> ctypes.CDLL:
         R.ref_tgv2_denoise_f32.argtypes = [ctypes.c_int, _f32p, _u, _u, _u, f, f, f, _u, _f32p]
         R.ref_process_tgv2_l1_f32.argtypes = [_f32p, _u, _u, _u, f, f, f, _u, ctypes.c_int,
                                               _f32p, _f32p, _f32p]
+        R.ref_tgv2_l1_deshade_masked_f32.argtypes = [_f32p, _f32p, _u, _u, _u, f, f, f, _u,
+                                                     _f32p, _f32p, _f32p, _f32p]
+        R.ref_process_tgv2_l1_masked_f32.argtypes = [_f32p, _f32p, _u, _u, _u, f, f, f, _u,
+                                                     ctypes.c_int, ctypes.c_int, _f32p, _f32p,
+                                                     _f32p]
         for suf, p in (("f32", _f32p), ("f64", _f64p)):
             getattr(R, f"ref_divergence_{suf}").argtypes = [p, p, p, _u, _u, _u, p]
             for name in ("cosine_transform", "inverse_cosine_transform", "solve_poisson"):

@@ -1,5 +1,7 @@
 // TEST INFRASTRUCTURE — extern "C" entry points of the CPU oracle (tgv_oracle.hpp),
 // loaded by tests/ and bench.py's CPU-baseline leg through ctypes.  Not product code.
+#include <vector>
+
 #include "tgv_adjoint.hpp"
 #include "tgv_oracle.hpp"
 
@@ -72,6 +74,22 @@ int oracle_set_threads(int n) {
     void oracle_deshade_epilogue_##SUF(const T* u, T* l, const T* mask, int clamp, int add_back,  \
                                        unsigned long long n, T* r) {                              \
         oracle::deshade_epilogue<T>(u, l, mask, clamp != 0, add_back != 0, (index_t)n, r);        \
+    }                                                                                             \
+    void oracle_masked_deshade_epilogue_##SUF(const T* u, T* l, const T* mask, int clamp,         \
+                                              int add_back, unsigned long long n, T* r) {         \
+        oracle::masked_deshade_epilogue<T>(u, l, mask, clamp != 0, add_back != 0, (index_t)n, r); \
+    }                                                                                             \
+    unsigned oracle_tgv2_deshade_masked_##SUF(                                                    \
+        const T* f, const T* mask, unsigned w, unsigned h, unsigned d, double lambda,             \
+        double alpha0, double alpha1, unsigned iterations, double tau, double sigma,              \
+        double theta, int data_term, int two_d, T* u, T* vx, T* vy, T* vz) {                      \
+        const size_t n = (size_t)w * h * d;                                                       \
+        std::vector<unsigned char> dom(n);                                                        \
+        for (size_t i = 0; i < n; ++i) dom[i] = mask[i] >= T(1) ? 1 : 0;                          \
+        return oracle::tgv2_deshade<T>(f, dims(w, h, d),                                          \
+                                       make_params(lambda, alpha0, alpha1, iterations, tau,       \
+                                                   sigma, theta, data_term, two_d),               \
+                                       u, vx, vy, vz, nullptr, dom.data());                       \
     }
 
 ORACLE_TYPED(float, f32)

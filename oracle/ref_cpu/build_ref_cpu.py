@@ -28,7 +28,7 @@ ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
 DEFAULT_REFERENCE = "/root/reference"
 
-MODULE_DIRS = ("tgv_cuda", "tgv_deshade", "cuda_image_operations")
+MODULE_DIRS = ("tgv_cuda", "tgv_deshade", "tgv_deshade_masked", "cuda_image_operations")
 # translation units that provide the launchers ref_harness.cpp calls
 UNITS = (
     "tgv_deshade/tgv2_l1_deshade.cu",
@@ -41,6 +41,11 @@ UNITS = (
     "cuda_image_operations/solve_poisson_in_cosine_domain.cu",
     "cuda_image_operations/subtract.cu",
     "cuda_image_operations/clamp_negative_values.cu",
+    "cuda_image_operations/multiply.cu",
+    "cuda_image_operations/add.cu",
+    "cuda_image_operations/invert.cu",
+    "tgv_deshade_masked/tgv2_l1_deshade_masked.cu",
+    "tgv_deshade_masked/tgv2_l1_deshade_masked_2d.cu",
 )
 
 _LAUNCH = re.compile(r"\b([A-Za-z_]\w*)\s*<<<(.*?)>>>\s*\(", re.S)

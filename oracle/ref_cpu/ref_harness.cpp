@@ -6,6 +6,7 @@
 // source/modules/cuda_image_operations/CudaImageOperationsProcessor.cpp:286-294.
 #include <cstring>
 #include <functional>
+#include <vector>
 
 #include "cuda.h"
 
@@ -64,6 +65,32 @@ template <typename Pixel>
 Pixel* clamp_negative_values_kernel_launch(Pixel* image, uint width, uint height, uint depth,
                                            Pixel value);
 
+template <typename Pixel>
+Pixel* multiply_kernel_launch(Pixel* image1, Pixel* image2, uint width, uint height, uint depth);
+template <typename Pixel>
+Pixel* add_kernel_launch(Pixel* image1, Pixel* image2, uint width, uint height, uint depth);
+template <typename Pixel>
+Pixel* invert_kernel_launch(Pixel* image, uint width, uint height, uint depth);
+
+using RefIndices = const std::vector<uint>&;
+template <typename Pixel>
+Pixel* tgv2_l1_deshade_masked_launch(
+    Pixel* f_host, uint width, uint height, uint depth, Pixel lambda, uint iteration_count,
+    uint paint_iteration_interval, const int cuda_block_dimension,
+    DeshadeIterationCallback<Pixel> iteration_finished_callback, Pixel alpha0, Pixel alpha1,
+    Pixel** v_x_host, Pixel** v_y_host, Pixel** v_z_host, RefIndices masked, RefIndices left,
+    RefIndices not_left, RefIndices right, RefIndices not_right, RefIndices top,
+    RefIndices not_top, RefIndices bottom, RefIndices not_bottom, RefIndices front,
+    RefIndices not_front, RefIndices back, RefIndices not_back);
+template <typename Pixel>
+Pixel* tgv2_l1_deshade_masked_2d_launch(
+    Pixel* f_host, uint width, uint height, Pixel lambda, uint iteration_count,
+    uint paint_iteration_interval, const int cuda_block_dimension,
+    DeshadeIterationCallback2D<Pixel> iteration_finished_callback, Pixel alpha0, Pixel alpha1,
+    Pixel** v_x_host, Pixel** v_y_host, RefIndices masked, RefIndices left, RefIndices not_left,
+    RefIndices right, RefIndices not_right, RefIndices top, RefIndices not_top,
+    RefIndices bottom, RefIndices not_bottom);
+
 namespace {
 template <class P>
 void take(P* src, P* dst, size_t n) {
@@ -89,6 +116,52 @@ P* integrate(P* vx, P* vy, P* vz, uint w, uint h, uint d) {
     P* l = inverse_cosine_transform_kernel_launch<P>(sol, w, h, d);
     delete[] sol;
     return l;
+}
+// The index lists of TGVDeshadeMaskedProcessor::buildMaskIndices
+// (tgv_deshade_masked/TGVDeshadeMaskedProcessor.cpp:337-385): voxels with mask >= 1,
+// split by whether they lie on each face of the volume.
+struct MaskIndices {
+    std::vector<uint> inside, edge[6], not_edge[6];  // left right top bottom front back
+};
+MaskIndices mask_indices(const float* mask, uint w, uint h, uint d) {
+    MaskIndices m;
+    for (uint z = 0; z < d; ++z)
+        for (uint y = 0; y < h; ++y)
+            for (uint x = 0; x < w; ++x) {
+                const uint i = (z * h + y) * w + x;
+                if (mask[i] < 1) continue;
+                m.inside.push_back(i);
+                const bool on[6] = {x == 0, x == w - 1, y == 0, y == h - 1, z == 0, z == d - 1};
+                for (int k = 0; k < 6; ++k) (on[k] ? m.edge[k] : m.not_edge[k]).push_back(i);
+            }
+    return m;
+}
+
+// tgv2_l1_deshade_masked_launch (3-D) or its 2-D twin (depth == 1), as
+// TGVDeshadeMaskedProcessor.cpp:77-212 / :214-330 call them without a callback.
+float* masked_launch(const float* f, const float* mask, uint w, uint h, uint d, float lambda,
+                     float alpha0, float alpha1, uint iterations, float** vx, float** vy,
+                     float** vz) {
+    const size_t n = (size_t)w * h * d;
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    const MaskIndices m = mask_indices(mask, w, h, d);
+    float* u;
+    if (d > 1) {
+        u = tgv2_l1_deshade_masked_launch<float>(
+            fin, w, h, d, lambda, iterations, iterations + 1, -1, nullptr, alpha0, alpha1, vx, vy,
+            vz, m.inside, m.edge[0], m.not_edge[0], m.edge[1], m.not_edge[1], m.edge[2],
+            m.not_edge[2], m.edge[3], m.not_edge[3], m.edge[4], m.not_edge[4], m.edge[5],
+            m.not_edge[5]);
+    } else {
+        u = tgv2_l1_deshade_masked_2d_launch<float>(
+            fin, w, h, lambda, iterations, iterations + 1, -1, nullptr, alpha0, alpha1, vx, vy,
+            m.inside, m.edge[0], m.not_edge[0], m.edge[1], m.not_edge[1], m.edge[2],
+            m.not_edge[2], m.edge[3], m.not_edge[3]);
+        *vz = new float[n]();
+    }
+    delete[] fin;
+    return u;
 }
 }  // namespace
 
@@ -194,6 +267,65 @@ void ref_process_tgv2_l1_f32(const float* f, uint w, uint h, uint d, float lambd
         delete[] r;
         r = r2;
     }
+    take(u, denoised, n);
+    take(l, shading, n);
+    take(r, deshaded, n);
+}
+
+// The masked TGV loop alone (v_z is zero for depth == 1).
+void ref_tgv2_l1_deshade_masked_f32(const float* f, const float* mask, uint w, uint h, uint d,
+                                    float lambda, float alpha0, float alpha1, uint iterations,
+                                    float* u, float* vx, float* vy, float* vz) {
+    const size_t n = (size_t)w * h * d;
+    float *ox, *oy, *oz;
+    float* ou = masked_launch(f, mask, w, h, d, lambda, alpha0, alpha1, iterations, &ox, &oy, &oz);
+    take(ou, u, n);
+    take(ox, vx, n);
+    take(oy, vy, n);
+    take(oz, vz, n);
+}
+
+// TGVDeshadeMaskedProcessor::processTGV2L1GPUCuda (TGVDeshadeMaskedProcessor.cpp:77-212,
+// 2-D :214-330) without a callback: the masked loop, then
+// TGVDeshadeProcessor::deshade_poisson_cosine_transform (TGVDeshadeProcessor.cpp:71-95)
+// with the mask, then the background add-back or a second mask multiply.
+void ref_process_tgv2_l1_masked_f32(const float* f, const float* mask, uint w, uint h, uint d,
+                                    float lambda, float alpha0, float alpha1, uint iterations,
+                                    int set_negative_values_to_zero, int add_background_back,
+                                    float* denoised, float* shading, float* deshaded) {
+    const size_t n = (size_t)w * h * d;
+    float *vx, *vy, *vz;
+    float* u = masked_launch(f, mask, w, h, d, lambda, alpha0, alpha1, iterations, &vx, &vy, &vz);
+    float* mk = new float[n];
+    std::memcpy(mk, mask, sizeof(float) * n);
+    float* l = integrate<float>(vx, vy, vz, w, h, d);
+    delete[] vx;
+    delete[] vy;
+    delete[] vz;
+    float* r = subtract_kernel_launch<float>(u, l, w, h, d);
+    float* t = multiply_kernel_launch<float>(l, mk, w, h, d);
+    delete[] l;
+    l = t;
+    t = multiply_kernel_launch<float>(r, mk, w, h, d);
+    delete[] r;
+    r = t;
+    if (set_negative_values_to_zero) {
+        t = clamp_negative_values_kernel_launch<float>(r, w, h, d, 0.0f);
+        delete[] r;
+        r = t;
+    }
+    if (add_background_back) {
+        float* inv = invert_kernel_launch<float>(mk, w, h, d);
+        float* bg = multiply_kernel_launch<float>(u, inv, w, h, d);
+        t = add_kernel_launch<float>(r, bg, w, h, d);
+        delete[] inv;
+        delete[] bg;
+    } else {
+        t = multiply_kernel_launch<float>(r, mk, w, h, d);
+    }
+    delete[] r;
+    r = t;
+    delete[] mk;
     take(u, denoised, n);
     take(l, shading, n);
     take(r, deshaded, n);

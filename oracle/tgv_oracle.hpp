@@ -122,9 +122,17 @@ using IterCallback = std::function<bool(unsigned, unsigned, const T*, const T*, 
 // tgv_cuda/tgv2_l2.cu:27-56, tgv_cuda/tgv2_common_2d.cu:55-279.
 // Writes u (denoised) and v (the bias gradient field).  v_z may be null for 2-D.
 // Returns the number of iterations run (a callback may stop the loop early).
+//
+// domain (optional): the masked deshade of tgv_deshade_masked/tgv2_l1_deshade_masked.cu
+// (and _2d.cu), whose kernels (tgv2_masked_common.cu, tgv_masked_common.cu) update
+// only the voxels with mask >= 1 (index lists built by
+// TGVDeshadeMaskedProcessor.cpp:337-385).  Voxels with domain[i] == 0 are never
+// updated: they keep u = u_bar = f and p = v = v_bar = q = 0, and the differences
+// taken at updated voxels read those values.
 template <class T>
 unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_out,
-                      T* vy_out, T* vz_out, IterCallback<T> cb = nullptr) {
+                      T* vy_out, T* vz_out, IterCallback<T> cb = nullptr,
+                      const unsigned char* domain = nullptr) {
     const index_t n = g.n();
     const bool three = !prm.two_d;
     const T tau = T(prm.tau > 0 ? prm.tau : default_step());
@@ -149,6 +157,7 @@ unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_
         if (three) forward_diff(2, u_bar.data(), gz.data(), g);
 #pragma omp parallel for schedule(static)
         for (index_t i = 0; i < n; ++i) {
+            if (domain && !domain[i]) continue;
             px[i] = fma_t(sigma, T(gx[i] - vbx[i]), px[i]);
             py[i] = fma_t(sigma, T(gy[i] - vby[i]), py[i]);
             T nrm;
@@ -171,6 +180,7 @@ unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_
         const T tl = T(tau * lambda);
 #pragma omp parallel for schedule(static)
         for (index_t i = 0; i < n; ++i) {
+            if (domain && !domain[i]) continue;
             T div;
             if (!three) div = T(gx[i] + gy[i]);
             else if (prm.data_term == L2 && g.d == 1) div = T(gx[i] + gy[i]);  // tgv2_l2.cu:39-42
@@ -208,6 +218,7 @@ unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_
         // 4. q update and projection, v_prev = v
 #pragma omp parallel for schedule(static)
         for (index_t i = 0; i < n; ++i) {
+            if (domain && !domain[i]) continue;
             qxx[i] = fma_t(sigma, exx[i], qxx[i]);
             qyy[i] = fma_t(sigma, eyy[i], qyy[i]);
             qxy[i] = fma_t(sigma, exy[i], qxy[i]);
@@ -261,6 +272,7 @@ unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_
         // 6. primal v step and over-relaxation
 #pragma omp parallel for schedule(static)
         for (index_t i = 0; i < n; ++i) {
+            if (domain && !domain[i]) continue;
             vx[i] = T(vx[i] - T(tau * T(exx[i] - px[i])));
             vy[i] = T(vy[i] - T(tau * T(eyy[i] - py[i])));
             vbx[i] = T(vx[i] + T(theta * T(vx[i] - vpx[i])));
@@ -437,6 +449,24 @@ void deshade_epilogue(const T* u, T* l, const T* mask, bool set_negative_values_
         }
         if (set_negative_values_to_zero && r < 0) r = T(0);
         if (add_background_back && mask) r = T(r + T(u[i] * T(T(1) - mask[i])));
+        r_out[i] = r;
+    }
+}
+
+// The tail of TGVDeshadeMaskedProcessor::processTGV2L1GPUCuda
+// (TGVDeshadeMaskedProcessor.cpp:186-211): deshade_epilogue with the mask applied to l
+// and r, then either the background add-back or a second multiply by the mask.
+template <class T>
+void masked_deshade_epilogue(const T* u, T* l, const T* mask, bool set_negative_values_to_zero,
+                             bool add_background_back, index_t n, T* r_out) {
+#pragma omp parallel for schedule(static)
+    for (index_t i = 0; i < n; ++i) {
+        T r = T(u[i] - l[i]);
+        l[i] = T(l[i] * mask[i]);
+        r = T(r * mask[i]);
+        if (set_negative_values_to_zero && r < 0) r = T(0);
+        if (add_background_back) r = T(r + T(u[i] * T(T(1) - mask[i])));
+        else r = T(r * mask[i]);
         r_out[i] = r;
     }
 }

@@ -45,6 +45,26 @@ DENOISE = [  # (name, data term, shape, seed, lambda, alpha0, alpha1, iterations
 DCT_SHAPES = [(10, 12, 16), (1, 18, 24), (5, 7, 1), (1, 1, 9), (3, 1, 1), (4, 4, 4)]
 PROCESS = [("process3d", (8, 12, 16), 41, 1.0, 2.0, 1.0, 40),
            ("process3d_d1", (1, 20, 24), 42, 1.0, 2.0, 1.0, 40)]
+# masked deshade: (name, shape, seed, lambda, alpha0, alpha1, iterations, add_background_back)
+MASKED = [("masked3d", (8, 12, 16), 61, 1.0, 2.0, 1.0, 40, 0),
+          ("masked3d_odd", (7, 11, 13), 62, 0.8, 1.5, 0.9, 35, 1),
+          ("masked2d", (1, 20, 24), 63, 1.0, 2.0, 1.0, 40, 0),
+          ("masked2d_back", (1, 17, 21), 64, 1.0, 2.0, 1.0, 30, 1)]
+
+
+def domain_mask(shape, seed):
+    """An off-centre ellipsoid that reaches two faces of the volume, mostly 1 inside,
+    a few voxels of 2 (inside, and weighting the outputs), a rim of 0.5 (outside the
+    TGV domain, still weighting the outputs), 0 elsewhere."""
+    rng = np.random.default_rng(seed)
+    d, h, w = shape
+    z, y, x = np.meshgrid(np.linspace(-1, 1, d) if d > 1 else np.zeros(1),
+                          np.linspace(-1, 1, h), np.linspace(-1, 1, w), indexing="ij")
+    r2 = ((x - 0.35) / 0.9) ** 2 + ((y + 0.3) / 0.8) ** 2 + (z / 1.1) ** 2
+    m = np.where(r2 < 1.0, 1.0, np.where(r2 < 1.3, 0.5, 0.0))
+    inside = np.flatnonzero(m == 1.0)
+    m.flat[rng.choice(inside, max(1, inside.size // 20), replace=False)] = 2.0
+    return m.astype(np.float32)
 
 
 def empties(f, k):
@@ -99,9 +119,27 @@ def main() -> int:
         R.ref_process_tgv2_l1_f32(f, w, h, d, lam, a0, a1, it, 1, u, l, r)
         cases[name] = dict(f=f, denoised=u, shading=l, deshaded=r,
                            params=np.array([lam, a0, a1, it], np.float64))
+    for name, shape, seed, lam, a0, a1, it, back in MASKED:
+        f = tissue_phantom_3d(*shape, seed=seed)
+        mask = domain_mask(shape, seed)
+        d, h, w = shape
+        u, vx, vy, vz = empties(f, 4)
+        R.ref_tgv2_l1_deshade_masked_f32(f, mask, w, h, d, lam, a0, a1, it, u, vx, vy, vz)
+        du, dl, dr = empties(f, 3)
+        R.ref_process_tgv2_l1_masked_f32(f, mask, w, h, d, lam, a0, a1, it, 1, back, du, dl, dr)
+        cases[name] = dict(f=f, mask=mask, u=u, v_x=vx, v_y=vy, v_z=vz, denoised=du,
+                           shading=dl, deshaded=dr, add_background_back=np.array(back),
+                           params=np.array([lam, a0, a1, it], np.float64))
+    written = 0
     for name, c in cases.items():
-        np.savez_compressed(os.path.join(OUT, name + ".npz"), **c)
-    print(f"wrote {len(cases)} fixtures to {OUT}")
+        path = os.path.join(OUT, name + ".npz")
+        if os.path.exists(path):  # rewrite only fixtures whose arrays changed
+            with np.load(path) as old:
+                if set(old.files) == set(c) and all(np.array_equal(old[k], c[k]) for k in c):
+                    continue
+        np.savez_compressed(path, **c)
+        written += 1
+    print(f"{written} of {len(cases)} fixtures written to {OUT}")
     return 0
 
 
