@@ -84,6 +84,11 @@ _SIGS = {
     "tgvdct_divergence_launch": [_f32p, _f32p, _vp, _u32, _u32, _u32, _f32p],
     "tgvdct_divergence_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp],
     "tgvdct_set_domain_mask_dev": [_vp, _vp, _vp],
+    "tgvdct_convergence_test": [ctypes.POINTER(Params), _f32p, _vp, _u32, _vp, _vp, _u32,
+                                ctypes.POINTER(_u32), _vp],
+    "tgvdct_convergence_optimization": [ctypes.POINTER(Params), _f32p, _vp, _i32,
+                                        ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_float), _f32p, _f32p, _f32p],
     "tgvdct_process_tgv2_l1_masked": [ctypes.POINTER(Params), _f32p, _f32p, _i32, _i32, _i32,
                                       CALLBACK, _vp, _f32p, _f32p, _f32p],
     "tgvdct_tgv2_l1_deshade_masked_launch": [_f32p, _f32p, _u32, _u32, _u32, _flt, _u32, _u32,
@@ -347,6 +352,50 @@ class TGVDeshadeProcessor:
                                             u, l, r))
         del keep
         return u, l, r
+
+
+def convergence_test(input_image, lambda_, alpha0, alpha1, iteration_count,
+                     check_iteration_interval=1, mask=None, **params):
+    """TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceTest and ...Metric
+    (TGVDeshadeProcessor.cpp:479-568).  Returns (ncc history, time-TV history,
+    metric TVs (2,)) as FP64 numpy arrays."""
+    f = _f32(input_image)
+    w, h, d = _dims(f)
+    p = default_params(width=w, height=h, depth=d, lambda_=lambda_, alpha0=alpha0,
+                       alpha1=alpha1, iteration_count=iteration_count, **params)
+    cap = iteration_count // max(check_iteration_interval, 1) + 1
+    ncc, tv, mt = np.zeros(cap), np.zeros(cap), np.zeros(2)
+    cnt = _u32()
+    mptr, m = None, None
+    if mask is not None:
+        m = _f32(mask)
+        mptr = m.ctypes.data_as(_vp)
+    _check(lib().tgvdct_convergence_test(ctypes.byref(p), f, mptr, check_iteration_interval,
+                                         ncc.ctypes.data_as(_vp), tv.ctypes.data_as(_vp), cap,
+                                         ctypes.byref(cnt), mt.ctypes.data_as(_vp)),
+           allow_stop=False)
+    k = min(int(cnt.value), cap)
+    return ncc[:k], tv[:k], mt
+
+
+def convergence_optimization(input_image, lambda_, mask=None, set_negative_values_to_zero=True,
+                             **params):
+    """TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceOptimization
+    (TGVDeshadeProcessor.cpp:571-646): returns (alpha0, alpha1, u, l, r)."""
+    f = _f32(input_image)
+    w, h, d = _dims(f)
+    p = default_params(width=w, height=h, depth=d, lambda_=lambda_, **params)
+    a0, a1 = ctypes.c_float(), ctypes.c_float()
+    u, l, r = (np.empty_like(f) for _ in range(3))
+    mptr, m = None, None
+    if mask is not None:
+        m = _f32(mask)
+        mptr = m.ctypes.data_as(_vp)
+    _check(lib().tgvdct_convergence_optimization(ctypes.byref(p), f, mptr,
+                                                 int(set_negative_values_to_zero),
+                                                 ctypes.byref(a0), ctypes.byref(a1), u, l, r),
+           allow_stop=False)
+    return a0.value, a1.value, u, l, r
 
 
 # ---------------------------------------------------------------------------

@@ -5,7 +5,8 @@ parallel, then linked into ``ambient_image_processor_gb300/_build/libtgvdct.so``
 No cmake, no torch extension machinery: the library exposes plain ``extern "C"``
 symbols declared in ``include/tgvdct.h``.  On top of it, g++ builds the host-only
 reference-signature layer ``libtgvdct_refapi.so`` (``include/tgvdct_reference_api.hpp``)
-and the terminal program ``tgv2_deshade_application``.
+and the terminal programs ``tgv2_deshade_application`` and
+``tgv2_deshade_convergence_test_application``.
 
     python -m ambient_image_processor_gb300.build
 """
@@ -25,6 +26,7 @@ LIB = os.path.join(OUT, "libtgvdct.so")
 REFAPI = os.path.join(PKG, "refapi")
 REFAPI_LIB = os.path.join(OUT, "libtgvdct_refapi.so")
 CLI = os.path.join(OUT, "tgv2_deshade_application")
+CONVERGENCE_CLI = os.path.join(OUT, "tgv2_deshade_convergence_test_application")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
@@ -39,6 +41,8 @@ UNITS = {
     "capi.cu": [],
     "noalloc.cu": [],
     "dct_tc.cu": [],
+    "dct_tc2.cu": [],
+    "metrics.cu": [],
     # the adjoint recomputes forward predicates (prox branch, projection activity)
     # and must round exactly like tgv_kernels.cu
     "adjoint.cu": ["-fmad=false"],
@@ -101,6 +105,10 @@ def build_host(force: bool = False) -> None:
     cli_src = [os.path.join(REFAPI, "tgv2_deshade_main.cpp"), os.path.join(REFAPI, "metaimage.cpp")]
     if force or _stale(CLI, [*cli_src, *hdrs, LIB]):
         _run([cxx, *flags, "-o", CLI, *cli_src, *link])
+    conv_src = [os.path.join(REFAPI, "tgv2_deshade_convergence_test_main.cpp"),
+                os.path.join(REFAPI, "metaimage.cpp")]
+    if force or _stale(CONVERGENCE_CLI, [*conv_src, *hdrs, LIB]):
+        _run([cxx, *flags, "-o", CONVERGENCE_CLI, *conv_src, *link])
 
 
 if __name__ == "__main__":

@@ -1,5 +1,6 @@
 // C ABI of the TGV-DCT path (include/tgvdct.h): contexts, status codes, the
 // iteration loop with its callback, and the host-buffer drop-in launchers.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -359,6 +360,63 @@ void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_
     }
 }
 
+}  // namespace
+
+namespace {
+// The convergence test on a context whose st.f holds the input: every `interval`
+// iterations l = integrate(v) (times the mask when given) and, from the second check
+// on, one (ncc, time-TV) pair of l against the previous l (FP64, on the device).
+// Afterwards the TV of each metric series over the checks, all differences but the
+// last (TGVDeshadeProcessor.cpp:548-568).
+void convergence_on_context(tgvdct_context* c, const float* mask_dev, uint32_t interval,
+                            std::vector<double>& ncc, std::vector<double>& tv, double* mt,
+                            cudaStream_t s) {
+    const size_t n = voxels(c->prm);
+    c->prm.paint_iteration_interval = interval;
+    const uint32_t checks = interval > 0 ? c->prm.iteration_count / interval + 1 : 0;
+    DevBuf lbuf(2 * n), rbuf(n);
+    double* dmem = nullptr;
+    const size_t ndbl = 8 + 2 * (size_t)checks;
+    TGV_CUDA(cudaMalloc(&dmem, ndbl * sizeof(double)));
+    struct Free {
+        double* p;
+        ~Free() { cudaFree(p); }
+    } fr{dmem};
+    TGV_CUDA(cudaMemsetAsync(dmem, 0, ndbl * sizeof(double), s));
+    double* sums = dmem;
+    double* hist = dmem + 8;
+    DctPlan* plan = plan_of(c);
+    float* cur = lbuf.p;
+    float* prev = lbuf.p + n;
+    bool have_prev = false;
+    uint32_t count = 0;
+    run_loop(c, s, true, [&](uint32_t) {
+        poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, cur,
+                          c->prm.dct_mode, c->prm.poisson_eigen, s);
+        if (mask_dev)  // l *= mask (TGVDeshadeProcessor.cpp:85-89); r is not used
+            deshade_epilogue(c->st.u, cur, mask_dev, n, true, false, false, rbuf.p, s);
+        if (have_prev && count < checks) convergence_metrics(cur, prev, n, sums, hist + 2 * count++, s);
+        have_prev = true;
+        std::swap(cur, prev);
+        return false;
+    });
+    std::vector<double> h(2 * (size_t)count);
+    if (count)
+        TGV_CUDA(cudaMemcpyAsync(h.data(), hist, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TGV_CUDA(cudaStreamSynchronize(s));
+    ncc.resize(count);
+    tv.resize(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        ncc[k] = h[2 * k];
+        tv[k] = h[2 * k + 1];
+    }
+    for (int m = 0; m < 2; ++m) {
+        const std::vector<double>& v = m == 0 ? ncc : tv;
+        double acc = 0.0;
+        for (size_t i = 0; i + 2 < v.size(); ++i) acc += std::fabs(v[i + 1] - v[i]);
+        mt[m] = acc;
+    }
+}
 }  // namespace
 
 namespace {
@@ -975,6 +1033,119 @@ tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
         }
         check_tgv_flag(c, s);
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_convergence_test(const tgvdct_params* p, const float* f_host,
+                                      const float* mask_host, uint32_t check_iteration_interval,
+                                      double* ncc_history, double* time_tv_history,
+                                      uint32_t capacity, uint32_t* history_count,
+                                      double* metric_tv) {
+    return guarded([&] {
+        TGV_REQUIRE(p && f_host && metric_tv, "null argument");
+        TGV_REQUIRE(check_iteration_interval >= 1, "check_iteration_interval must be >= 1");
+        TGV_REQUIRE(capacity == 0 || (ncc_history && time_tv_history), "null history buffer");
+        CtxGuard g;
+        create_into(p, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(*p);
+        DevBuf m(mask_host ? n : 0);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        if (mask_host) TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        std::vector<double> ncc, tv;
+        convergence_on_context(c, mask_host ? m.p : nullptr, check_iteration_interval, ncc, tv,
+                               metric_tv, s);
+        check_tgv_flag(c, s);
+        const size_t k = std::min<size_t>(ncc.size(), capacity);
+        for (size_t i = 0; i < k; ++i) {
+            ncc_history[i] = ncc[i];
+            time_tv_history[i] = tv[i];
+        }
+        if (history_count) *history_count = (uint32_t)ncc.size();
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_convergence_optimization(const tgvdct_params* p, const float* f_host,
+                                              const float* mask_host,
+                                              int32_t set_negative_values_to_zero,
+                                              float* alpha0_out, float* alpha1_out,
+                                              float* denoised_host, float* shading_host,
+                                              float* deshaded_host) {
+    return guarded([&] {
+        TGV_REQUIRE(p && f_host && alpha0_out && alpha1_out && denoised_host && shading_host &&
+                        deshaded_host,
+                    "null argument");
+        tgvdct_params q = *p;
+        q.iteration_count = 10;  // check_iteration_count (TGVDeshadeProcessor.cpp:583)
+        q.paint_iteration_interval = 1;
+        CtxGuard g;
+        create_into(&q, &g.c);
+        tgvdct_context* c = g.c;
+        const size_t n = voxels(q);
+        DevBuf f(n), m(mask_host ? n : 0);
+        cudaStream_t s = 0;
+        TGV_CUDA(cudaMemcpyAsync(f.p, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        if (mask_host) TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        const float* mask_dev = mask_host ? m.p : nullptr;
+        auto metric = [&](double a0, double a1, int which) {
+            c->prm.alpha0 = (float)a0;
+            c->prm.alpha1 = (float)a1;
+            c->prm.iteration_count = 10;
+            TGV_CUDA(cudaMemcpyAsync(c->st.f, f.p, n * 4, cudaMemcpyDeviceToDevice, s));
+            std::vector<double> ncc, tv;
+            double mt[2];
+            convergence_on_context(c, mask_dev, 1, ncc, tv, mt, s);
+            return (float)mt[which];  // the reference keeps metrics as float
+        };
+        // decade of alpha1 = alpha0 (:587-612): the first decade whose NCC-series TV
+        // falls below the previous one ends the search
+        int converged = 0;
+        float before = 0.f;
+        for (int i = 0; i < 11; ++i) {
+            const double a = std::pow(10.0, -i);
+            const float v = metric(a, a, 0);
+            if (v < before) {
+                converged = i - 1;
+                break;
+            }
+            before = v;
+        }
+        const double alpha1 = std::pow(10.0, -converged);
+        // ratio alpha0 / alpha1 maximising the time-TV series' TV (:614-632)
+        const double ratios[9] = {1, 1.5, 1.8, 2, 2.2, 2.3, 2.35, 2.4, 2.45};
+        int best = 0;
+        float best_v = 0.f;
+        for (int i = 0; i < 9; ++i) {
+            const float v = metric(alpha1 * ratios[i], alpha1, 1);
+            if (v > best_v) {
+                best_v = v;
+                best = i;
+            }
+        }
+        const double alpha0 = ratios[best] * alpha1;
+        *alpha0_out = (float)alpha0;
+        *alpha1_out = (float)alpha1;
+        // the final deshade (:638-645): 500 iterations, the terminal program's overload
+        // of processTGV2L1GPUCuda (r weighted by the mask, l not; :122-166)
+        c->prm.alpha0 = (float)alpha0;
+        c->prm.alpha1 = (float)alpha1;
+        c->prm.iteration_count = 500;
+        c->prm.paint_iteration_interval = 0;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f.p, n * 4, cudaMemcpyDeviceToDevice, s));
+        run_loop(c, s, false, [](uint32_t) { return false; });
+        DevBuf l(n), r(n);
+        DctPlan* plan = plan_of(c);
+        poisson_integrate(plan, c->st.v[0], c->st.v[1], c->st.three ? c->st.v[2] : nullptr, l.p,
+                          c->prm.dct_mode, c->prm.poisson_eigen, s);
+        deshade_epilogue(c->st.u, l.p, mask_dev, n, false, set_negative_values_to_zero != 0, false,
+                         r.p, s);
+        TGV_CUDA(cudaMemcpyAsync(denoised_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
+        check_tgv_flag(c, s);
+        return TGVDCT_OK;
     });
 }
 

@@ -143,6 +143,11 @@ struct DctPlan {
     float* tf[2][3] = {};
     int* dev_err = nullptr;                        // set by a tensor-core pass whose wait timed out
     void* tc_block = nullptr;
+    // pipelined tensor-core passes (dct_tc2.cu): the matrices as shared-memory stage
+    // images, [BF16X3, TF32][fwd, inv][axis], and their number of K stages
+    void* pipe_img[2][2][3] = {};
+    int pipe_chunks[2][2][3] = {};
+    void* pipe_block = nullptr;
 };
 // Tensor-core passes need every side <= 256.
 bool dct_tc_supported(const DctPlan* p);
@@ -156,6 +161,11 @@ bool dct_tc_check(DctPlan* p, cudaStream_t st);
 void pass_tc(DctPlan* p, int axis, bool inverse, const float* in, float* out, int epi, float scale,
              bool div, const float* vx, const float* vy, const float* vz, int dct_mode,
              cudaStream_t st);
+// Pipelined tensor-core pass (TMA-fed, warp-specialised): returns false, doing
+// nothing, where its rules exclude the plan or the buffers (then pass_tc applies).
+bool dct_pipe_supported(const DctPlan* p);
+bool pass_pipe(DctPlan* p, int axis, bool inverse, const float* in, float* out, int epi,
+               float scale, int dct_mode, cudaStream_t st);
 DctPlan* dct_plan_create(int W, int H, int D);
 void dct_plan_destroy(DctPlan* p);
 size_t dct_plan_bytes(int W, int H, int D);
@@ -175,6 +185,10 @@ void inverse_cosine_transform(DctPlan* plan, const float* in, float* out, int dc
 void solve_poisson(DctPlan* plan, const float* in, float* out, int eigen_mode, cudaStream_t st);
 
 // ---- element-wise ------------------------------------------------------------
+// One check of the convergence test: appends (ncc(l, l_before), sum |l - l_before|)
+// to slot[0..1] (FP64 device memory).  sums: 8 zeroed doubles of scratch, left zeroed.
+void convergence_metrics(const float* l, const float* l_before, size_t n, double* sums,
+                         double* slot, cudaStream_t st);
 void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,
                       bool clamp, bool add_back, float* r, cudaStream_t st,
                       bool mask_again = false);

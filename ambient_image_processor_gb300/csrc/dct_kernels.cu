@@ -429,6 +429,7 @@ DctPlan* dct_plan_create(int W, int H, int D) {
 void dct_plan_destroy(DctPlan* p) {
     if (!p) return;
     if (p->tc_block) cudaFree(p->tc_block);
+    if (p->pipe_block) cudaFree(p->pipe_block);
     cudaFree(p->block);
     delete p;
 }
@@ -446,7 +447,7 @@ void any_pass(DctPlan* p, int axis, bool inverse, const float* in, float* out, i
     if (dct_mode == TGVDCT_DCT_FP32) {
         pass(p, axis, inverse ? p->inv[axis] : p->fwd[axis], in, out, epi, scale, A_PLAIN, 0, 0, 0,
              st);
-    } else {
+    } else if (!pass_pipe(p, axis, inverse, in, out, epi, scale, dct_mode, st)) {
         pass_tc(p, axis, inverse, in, out, epi, scale, false, nullptr, nullptr, nullptr, dct_mode,
                 st);
     }
@@ -527,7 +528,12 @@ void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float
     // forward: x (divergence fused into the operand load), y, z (+ Poisson division)
     if (dct_mode == TGVDCT_DCT_FP32)
         pass(p, 0, p->fwd[0], nullptr, t0, EPI_NONE, 1.f, A_DIVERGENCE, vx, vy, vz, st);
-    else
+    else if (dct_pipe_supported(p)) {
+        // the pipelined passes take a plain operand: divergence first, into t1
+        divergence(p, vx, vy, vz, t1, st);
+        if (!pass_pipe(p, 0, false, t1, t0, EPI_NONE, 1.f, dct_mode, st))
+            pass_tc(p, 0, false, nullptr, t0, EPI_NONE, 1.f, true, vx, vy, vz, dct_mode, st);
+    } else
         pass_tc(p, 0, false, nullptr, t0, EPI_NONE, 1.f, true, vx, vy, vz, dct_mode, st);
     if (p->D == 1) {
         any_pass(p, 1, false, t0, t1, epi, 1.f, dct_mode, st);

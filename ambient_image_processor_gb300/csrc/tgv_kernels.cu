@@ -42,6 +42,10 @@ struct Dual<TGVDCT_STATE_FP32> {
     using T = float;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float) { return p[i]; }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) { p[i] = v; }
+    // streaming store (evict-first): the next read of the field is an iteration away
+    static __device__ __forceinline__ void st_cs(T* p, size_t i, float v, float) {
+        __stcs(p + i, v);
+    }
 };
 
 template <>
@@ -52,6 +56,9 @@ struct Dual<TGVDCT_STATE_BF16_DUAL> {
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) {
         p[i] = __float2bfloat16_rn(v);
+    }
+    static __device__ __forceinline__ void st_cs(T* p, size_t i, float v, float) {
+        __stcs((unsigned short*)p + i, __bfloat16_as_ushort(__float2bfloat16_rn(v)));
     }
 };
 
@@ -72,6 +79,10 @@ struct Dual<TGVDCT_STATE_FX16_DUAL> {
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float enc) {
         const float c = fminf(fmaxf(v * enc, -32767.f), 32767.f);
         p[i] = (T)__float_as_int(c + 12582912.f);  // low 16 bits: the rounded code
+    }
+    static __device__ __forceinline__ void st_cs(T* p, size_t i, float v, float enc) {
+        const float c = fminf(fmaxf(v * enc, -32767.f), 32767.f);
+        __stcs((short*)p + i, (short)__float_as_int(c + 12582912.f));
     }
 };
 
@@ -675,6 +686,7 @@ struct Args {
     T* p_out[3];
     T* q_out[6];  // state order: xx yy zz xy xz yz
     float tau, sigma, theta, tau_lambda, alpha0, alpha1;
+    float thr_p, thr_q;  // squared-norm bounds below which the projections are skipped
     float penc, pdec, qenc, qdec;
     int skip_bz;
     int* err;
@@ -722,18 +734,24 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int 
 
 // p <- proj_{alpha1}(p + sigma (g - vb)), the reference's tgv_kernel_part22 arithmetic.
 // The division by max(1, |p|/alpha1) is skipped when that factor is 1 (x / 1 == x).
+// thr = alpha1^2 (1 - 2^-19): while the float sum of squares stays at or below it,
+// |p| / alpha1 rounds to at most 1 whatever the last-bit errors of the sum (5
+// roundings) and of norm3df (a few ulp), so the projection is the identity and the
+// norm is not evaluated; the result is bit-identical to evaluating it.
 template <bool THREE>
 __device__ __forceinline__ void dual_p_update(const float* g, const float* vb, float* p,
-                                              float sigma, float alpha1) {
+                                              float sigma, float alpha1, float thr) {
     p[0] = __fmaf_rn(sigma, g[0] - vb[0], p[0]);
     p[1] = __fmaf_rn(sigma, g[1] - vb[1], p[1]);
-    float nrm;
+    float ss = p[0] * p[0] + p[1] * p[1];  // also the 2-D norm's argument (tgv2_common_2d.cu:113)
     if constexpr (THREE) {
         p[2] = __fmaf_rn(sigma, g[2] - vb[2], p[2]);
-        nrm = norm3df(p[0], p[1], p[2]);
-    } else {
-        nrm = sqrtf(p[0] * p[0] + p[1] * p[1]);
+        ss = ss + p[2] * p[2];
     }
+    if (!(ss > thr)) return;  // inside the ball (NaN: the reference divides by 1 as well)
+    float nrm;
+    if constexpr (THREE) nrm = norm3df(p[0], p[1], p[2]);
+    else nrm = sqrtf(ss);
     nrm = fmaxf(1.f, nrm / alpha1);
     if (nrm > 1.f) {
         p[0] = p[0] / nrm;
@@ -744,10 +762,11 @@ __device__ __forceinline__ void dual_p_update(const float* g, const float* vb, f
 
 // q <- proj_{alpha0}(q + sigma E vbar); xm/ym/zm: vbar at x-1 / y-1 / z-1 (0 outside);
 // q in slot order xx yy xy zz xz yz (tgv_kernel_part5 arithmetic)
+// thr = alpha0^2 (1 - 2^-19): at or below it sqrtf(sq) / alpha0 rounds to at most 1.
 template <bool THREE>
 __device__ __forceinline__ void dual_q_update(const float* vb, const float* xm, const float* ym,
                                               const float* zm, float* q, float sigma,
-                                              float alpha0) {
+                                              float alpha0, float thr) {
     const float exx = xm[0] - vb[0];
     const float eyy = ym[1] - vb[1];
     const float exy = ((xm[1] - vb[1]) + (ym[0] - vb[0])) * 0.5f;
@@ -764,6 +783,7 @@ __device__ __forceinline__ void dual_q_update(const float* vb, const float* xm, 
         q[5] = __fmaf_rn(sigma, eyz, q[5]);
         sq = sq + q[3] * q[3] + 2.f * q[4] * q[4] + 2.f * q[5] * q[5];
     }
+    if (!(sq > thr)) return;
     const float qn = fmaxf(1.f, sqrtf(sq) / alpha0);
     constexpr int NQ = THREE ? 6 : 3;
     if (qn > 1.f) {
@@ -772,7 +792,7 @@ __device__ __forceinline__ void dual_q_update(const float* vb, const float* xm, 
     }
 }
 
-template <int PREC, bool THREE, int DATA, int NS>
+template <int PREC, bool THREE, int DATA, int NS, bool MASKED>
 __global__ void __launch_bounds__(tma::NTHREADS, 2)
     tgv_fused_tma_kernel(const __grid_constant__ tma::Args<typename Dual<PREC>::T> a) {
     using namespace tma;
@@ -878,7 +898,8 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     // ubar(z) own/+x/+y, ubar(z+1) own, vbar(z) own, p(z)
     // a voxel outside the masked deshade's domain keeps p = q = 0 and u, v unchanged
     auto live = [&](int plane) {
-        return a.dom == nullptr || a.dom[(size_t)plane * a.WH + col] != 0;
+        if constexpr (MASKED) return a.dom[(size_t)plane * a.WH + col] != 0;
+        else return true;
     };
     auto dual_p_at = [&](const uint8_t* sz, const uint8_t* sn, bool lv) {
         if (!lv) return make_float3(0.f, 0.f, 0.f);
@@ -890,7 +911,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         float pp[3];
 #pragma unroll
         for (int c = 0; c < NC; ++c) pp[c] = dec_p(pb(sz, c)[odp]);
-        dual_p_update<THREE>(g, vb, pp, a.sigma, a.alpha1);
+        dual_p_update<THREE>(g, vb, pp, a.sigma, a.alpha1, a.thr_p);
 #pragma unroll
         for (int c = 0; c < NC; ++c) pp[c] = rq_p(pp[c]);
         return make_float3(pp[0], pp[1], THREE ? pp[2] : 0.f);
@@ -914,7 +935,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         }
 #pragma unroll
         for (int k = 0; k < NQ; ++k) q[k] = dec_q(qb(sz, k)[odq]);
-        dual_q_update<THREE>(vb, xm, ym, zm, q, a.sigma, a.alpha0);
+        dual_q_update<THREE>(vb, xm, ym, zm, q, a.sigma, a.alpha0, a.thr_q);
 #pragma unroll
         for (int k = 0; k < NQ; ++k) out[k * NE + e] = rq_q(q[k]);
     };
@@ -922,9 +943,9 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     auto load_tile = [&](int z) {
         if (interior && z < z1) {
             const size_t i = (size_t)z * a.WH + col;
-            tu = a.u[i];
-            tf = a.f[i];
-            for (int c = 0; c < NC; ++c) tv[c] = a.v[c][i];
+            tu = __ldcs(a.u + i);  // read once per iteration: evict-first
+            tf = __ldcs(a.f + i);
+            for (int c = 0; c < NC; ++c) tv[c] = __ldcs(a.v[c] + i);
         }
     };
 
@@ -1023,8 +1044,8 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             // outside the domain the stored state is already the frozen one
             const bool lt = live(t);
             if (lt) {
-                a.u[i] = uu;
-                a.ubar_out[i] = uu + a.theta * (uu - pu);
+                __stcs(a.u + i, uu);
+                __stcs(a.ubar_out + i, uu + a.theta * (uu - pu));
             }
             const bool has_next = t + 1 < D;
             const float qxx = Qt[e], qyy = Qt[NE + e], qxy = Qt[2 * NE + e];
@@ -1048,17 +1069,17 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
                     const float vn = vo[c] - a.tau * (d[c] - pv[c]);
-                    a.v[c][i] = vn;
-                    a.vbar_out[c][i] = vn + a.theta * (vn - vo[c]);
-                    S::st(a.p_out[c], i, pv[c], a.penc);
+                    __stcs(a.v[c] + i, vn);
+                    __stcs(a.vbar_out[c] + i, vn + a.theta * (vn - vo[c]));
+                    S::st_cs(a.p_out[c], i, pv[c], a.penc);
                 }
-                S::st(a.q_out[0], i, qxx, a.qenc);
-                S::st(a.q_out[1], i, qyy, a.qenc);
-                S::st(a.q_out[3], i, qxy, a.qenc);
+                S::st_cs(a.q_out[0], i, qxx, a.qenc);
+                S::st_cs(a.q_out[1], i, qyy, a.qenc);
+                S::st_cs(a.q_out[3], i, qxy, a.qenc);
                 if constexpr (THREE) {
-                    S::st(a.q_out[2], i, qzz, a.qenc);
-                    S::st(a.q_out[4], i, qxz, a.qenc);
-                    S::st(a.q_out[5], i, qyz, a.qenc);
+                    S::st_cs(a.q_out[2], i, qzz, a.qenc);
+                    S::st_cs(a.q_out[4], i, qxz, a.qenc);
+                    S::st_cs(a.q_out[5], i, qyz, a.qenc);
                 }
             }
 #pragma unroll
@@ -1288,16 +1309,26 @@ TmaCache<PREC>* tma_cache(TgvState& s) {
 template <int PREC, bool THREE, int DATA>
 void launch_tma(const tma::Args<typename Dual<PREC>::T>& a, cudaStream_t st) {
     constexpr int NS = tma_stages<PREC>();
-    auto kern = tgv_fused_tma_kernel<PREC, THREE, DATA, NS>;
+    // the domain test is compiled only into the masked instances
+    auto kern = a.dom ? tgv_fused_tma_kernel<PREC, THREE, DATA, NS, true>
+                      : tgv_fused_tma_kernel<PREC, THREE, DATA, NS, false>;
     const size_t smem = tma_smem_bytes<PREC>();
-    static bool configured = false;
-    if (!configured) {
+    static bool configured[2] = {false, false};
+    bool& done = configured[a.dom ? 1 : 0];
+    if (!done) {
         TGV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
+        done = true;
     }
     const dim3 grid(ceil_div(a.W, tma::TX), ceil_div(a.H, tma::TY), ceil_div(a.D, a.zchunk));
     kern<<<grid, tma::NTHREADS, smem, st>>>(a);
     TGV_CHECK_LAUNCH();
+}
+
+// alpha^2 (1 - 2^-19), or -1 (never skip) where alpha^2 would leave the normal range
+float projection_skip_bound(float alpha) {
+    const double a2 = (double)alpha * alpha;
+    if (!(a2 > 1e-30 && a2 < 1e30)) return -1.f;
+    return (float)(a2 * (1.0 - 1.0 / (1 << 19)));
 }
 
 template <int PREC>
@@ -1314,6 +1345,8 @@ void iterate_tma(TgvState& s, const TgvStep& k, int* err, cudaStream_t st) {
     a.pdec = k.alpha1 / 32767.f;
     a.qenc = 32767.f / k.alpha0;
     a.qdec = k.alpha0 / 32767.f;
+    a.thr_p = projection_skip_bound(k.alpha1);
+    a.thr_q = projection_skip_bound(k.alpha0);
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
     a.err = err;
     a.dom = s.domain;

@@ -409,6 +409,59 @@ def run_ours(args):
     return 0
 
 
+def run_accuracy(args):
+    """Error of the whole deshade against the FP64 oracle, per precision form.
+
+    The FP64 oracle runs the same workload (log domain, no clamp) on the host cores
+    (several minutes at 256x256x192 x 1500); each GPU form runs once.  Prints one
+    JSON line: relative L2 error of the denoised image u, the shading field l and the
+    corrected image r (all exponentiated back, as the user gets them), and the
+    voxel-iterations per second of each form's iteration loop."""
+    import torch
+    import oracle
+    import ambient_image_processor_gb300 as pkg
+
+    d, h, w, iters = WORKLOADS[args.workload]
+    if args.iterations:
+        iters = args.iterations
+    f_host = make_input(args.workload)
+    oracle.set_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    ou, ol, orr = oracle.process_tgv2_l1(np.log(f_host.astype(np.float64)), 1.0, 2.0, 1.0, iters,
+                                         set_negative_values_to_zero=False, dtype=np.float64)
+    t_oracle = time.perf_counter() - t0
+    ref = {"u": np.exp(ou), "l": np.exp(ol), "r": np.exp(orr)}
+    forms = [("fp32", 0, "fp32", 0), ("fp32", 0, "fp32", 1), ("fp32", 0, "bf16x3", 1),
+             ("fp32", 0, "tf32", 1), ("fx16_dual", 2, "fp32", 1), ("bf16_dual", 1, "fp32", 1),
+             ("fx16_dual", 2, "bf16x3", 1)]
+    f = torch.from_numpy(f_host).cuda()
+    u, l, r = (torch.empty_like(f) for _ in range(3))
+    stream = torch.cuda.current_stream()
+    res = []
+    for name, prec, dct, eig in forms:
+        prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iters,
+                                 state_precision=prec, dct_mode=DCT_MODES[dct],
+                                 poisson_eigen=eig)
+        with pkg.Context(prm) as ctx:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.process_dev(f.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
+                            set_negative_values_to_zero=False, log_domain=True,
+                            stream=stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ctx.check_device_error(stream.cuda_stream)
+        got = {"u": u.cpu().numpy(), "l": l.cpu().numpy(), "r": r.cpu().numpy()}
+        err = {k: float(np.linalg.norm(got[k] - ref[k]) / np.linalg.norm(ref[k])) for k in ref}
+        ms = e0.elapsed_time(e1)
+        res.append({"state": name, "dct": dct, "eigen": "accurate" if eig else "reference",
+                    "rel_l2": err, "ms_per_deshade": ms,
+                    "voxel_iters_per_s": d * h * w * iters / (ms * 1e-3)})
+    print(json.dumps({"accuracy_vs_fp64": res, "workload": args.workload, "iterations": iters,
+                      "oracle_seconds": t_oracle, "oracle_threads": os.cpu_count()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -431,9 +484,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="error of every precision form against the FP64 oracle instead")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.accuracy:
+        return run_accuracy(args)
     return run_ours(args)
 
 

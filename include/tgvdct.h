@@ -330,6 +330,37 @@ tgvdct_status tgvdct_process_dev(tgvdct_context* ctx, const float* f_dev, const 
                                  int32_t log_domain, float* u_dev, float* l_dev, float* r_dev,
                                  tgvdct_iteration_callback callback, void* user, void* stream);
 
+/* ---- convergence metrics ------------------------------------------------------ */
+/* Replaces TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceTest and
+   ..._convergenceTestMetric (tgv_deshade/TGVDeshadeProcessor.cpp:479-568): runs the
+   TGV loop of p (callback cadence check_iteration_interval) and at every check
+   integrates l from v (times the mask when mask_host is given).  From the second
+   check on it records the normalised cross-correlation of l with the previous
+   check's l (normalised with the current l's mean for both images, as the reference
+   does, :190-193) and their time total variation sum |l - l_before|.  The first
+   `capacity` pairs go to ncc_history / time_tv_history, their number to
+   *history_count (may be NULL).  metric_tv[0], [1]: the total variation of each
+   series over the checks, sum |h[i+1] - h[i]| for i < count - 2 (the reference's
+   bound).  Sums are FP64 on the device (the reference accumulates in float). */
+tgvdct_status tgvdct_convergence_test(const tgvdct_params* p, const float* f_host,
+                                      const float* mask_host, uint32_t check_iteration_interval,
+                                      double* ncc_history, double* time_tv_history,
+                                      uint32_t capacity, uint32_t* history_count,
+                                      double* metric_tv);
+
+/* Replaces TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceOptimization
+   (TGVDeshadeProcessor.cpp:571-646): picks alpha1 = alpha0 = 10^-i by the first decade
+   whose 10-iteration NCC-series TV drops, then alpha0 / alpha1 among {1, 1.5, 1.8, 2,
+   2.2, 2.3, 2.35, 2.4, 2.45} by the largest time-TV-series TV, and runs the 500-iteration
+   deshade with them (r weighted by the mask if given, then clamped if asked).  p gives
+   lambda and the modes; its alphas and iteration count are not used. */
+tgvdct_status tgvdct_convergence_optimization(const tgvdct_params* p, const float* f_host,
+                                              const float* mask_host,
+                                              int32_t set_negative_values_to_zero,
+                                              float* alpha0_out, float* alpha1_out,
+                                              float* denoised_host, float* shading_host,
+                                              float* deshaded_host);
+
 /* ---- masked deshade (tgv_deshade_masked/) ---------------------------------- */
 /* Restricts the TGV loop of a context to the voxels whose mask value is >= 1
    (TGVDeshadeMaskedProcessor::buildMaskIndices, TGVDeshadeMaskedProcessor.cpp:337-385):

@@ -58,6 +58,9 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = [p, p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
             fn = getattr(L, f"oracle_masked_deshade_epilogue_{suf}")
             fn.argtypes = [p, p, p, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, p]
+            fn = getattr(L, f"oracle_convergence_test_{suf}")
+            fn.argtypes = [p, ctypes.c_void_p, _u, _u, _u, _d, _d, _d, _u, _u, p, p, _u, p]
+            fn.restype = _u
             fn = getattr(L, f"oracle_tgv2_deshade_masked_{suf}")
             fn.argtypes = [p, p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int,
                            ctypes.c_int, p, p, p, p]
@@ -220,6 +223,23 @@ def process_tgv2_l1_masked(f, mask, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterati
     return u, l, r
 
 
+def convergence_test(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=20, interval=1,
+                     mask=None, dtype=np.float64):
+    """TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceTest(+Metric): returns
+    (ncc history, time-TV history, (TV of the NCC series, TV of the time-TV series))."""
+    f = np.ascontiguousarray(f, dtype=dtype)
+    w, h, d = _shape3(f)
+    cap = max(1, iterations // max(interval, 1))
+    ncc, tv, mt = np.zeros(cap, dtype), np.zeros(cap, dtype), np.zeros(2, dtype)
+    mptr = None
+    if mask is not None:
+        mask = np.ascontiguousarray(mask, dtype=dtype)
+        mptr = mask.ctypes.data_as(ctypes.c_void_p)
+    k = getattr(lib(), f"oracle_convergence_test_{_dt(dtype)}")(
+        f, mptr, w, h, d, lambda_, alpha0, alpha1, iterations, interval, ncc, tv, cap, mt)
+    return ncc[:k], tv[:k], mt
+
+
 def tgv2_gradient(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=10, *, grad_u=None,
                   grad_v=None, data_term="l1", tau=0.0, sigma=0.0, theta=1.0):
     """FP64 reverse mode of the 3-D loop: returns (u_K, dL/df, dL/d(lambda, alpha0, alpha1))
@@ -265,6 +285,9 @@ def ref() -> ctypes.CDLL:
         R.ref_tgv2_denoise_f32.argtypes = [ctypes.c_int, _f32p, _u, _u, _u, f, f, f, _u, _f32p]
         R.ref_process_tgv2_l1_f32.argtypes = [_f32p, _u, _u, _u, f, f, f, _u, ctypes.c_int,
                                               _f32p, _f32p, _f32p]
+        R.ref_convergence_test_f32.argtypes = [_f32p, ctypes.c_void_p, _u, _u, _u, f, f, f, _u,
+                                               _u, _f32p, _f32p, _u, _f32p]
+        R.ref_convergence_test_f32.restype = _u
         R.ref_tgv2_l1_deshade_masked_f32.argtypes = [_f32p, _f32p, _u, _u, _u, f, f, f, _u,
                                                      _f32p, _f32p, _f32p, _f32p]
         R.ref_process_tgv2_l1_masked_f32.argtypes = [_f32p, _f32p, _u, _u, _u, f, f, f, _u,

@@ -92,6 +92,26 @@ int oracle_set_threads(int n) {
                                        u, vx, vy, vz, nullptr, dom.data());                       \
     }
 
+#define ORACLE_CONVERGENCE(T, SUF)                                                                \
+    unsigned oracle_convergence_test_##SUF(const T* f, const T* mask, unsigned w, unsigned h,    \
+                                           unsigned d, double lambda, double alpha0,             \
+                                           double alpha1, unsigned iterations, unsigned interval, \
+                                           T* ncc, T* tv, unsigned capacity, T* metric_tv) {      \
+        auto r = oracle::convergence_test<T>(                                                     \
+            f, mask, dims(w, h, d),                                                               \
+            make_params(lambda, alpha0, alpha1, iterations, 0, 0, 1, oracle::L1, 0), interval);   \
+        for (size_t i = 0; i < r.ncc.size() && i < capacity; ++i) {                              \
+            ncc[i] = r.ncc[i];                                                                    \
+            tv[i] = r.tv[i];                                                                      \
+        }                                                                                         \
+        metric_tv[0] = r.metric_tv[0];                                                            \
+        metric_tv[1] = r.metric_tv[1];                                                            \
+        return (unsigned)r.ncc.size();                                                            \
+    }
+ORACLE_CONVERGENCE(float, f32)
+ORACLE_CONVERGENCE(double, f64)
+#undef ORACLE_CONVERGENCE
+
 ORACLE_TYPED(float, f32)
 ORACLE_TYPED(double, f64)
 

@@ -4,6 +4,7 @@
 // ITK-level glue that call them are restated here from
 // source/modules/tgv_deshade/TGVDeshadeProcessor.cpp:122-166,386-408 and
 // source/modules/cuda_image_operations/CudaImageOperationsProcessor.cpp:286-294.
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <vector>
@@ -329,6 +330,87 @@ void ref_process_tgv2_l1_masked_f32(const float* f, const float* mask, uint w, u
     take(u, denoised, n);
     take(l, shading, n);
     take(r, deshaded, n);
+}
+
+// processTGV2L1DeshadeCuda_convergenceTest / ..._convergenceTestMetric
+// (TGVDeshadeProcessor.cpp:479-568) on the reference's launcher and Poisson chain,
+// with the float image statistics of :168-220 restated (ITK order: x fastest).
+unsigned ref_convergence_test_f32(const float* f, const float* mask, uint w, uint h, uint d,
+                                  float lambda, float alpha0, float alpha1, uint iterations,
+                                  uint interval, float* ncc, float* tv, unsigned capacity,
+                                  float* metric_tv) {
+    const size_t n = (size_t)w * h * d;
+    std::vector<float> l_before;
+    std::vector<float> hn, ht;
+    auto mean = [&](const std::vector<float>& a) {
+        float m = 0;
+        for (float v : a) m += v;
+        return m /= (float)n;
+    };
+    auto stdev = [&](const std::vector<float>& a, float m) {
+        float s = 0;
+        for (float v : a) {
+            const float dd = v - m;
+            s += dd * dd;
+        }
+        return std::sqrt(s / (float)(n - 1));
+    };
+    DeshadeIterationCallback<float> cb = [&](uint, uint, float*, float* vx, float* vy,
+                                             float* vz) {
+        float* l = integrate<float>(vx, vy, vz, w, h, d);
+        if (mask) {
+            float* mk = new float[n];
+            std::memcpy(mk, mask, sizeof(float) * n);
+            float* t = multiply_kernel_launch<float>(l, mk, w, h, d);
+            delete[] mk;
+            delete[] l;
+            l = t;
+        }
+        std::vector<float> cur(l, l + n);
+        delete[] l;
+        if (!l_before.empty()) {
+            const float m1 = mean(cur), s1 = stdev(cur, m1);
+            const float m2 = mean(cur), s2 = stdev(l_before, m2);
+            float acc = 0;
+            for (size_t i = 0; i < n; ++i) acc += (cur[i] - m1) * (l_before[i] - m2);
+            hn.push_back(acc / (s1 * s2 * (float)n));
+            float* a = new float[n];
+            float* b = new float[n];
+            std::memcpy(a, cur.data(), sizeof(float) * n);
+            std::memcpy(b, l_before.data(), sizeof(float) * n);
+            float* diff = subtract_kernel_launch<float>(a, b, w, h, d);
+            float t = 0;
+            for (size_t i = 0; i < n; ++i) t += std::fabs(diff[i]);
+            delete[] a;
+            delete[] b;
+            delete[] diff;
+            ht.push_back(t);
+        }
+        l_before.swap(cur);
+        return false;
+    };
+    float* fin = new float[n];
+    std::memcpy(fin, f, sizeof(float) * n);
+    float *ox, *oy, *oz;
+    float* ou = tgv2_l1_deshade_launch<float>(fin, w, h, d, lambda, iterations, interval, -1, cb,
+                                              alpha0, alpha1, &ox, &oy, &oz);
+    delete[] fin;
+    delete[] ou;
+    delete[] ox;
+    delete[] oy;
+    delete[] oz;
+    const std::vector<float>* series[2] = {&hn, &ht};
+    for (int m = 0; m < 2; ++m) {
+        float acc = 0;
+        for (size_t i = 0; i + 2 < series[m]->size(); ++i)
+            acc += std::fabs((*series[m])[i + 1] - (*series[m])[i]);
+        metric_tv[m] = acc;
+    }
+    for (size_t i = 0; i < hn.size() && i < capacity; ++i) {
+        ncc[i] = hn[i];
+        tv[i] = ht[i];
+    }
+    return (unsigned)hn.size();
 }
 
 }  // extern "C"

@@ -471,4 +471,82 @@ void masked_deshade_epilogue(const T* u, T* l, const T* mask, bool set_negative_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Convergence metrics of TGVDeshadeProcessor::processTGV2L1DeshadeCuda_convergenceTest
+// and ..._convergenceTestMetric (TGVDeshadeProcessor.cpp:479-568), with the image
+// statistics of :168-220 accumulated in T in the images' linear order (the
+// reference's ITK iteration order, x fastest; T = float is its own arithmetic).
+// The deshade loop calls back every `interval` iterations; each call integrates l
+// from v (times the mask when one is given); from the second call on it records
+// the normalised cross-correlation of l with the previous l and their time total
+// variation sum |l - l_before|.  The normalisation uses the mean of the current l
+// for both images, as the reference's normalized_cross_correlation does (:190-193).
+template <class T>
+T linear_mean(const std::vector<T>& a) {
+    T m = 0;
+    for (const T v : a) m = T(m + v);
+    return T(m / T(a.size()));
+}
+template <class T>
+T linear_std(const std::vector<T>& a, T mean) {
+    T s = 0;
+    for (const T v : a) {
+        const T d = T(v - mean);
+        s = T(s + T(d * d));
+    }
+    return T(std::sqrt(T(s / T(a.size() - 1))));
+}
+template <class T>
+T normalized_cross_correlation(const std::vector<T>& a, const std::vector<T>& b) {
+    const T m1 = linear_mean(a), s1 = linear_std(a, m1);
+    const T m2 = linear_mean(a), s2 = linear_std(b, m2);
+    T acc = 0;
+    for (size_t i = 0; i < a.size(); ++i) acc = T(acc + T(T(a[i] - m1) * T(b[i] - m2)));
+    return T(acc / T(T(s1 * s2) * T(a.size())));
+}
+template <class T>
+T time_tv(const std::vector<T>& a, const std::vector<T>& b) {
+    T s = 0;
+    for (size_t i = 0; i < a.size(); ++i) s = T(s + std::fabs(T(a[i] - b[i])));
+    return s;
+}
+
+template <class T>
+struct ConvergenceHistory {
+    std::vector<T> ncc, tv;
+    T metric_tv[2] = {0, 0};
+};
+
+template <class T>
+ConvergenceHistory<T> convergence_test(const T* f, const T* mask, Dims g, Params prm,
+                                       unsigned interval) {
+    const index_t n = g.n();
+    ConvergenceHistory<T> h;
+    std::vector<T> l_before;
+    prm.paint_interval = interval;
+    std::vector<T> u(n), vx(n), vy(n), vz(n);
+    tgv2_deshade<T>(f, g, prm, u.data(), vx.data(), vy.data(), vz.data(),
+                    [&](unsigned, unsigned, const T*, const T* px, const T* py, const T* pz) {
+                        std::vector<T> l(n);
+                        integrate_poisson_dct<T>(px, py, pz, g, l.data());
+                        if (mask)
+                            for (index_t i = 0; i < n; ++i) l[i] = T(l[i] * mask[i]);
+                        if (!l_before.empty()) {
+                            h.ncc.push_back(normalized_cross_correlation(l, l_before));
+                            h.tv.push_back(time_tv(l, l_before));
+                        }
+                        l_before.swap(l);
+                        return false;
+                    });
+    // :556-566: sum of |h[i+1] - h[i]| for i < size - 2 (the last difference is left out)
+    const std::vector<T>* series[2] = {&h.ncc, &h.tv};
+    for (int m = 0; m < 2; ++m) {
+        T acc = 0;
+        const std::vector<T>& v = *series[m];
+        for (size_t i = 0; i + 2 < v.size(); ++i) acc = T(acc + std::fabs(T(v[i + 1] - v[i])));
+        h.metric_tv[m] = acc;
+    }
+    return h;
+}
+
 }  // namespace oracle

@@ -10,6 +10,7 @@ read the committed .npz files.
 """
 from __future__ import annotations
 
+import ctypes
 import os
 import sys
 
@@ -50,6 +51,12 @@ MASKED = [("masked3d", (8, 12, 16), 61, 1.0, 2.0, 1.0, 40, 0),
           ("masked3d_odd", (7, 11, 13), 62, 0.8, 1.5, 0.9, 35, 1),
           ("masked2d", (1, 20, 24), 63, 1.0, 2.0, 1.0, 40, 0),
           ("masked2d_back", (1, 17, 21), 64, 1.0, 2.0, 1.0, 30, 1)]
+
+
+# convergence metrics: (name, shape, seed, lambda, alpha0, alpha1, iterations, interval, masked)
+CONVERGENCE = [("convergence3d", (6, 10, 12), 71, 1.0, 2.0, 1.0, 14, 1, False),
+               ("convergence3d_mask", (5, 9, 11), 72, 1.0, 1.5, 0.8, 16, 2, True),
+               ("convergence3d_d1", (1, 16, 20), 73, 1.0, 2.0, 1.0, 12, 1, False)]
 
 
 def domain_mask(shape, seed):
@@ -130,6 +137,19 @@ def main() -> int:
         cases[name] = dict(f=f, mask=mask, u=u, v_x=vx, v_y=vy, v_z=vz, denoised=du,
                            shading=dl, deshaded=dr, add_background_back=np.array(back),
                            params=np.array([lam, a0, a1, it], np.float64))
+    for name, shape, seed, lam, a0, a1, it, interval, masked in CONVERGENCE:
+        f = tissue_phantom_3d(*shape, seed=seed)
+        d, h, w = shape
+        mask = domain_mask(shape, seed) if masked else None
+        cap = it
+        ncc, tv, mt = np.zeros(cap, np.float32), np.zeros(cap, np.float32), np.zeros(2, np.float32)
+        k = R.ref_convergence_test_f32(f, None if mask is None else mask.ctypes.data_as(
+            ctypes.c_void_p), w, h, d, lam, a0, a1, it, interval, ncc, tv, cap, mt)
+        c = dict(f=f, ncc=ncc[:k], time_tv=tv[:k], metric_tv=mt,
+                 params=np.array([lam, a0, a1, it, interval], np.float64))
+        if mask is not None:
+            c["mask"] = mask
+        cases[name] = c
     written = 0
     for name, c in cases.items():
         path = os.path.join(OUT, name + ".npz")

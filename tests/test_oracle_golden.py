@@ -111,6 +111,17 @@ def test_full_mask_is_the_unmasked_loop():
         assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("name", ["convergence3d", "convergence3d_mask", "convergence3d_d1"])
+def test_convergence_metrics_match_reference(name):
+    """processTGV2L1DeshadeCuda_convergenceTest(+Metric): NCC and time-TV of l between
+    checks, and their total variation over the history."""
+    g = load_golden(name)
+    lam, a0, a1, it, interval = g["params"]
+    ncc, tv, mt = oracle.convergence_test(g["f"], lam, a0, a1, int(it), int(interval),
+                                          mask=g.get("mask"), dtype=np.float32)
+    assert same(ncc, g["ncc"]) and same(tv, g["time_tv"]) and same(mt, g["metric_tv"])
+
+
 def test_forward_dct_is_scipy_dctn():
     scipy_fft = pytest.importorskip("scipy.fft")
     rng = np.random.default_rng(0)
