@@ -134,6 +134,9 @@ struct DctPlan {
     float* inv[3] = {nullptr, nullptr, nullptr};   // S (N x N) per axis
     float* cosk[3] = {nullptr, nullptr, nullptr};  // cospif(k / N), device-evaluated
     float* eig[3] = {nullptr, nullptr, nullptr};   // 4 sin^2(pi k / 2N)
+    // 2 cosk * 2^32 as exact integers (sides <= 256; null otherwise): the FP64-free
+    // form of the reference eigenvalues (poisson_den_ref)
+    long long* cosk_fx[3] = {nullptr, nullptr, nullptr};
     float* tmp[2] = {nullptr, nullptr};            // two V-sized scratch volumes
     void* block = nullptr;                         // owning allocation (null for views)
     // tensor-core operands (sides <= 256): per axis, forward and inverse matrices
@@ -185,7 +188,36 @@ void inverse_cosine_transform(DctPlan* plan, const float* in, float* out, int dc
 void solve_poisson(DctPlan* plan, const float* in, float* out, int eigen_mode, cudaStream_t st);
 
 // ---- element-wise ------------------------------------------------------------
-// One check of the convergence test: appends (ncc(l, l_before), sum |l - l_before|)
+// The reference's Poisson denominator (float)(base - 2a - 2b - 2c), evaluated by
+// solve_poisson_in_cosine_domain.cu:48-53 in FP64 from the float cosines a, b, c of
+// the three frequencies (c = 0 in 2-D), without FP64 arithmetic (a small fraction of
+// the FP32 rate on this GPU).  For sides <= 256 every float cospi(k / N) is 0 or at
+// least sin(pi / 512) > 2^-8 in magnitude, so 2 cospi(k / N) is an integer multiple
+// of 2^-32 and the FP64 sum is exact.  The plan keeps t[k] = 2 cospi(k / N) * 2^32 as
+// 64-bit integers (DctPlan::cosk_fx, checked exact when built); the sum
+// S = base * 2^32 - t0 - t1 - t2 is then exact, 0 <= S < 2^36, and
+// fixed32_to_float rounds S * 2^-32 once to float: bit-identical to the FP64 form.
+__device__ __forceinline__ float fixed32_to_float(long long S) {
+    const unsigned long long u = (unsigned long long)S;
+    const float hi = __uint2float_rn((unsigned)(u >> 12));                  // < 2^24: exact
+    const float lo = __uint2float_rn((unsigned)(u & 4095u)) * 2.44140625e-4f;  // exact, < 1
+    return (hi + lo) * 9.5367431640625e-07f;  // one rounding, then 2^-20 (exact)
+}
+__device__ __forceinline__ float poisson_den_ref(int three, const long long* t0,
+                                                 const long long* t1, const long long* t2,
+                                                 const float* c0, const float* c1,
+                                                 const float* c2, int kx, int ky, int kz) {
+    if (t0) {
+        long long S = (three ? 6ll : 4ll) * 4294967296ll - t0[kx] - t1[ky];
+        if (three) S -= t2[kz];
+        return fixed32_to_float(S);
+    }
+    double den = (three ? 6.0 : 4.0) - 2.0 * (double)c0[kx] - 2.0 * (double)c1[ky];
+    if (three) den -= 2.0 * (double)c2[kz];
+    return (float)den;
+}
+
+// One check of the convergence test:// One check of the convergence test: appends (ncc(l, l_before), sum |l - l_before|)
 // to slot[0..1] (FP64 device memory).  sums: 8 zeroed doubles of scratch, left zeroed.
 void convergence_metrics(const float* l, const float* l_before, size_t n, double* sums,
                          double* slot, cudaStream_t st);

@@ -43,6 +43,17 @@ __global__ void cosk_kernel(float* out, int N) {
     if (k < N) out[k] = cospif((float)k / (float)N);  // solve_poisson_in_cosine_domain.cu:48-53
 }
 
+// fx[k] = 2 cosk[k] * 2^32 as an integer; raises *inexact where the float is not an
+// integer multiple of 2^-32 (then the plan keeps the FP64 form)
+__global__ void cosk_fx_kernel(const float* cosk, int N, long long* fx, int* inexact) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const float v = cosk[k] * 8589934592.f;  // 2^33: exact scaling
+    const long long t = __float2ll_rn(v);
+    fx[k] = t;
+    if ((float)t != v) atomicExch(inexact, 1);
+}
+
 // ---- batched SIMT contraction ------------------------------------------------------
 constexpr int TM = 64, TN = 64, TK = 16, NT = 256;
 
@@ -65,6 +76,9 @@ struct GemmArgs {
     // epilogue
     float scale;
     int pz_layout;  // 1: outputs indexed (i = ky, j = kx); 2: (i = kz, j = ky*W + kx)
+    const long long* fx0;  // DctPlan::cosk_fx (null: the FP64 form)
+    const long long* fx1;
+    const long long* fx2;
     const float* cosk0;
     const float* cosk1;
     const float* cosk2;
@@ -159,10 +173,8 @@ __global__ void __launch_bounds__(NT) gemm_kernel(GemmArgs g) {
                     v = 0.f;
                 } else if constexpr (EPI == EPI_POISSON_REF) {
                     // FP32 cosines combined in FP64 (solve_poisson_in_cosine_domain.cu:48-53)
-                    double den = (g.D > 1 ? 6.0 : 4.0) - 2.0 * (double)g.cosk0[kx] -
-                                 2.0 * (double)g.cosk1[ky];
-                    if (g.D > 1) den -= 2.0 * (double)g.cosk2[kz];
-                    v = v / (float)den;
+                    v = v / poisson_den_ref(g.D > 1, g.fx0, g.fx1, g.fx2, g.cosk0, g.cosk1,
+                                            g.cosk2, kx, ky, kz);
                 } else {
                     float den = g.eig0[kx] + g.eig1[ky];
                     if (g.D > 1) den = den + g.eig2[kz];
@@ -261,6 +273,9 @@ void pass(const DctPlan* p, int axis, const float* Mat, const float* in, float* 
         g.sCb = 0;
         g.pz_layout = 2;
     }
+    g.fx0 = p->cosk_fx[0];
+    g.fx1 = p->cosk_fx[1];
+    g.fx2 = p->cosk_fx[2];
     if (aload == A_DIVERGENCE) {
         TGV_REQUIRE(axis == 0, "divergence fusion is on the x pass");
         launch_gemm<A_DIVERGENCE, EPI_NONE>(g, batches, st);
@@ -362,8 +377,10 @@ unsigned ew_grid(size_t n) {
 size_t dct_plan_bytes(int W, int H, int D) {
     size_t b = 0;
     const int N[3] = {W, H, D};
-    for (int a = 0; a < 3; ++a) b += 2 * a256((size_t)N[a] * N[a] * 4) + 2 * a256((size_t)N[a] * 4);
-    b += 2 * a256((size_t)W * H * D * 4);
+    for (int a = 0; a < 3; ++a)
+        b += 2 * a256((size_t)N[a] * N[a] * 4) + 2 * a256((size_t)N[a] * 4) +
+             a256((size_t)N[a] * 8);
+    b += 2 * a256((size_t)W * H * D * 4) + 256;
     return b;
 }
 
@@ -391,6 +408,8 @@ DctPlan* dct_plan_create(int W, int H, int D) {
         c += a256(n * 4);
         p->eig[a] = (float*)c;
         c += a256(n * 4);
+        p->cosk_fx[a] = (long long*)c;
+        c += a256(n * 8);
         std::vector<float> C(n * n), S(n * n), E(n);
         for (size_t k = 0; k < n; ++k) {
             for (size_t m = 0; m < n; ++m) {
@@ -416,13 +435,26 @@ DctPlan* dct_plan_create(int W, int H, int D) {
     p->tmp[0] = (float*)c;
     c += a256((size_t)W * H * D * 4);
     p->tmp[1] = (float*)c;
-    cudaError_t se = cudaDeviceSynchronize();
+    c += a256((size_t)W * H * D * 4);
+    int* inexact = (int*)c;
+    cudaError_t se = cudaMemset(inexact, 0, sizeof(int));
+    const bool small = W <= 256 && H <= 256 && D <= 256;
+    for (int a = 0; a < 3 && se == cudaSuccess && small; ++a) {
+        cosk_fx_kernel<<<ceil_div((size_t)N[a], 128), 128>>>(p->cosk[a], N[a], p->cosk_fx[a],
+                                                            inexact);
+        se = cudaGetLastError();
+    }
+    int h_inexact = 1;
+    if (se == cudaSuccess) se = cudaMemcpy(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost);
+    if (se == cudaSuccess) se = cudaDeviceSynchronize();
     if (se != cudaSuccess) {
         cudaFree(p->block);
         delete p;
         set_error(std::string("DCT plan setup: ") + cudaGetErrorString(se));
         throw Error{TGVDCT_ERR_CUDA};
     }
+    if (!small || h_inexact)  // the FP64 form of the reference eigenvalues
+        for (int a = 0; a < 3; ++a) p->cosk_fx[a] = nullptr;
     return p;
 }
 

@@ -71,6 +71,9 @@ struct TcArgs {
     const float* eig0;
     const float* eig1;
     const float* eig2;
+    const long long* fx0;  // DctPlan::cosk_fx (null: the FP64 form)
+    const long long* fx1;
+    const long long* fx2;
     int* err;
 };
 
@@ -405,10 +408,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) dct_tc_kernel(TcArgs g) {
                     if (kx == 0 && ky == 0 && kz == 0) {
                         x = 0.f;
                     } else if constexpr (EPI == TCE_POISSON_REF) {
-                        double den = (g.D > 1 ? 6.0 : 4.0) - 2.0 * (double)g.cosk0[kx] -
-                                     2.0 * (double)g.cosk1[ky];
-                        if (g.D > 1) den -= 2.0 * (double)g.cosk2[kz];
-                        x = x / (float)den;
+                        x = x / poisson_den_ref(g.D > 1, g.fx0, g.fx1, g.fx2, g.cosk0, g.cosk1,
+                                                g.cosk2, kx, ky, kz);
                     } else {
                         float den = g.eig0[kx] + g.eig1[ky];
                         if (g.D > 1) den = den + g.eig2[kz];
@@ -561,6 +562,9 @@ void pass_tc(DctPlan* p, int axis, bool inverse, const float* in, float* out, in
     g.eig1 = p->eig[1];
     g.eig2 = p->eig[2];
     g.err = p->dev_err;
+    g.fx0 = p->cosk_fx[0];
+    g.fx1 = p->cosk_fx[1];
+    g.fx2 = p->cosk_fx[2];
     const int dir = inverse ? 1 : 0;
     g.m_hi = p->bf_hi[dir][axis];
     g.m_lo = p->bf_lo[dir][axis];

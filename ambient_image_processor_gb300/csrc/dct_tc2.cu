@@ -4,23 +4,25 @@
 // the 128 lines of a CTA, n over the axis, k over the N output frequencies (or
 // samples), M is the N x N cosine matrix.  One CTA owns a 128 x N tile of D in TMEM
 // (128 lanes x N FP32 columns).  The K dimension (the axis) streams through a
-// 3-stage shared-memory pipeline; each stage holds a 64-byte slice of every row of
-// both operands:
+// shared-memory pipeline of 192 KB (3 stages for BF16x3, 6 for TF32); each stage
+// holds a 64-byte slice of every row of both operands:
 //
-//   producer (warp 5, one lane)   TMA: the FP32 input slab, 128 lines x KE samples,
+//   producer (warp 9, one lane)   TMA: the FP32 input slab, 128 lines x KE samples,
 //                                 straight from the volume (2-D or 3-D tensor map);
 //                                 bulk copy: the matching slice of M, which the plan
 //                                 stores once in the shared-memory image the MMA
 //                                 reads (BF16 hi and lo, or TF32).  Both complete on
 //                                 the stage's `full` mbarrier.
-//   converters (warps 0-3)        FP32 slab -> BF16 hi/lo (or TF32) in the canonical
+//   converters (warps 0-7)        FP32 slab -> BF16 hi/lo (or TF32) in the canonical
 //                                 K-major no-swizzle layout; arrive on `conv`.
-//   MMA issuer (warp 4, one lane) tcgen05.mma kind::f16 (three products, hi*hi +
+//   MMA issuer (warp 8, one lane) tcgen05.mma kind::f16 (three products, hi*hi +
 //                                 hi*lo + lo*hi) or kind::tf32, then tcgen05.commit
 //                                 to the stage's `empty` mbarrier, which frees the
 //                                 stage for the producer.
-//   epilogue (all 8 warps)        tcgen05.ld of the accumulator, scale or Poisson
-//                                 division, coalesced stores.
+//   epilogue (warps 10-13)        tcgen05.ld of the accumulator, scale or Poisson
+//                                 division, coalesced stores, while the next tile's
+//                                 MMAs fill the other TMEM accumulator (persistent
+//                                 CTAs, one per SM, two 128 x N accumulators).
 //
 // Canonical layout of a stage's operand tile (rows r, byte cb of the 64-byte slice):
 // 8-row x 16-byte core matrices, K-adjacent ones 128 bytes apart (LBO) and 8-row groups
@@ -44,8 +46,10 @@ namespace tgvdct {
 namespace {
 
 constexpr int P_M = 128;          // lines per CTA (MMA M)
-constexpr int P_THREADS = 256;    // 8 warps
-constexpr int P_STAGES = 3;
+constexpr int P_THREADS = 448;    // 14 warps: 8 converters, MMA, producer, 4 epilogue
+constexpr int P_CONV = 256;       // converter threads (warps 0-7)
+constexpr int P_MMA_WARP = 8, P_PROD_WARP = 9;  // epilogue: warps 10-13
+constexpr int P_STAGES_MAX = 6;
 constexpr int P_RB = 64;          // bytes per row per stage (K slice)
 constexpr int P_NMAX = 256;
 constexpr uint64_t P_WAIT_NS = 200000000ull;  // 200 ms: a stage normally lands in microseconds
@@ -64,6 +68,7 @@ struct PGeo {
     static constexpr int OFF_B = RAW;
     static constexpr int OFF_A = OFF_B + NB * BTILE;
     static constexpr int STAGE = OFF_A + NB * ATILE;         // 64 KB (BF16x3) / 32 KB (TF32)
+    static constexpr int NS = MODE == PM_BF16X3 ? 3 : 6;     // stages in 192 KB
 };
 
 struct PArgs {
@@ -72,6 +77,7 @@ struct PArgs {
     const uint8_t* bimg;  // the matrix in stage images: nchunks x NB x (NP rows x 64 B)
     int NA, NP, nchunks;
     long long L;          // lines per batch
+    int batches;
     int W, H, D;
     // output addressing: out[batch * SB + line * SL + k * sn]
     long long SL, SB, sn;
@@ -83,6 +89,9 @@ struct PArgs {
     const float* eig0;
     const float* eig1;
     const float* eig2;
+    const long long* fx0;  // DctPlan::cosk_fx (null: the FP64 form)
+    const long long* fx1;
+    const long long* fx2;
     int* err;
 };
 
@@ -251,34 +260,44 @@ __device__ __forceinline__ void convert_group(const float* v, uint8_t* ahi, uint
     }
 }
 
+// Persistent: every CTA loops over the (line tile, batch) tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; the accumulator alternates between two TMEM buffers so
+// that the epilogue warps drain tile i while the MMAs of tile i + 1 run.
 template <int MODE, int AXIS, int EPI>
 __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_constant__ PArgs g) {
     using G = PGeo<MODE>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ uint64_t full[P_STAGES], conv[P_STAGES], empty[P_STAGES];
+    constexpr int P_STAGES = G::NS;
+    __shared__ uint64_t full[P_STAGES_MAX], conv[P_STAGES_MAX], empty[P_STAGES_MAX];
+    __shared__ uint64_t acc_full[2], acc_empty[2];
     __shared__ uint32_t tmem_s;
     __shared__ int abort_s;
-    __shared__ int consumed_s, issued_s, committed_s;
+    __shared__ int consumed_s, issued_s, mma_chunks_s;
 
     if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)g.err : 0)) return;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long long line0 = (long long)blockIdx.x * P_M;
-    const int batch = blockIdx.y;
     const int nch = g.nchunks;
+    const long long ntl = (g.L + P_M - 1) / P_M;            // line tiles per batch
+    const long long ntiles = ntl * g.batches;
     const uint32_t bchunk = (uint32_t)(G::NB * g.NP * P_RB);  // matrix bytes per stage
-    uint32_t ncols = 32;
-    while (ncols < (uint32_t)g.NP) ncols <<= 1;
+    uint32_t acols = 32;                                       // accumulator columns
+    while (acols < (uint32_t)g.NP) acols <<= 1;
+    const uint32_t ncols = 2 * acols;
     volatile int* abort = &abort_s;
 
     if (tid == 0) {
         for (int s = 0; s < P_STAGES; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&conv[s], 128);
+            mbar_init(&conv[s], P_CONV);
             mbar_init(&empty[s], 1);
         }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+        }
         abort_s = 0;
-        consumed_s = issued_s = committed_s = 0;
+        consumed_s = issued_s = mma_chunks_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -293,159 +312,208 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
     tc_after();
     const uint32_t tmem = tmem_s;
 
-    if (warp == 5) {
+    if (warp == P_PROD_WARP) {
         // ---- producer
         if (lane == 0) {
-            int c = 0;
-            for (; c < nch; ++c) {
-                const int s = c % P_STAGES;
-                if (c >= P_STAGES &&
-                    !mwait(&empty[s], (uint32_t)((c / P_STAGES - 1) & 1), g.err, abort, true))
-                    break;
-                uint8_t* st = base + s * G::STAGE;
-                mbar_expect_tx(&full[s], (uint32_t)G::RAW + bchunk);
-                const int k0 = c * G::KE;
-                if constexpr (AXIS == PA_X) tma_2d(st, &g.in_map, k0, (int)line0, &full[s]);
-                else if constexpr (AXIS == PA_Y) tma_3d(st, &g.in_map, (int)line0, k0, batch, &full[s]);
-                else tma_2d(st, &g.in_map, (int)line0, k0, &full[s]);
-                bulk_copy(st + G::OFF_B, g.bimg + (size_t)c * bchunk, bchunk, &full[s]);
-            }
-            issued_s = c;
-        }
-    } else if (warp < 4) {
-        // ---- converters (128 threads)
-        int c = 0;
-        for (; c < nch; ++c) {
-            const int s = c % P_STAGES;
-            if (!mwait(&full[s], (uint32_t)((c / P_STAGES) & 1), g.err, abort, true)) break;
-            const uint8_t* st = base + s * G::STAGE;
-            const float* raw = (const float*)st;
-            uint8_t* ahi = base + s * G::STAGE + G::OFF_A;
-            uint8_t* alo = ahi + G::ATILE;
-            constexpr int GS = MODE == PM_BF16X3 ? 8 : 4;   // samples per 16-byte group
-            constexpr int NG = G::KE / GS;                  // groups per row: 4
-#pragma unroll
-            for (int i = 0; i < NG; ++i) {
-                const int u = tid + 128 * i;                // 512 units: (line, group)
-                float v[8];
-                if constexpr (AXIS == PA_X) {
-                    // slab [128 lines][KE]: lanes cover 8 lines x 4 groups (contiguous)
-                    const int j = u & 3, r = u >> 2;
-                    const float4* src = (const float4*)(raw + r * G::KE + j * GS);
-                    const float4 a = src[0];
-                    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-                    if constexpr (GS == 8) {
-                        const float4 b = src[1];
-                        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+            int gc = 0;
+            bool go = true;
+            for (long long t = blockIdx.x; t < ntiles && go; t += gridDim.x) {
+                const long long line0 = (t % ntl) * P_M;
+                const int batch = (int)(t / ntl);
+                for (int c = 0; c < nch; ++c, ++gc) {
+                    const int s = gc % P_STAGES;
+                    if (gc >= P_STAGES &&
+                        !mwait(&empty[s], (uint32_t)((gc / P_STAGES - 1) & 1), g.err, abort, true)) {
+                        go = false;
+                        break;
                     }
-                    convert_group<MODE>(v, ahi, alo, r, j);
-                } else {
-                    // slab [KE][128 lines]: lanes cover consecutive lines
-                    const int r = u & 127, j = u >> 7;
-#pragma unroll
-                    for (int t = 0; t < GS; ++t) v[t] = raw[(j * GS + t) * P_M + r];
-                    convert_group<MODE>(v, ahi, alo, r, j);
+                    uint8_t* st = base + s * G::STAGE;
+                    mbar_expect_tx(&full[s], (uint32_t)G::RAW + bchunk);
+                    const int k0 = c * G::KE;
+                    if constexpr (AXIS == PA_X) tma_2d(st, &g.in_map, k0, (int)line0, &full[s]);
+                    else if constexpr (AXIS == PA_Y)
+                        tma_3d(st, &g.in_map, (int)line0, k0, batch, &full[s]);
+                    else tma_2d(st, &g.in_map, (int)line0, k0, &full[s]);
+                    bulk_copy(st + G::OFF_B, g.bimg + (size_t)c * bchunk, bchunk, &full[s]);
                 }
             }
-            fence_proxy_async();
-            mbar_arrive(&conv[s]);
-            if (tid == 0) consumed_s = c + 1;
+            issued_s = gc;
         }
-    } else if (warp == 4) {
+    } else if (warp < P_CONV / 32) {
+        // ---- converters (256 threads)
+        int gc = 0;
+        bool go = true;
+        for (long long t = blockIdx.x; t < ntiles && go; t += gridDim.x) {
+            for (int c = 0; c < nch; ++c, ++gc) {
+                const int s = gc % P_STAGES;
+                if (!mwait(&full[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true)) {
+                    go = false;
+                    break;
+                }
+                const float* raw = (const float*)(base + s * G::STAGE);
+                uint8_t* ahi = base + s * G::STAGE + G::OFF_A;
+                uint8_t* alo = ahi + G::ATILE;
+                constexpr int GS = MODE == PM_BF16X3 ? 8 : 4;   // samples per 16-byte group
+                constexpr int NU = P_M * (G::KE / GS) / P_CONV;  // units per thread: 2
+#pragma unroll
+                for (int i = 0; i < NU; ++i) {
+                    const int u = tid + P_CONV * i;             // 512 units: (line, group)
+                    float v[8];
+                    if constexpr (AXIS == PA_X) {
+                        // slab [128 lines][KE]: lanes cover 8 lines x 4 groups (contiguous)
+                        const int j = u & 3, r = u >> 2;
+                        const float4* src = (const float4*)(raw + r * G::KE + j * GS);
+                        const float4 a = src[0];
+                        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+                        if constexpr (GS == 8) {
+                            const float4 b = src[1];
+                            v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+                        }
+                        convert_group<MODE>(v, ahi, alo, r, j);
+                    } else {
+                        // slab [KE][128 lines]: lanes cover consecutive lines
+                        const int r = u & 127, j = u >> 7;
+#pragma unroll
+                        for (int q = 0; q < GS; ++q) v[q] = raw[(j * GS + q) * P_M + r];
+                        convert_group<MODE>(v, ahi, alo, r, j);
+                    }
+                }
+                fence_proxy_async();
+                mbar_arrive(&conv[s]);
+                if (tid == 0) consumed_s = gc + 1;
+            }
+        }
+    } else if (warp == P_MMA_WARP) {
         // ---- MMA issuer
         if (lane == 0) {
             const uint32_t id = idesc<MODE>(g.NP);
-            int c = 0;
-            for (; c < nch; ++c) {
-                const int s = c % P_STAGES;
-                if (!mwait(&conv[s], (uint32_t)((c / P_STAGES) & 1), g.err, abort, true)) break;
+            int gc = 0, ti = 0;
+            bool go = true;
+            for (long long t = blockIdx.x; t < ntiles && go; t += gridDim.x, ++ti) {
+                const int b = ti & 1;
+                // the epilogue of tile ti - 2 has read accumulator b
+                if (ti >= 2 &&
+                    !mwait(&acc_empty[b], (uint32_t)((ti / 2 - 1) & 1), g.err, abort, true))
+                    break;
                 tc_after();
-                const uint32_t st = su32(base + s * G::STAGE);
-                const uint32_t bhi = st + G::OFF_B, blo = bhi + (uint32_t)(g.NP * P_RB);
-                const uint32_t ahi = st + G::OFF_A, alo = ahi + G::ATILE;
-#pragma unroll
-                for (int kk = 0; kk < 2; ++kk) {  // 32 bytes of K per MMA
-                    const uint32_t ko = kk * 256;   // two core matrices along K
-                    const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
-                    mma<MODE>(tmem, sdesc(ahi + ko), sdesc(bhi + ko), id, acc);
-                    if constexpr (MODE == PM_BF16X3) {
-                        mma<MODE>(tmem, sdesc(ahi + ko), sdesc(blo + ko), id, 1u);
-                        mma<MODE>(tmem, sdesc(alo + ko), sdesc(bhi + ko), id, 1u);
+                const uint32_t acc_t = tmem + (uint32_t)b * acols;
+                for (int c = 0; c < nch; ++c, ++gc) {
+                    const int s = gc % P_STAGES;
+                    if (!mwait(&conv[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true)) {
+                        go = false;
+                        break;
                     }
+                    tc_after();
+                    const uint32_t st = su32(base + s * G::STAGE);
+                    const uint32_t bhi = st + G::OFF_B, blo = bhi + (uint32_t)(g.NP * P_RB);
+                    const uint32_t ahi = st + G::OFF_A, alo = ahi + G::ATILE;
+#pragma unroll
+                    for (int kk = 0; kk < 2; ++kk) {  // 32 bytes of K per MMA
+                        const uint32_t ko = kk * 256;   // two core matrices along K
+                        const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                        mma<MODE>(acc_t, sdesc(ahi + ko), sdesc(bhi + ko), id, acc);
+                        if constexpr (MODE == PM_BF16X3) {
+                            mma<MODE>(acc_t, sdesc(ahi + ko), sdesc(blo + ko), id, 1u);
+                            mma<MODE>(acc_t, sdesc(alo + ko), sdesc(bhi + ko), id, 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                    mma_chunks_s = gc + 1;
                 }
-                mma_commit(&empty[s]);
+                if (go) mma_commit(&acc_full[b]);
             }
-            committed_s = c;
+        }
+    } else {
+        // ---- epilogue (warps 10-13: TMEM lane quarter q = warp % 4)
+        const int q = warp & 3;
+        int ti = 0;
+        for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++ti) {
+            const int b = ti & 1;
+            if (!mwait(&acc_full[b], (uint32_t)((ti / 2) & 1), g.err, abort, true)) break;
+            tc_after();
+            const long long line = (t % ntl) * P_M + q * 32 + lane;
+            const int batch = (int)(t / ntl);
+            float* out = g.out + (long long)batch * g.SB;
+            // Poisson division: the line fixes kx (and ky on the z pass); the column k is
+            // the remaining frequency.  Per line: the partial integer sum (reference
+            // eigenvalues) or the partial float sum (accurate eigenvalues, same order).
+            int kx = 0, ky = 0;
+            long long pref = 0;
+            float pacc = 0.f;
+            const long long* tk = g.pz_layout == 1 ? g.fx1 : g.fx2;  // table of column k
+            const float* ek = g.pz_layout == 1 ? g.eig1 : g.eig2;
+            if constexpr (EPI == PE_POISSON_REF || EPI == PE_POISSON_ACC) {
+                if (line < g.L) {
+                    if (g.pz_layout == 1) kx = (int)line;
+                    else { kx = (int)(line % g.W); ky = (int)(line / g.W); }
+                    if (g.fx0) {
+                        pref = (g.D > 1 ? 6ll : 4ll) * 4294967296ll - g.fx0[kx];
+                        if (g.pz_layout == 2) pref -= g.fx1[ky];
+                    }
+                    pacc = g.pz_layout == 2 ? g.eig0[kx] + g.eig1[ky] : g.eig0[kx];
+                }
+            }
+            for (int c0 = 0; c0 < g.NP; c0 += 8) {
+                float v[8];
+                tmem_ld8(tmem + (uint32_t)b * acols + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+                if (line >= g.L) continue;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int k = c0 + e;
+                    float x = v[e];
+                    if constexpr (EPI == PE_SCALE) {
+                        x = x * g.scale;
+                    } else if constexpr (EPI == PE_POISSON_REF || EPI == PE_POISSON_ACC) {
+                        x = x * 8.f;
+                        if (kx == 0 && ky == 0 && k == 0) {
+                            x = 0.f;
+                        } else if (k < g.NA) {
+                            if constexpr (EPI == PE_POISSON_REF) {
+                                if (g.fx0) {
+                                    x = x / fixed32_to_float(pref - tk[k]);
+                                } else {
+                                    const int yy = g.pz_layout == 1 ? k : ky;
+                                    x = x / poisson_den_ref(g.D > 1, nullptr, nullptr, nullptr,
+                                                            g.cosk0, g.cosk1, g.cosk2, kx, yy, k);
+                                }
+                            } else {
+                                x = x / (pacc + ek[k]);
+                            }
+                        }
+                    }
+                    v[e] = x;
+                }
+                if constexpr (AXIS == PA_X) {
+                    // out[line][k]: 8 consecutive values of one line
+                    float* dst = out + line * g.SL + c0;
+                    if (c0 + 8 <= g.NA) {
+                        *(float4*)dst = make_float4(v[0], v[1], v[2], v[3]);
+                        *(float4*)(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
+                    } else {
+                        for (int e = 0; e < 8 && c0 + e < g.NA; ++e) dst[e] = v[e];
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (c0 + e < g.NA) out[line * g.SL + (long long)(c0 + e) * g.sn] = v[e];
+                }
+            }
+            tc_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
     }
     __syncthreads();
-    // ---- completion: every MMA committed has finished, every copy issued has landed
-    const int committed = committed_s, issued = issued_s, consumed = consumed_s;
-    bool ok = !abort_s && committed == nch;
-    if (tid == 0 && committed > 0) {
-        const int c = committed - 1;
-        if (!mwait(&empty[c % P_STAGES], (uint32_t)((c / P_STAGES) & 1), g.err, abort, false))
-            ok = false;
-    }
-    if (tid == 32) {  // copies issued but never consumed (error exit only)
-        for (int c = consumed; c < issued; ++c)
-            mwait(&full[c % P_STAGES], (uint32_t)((c / P_STAGES) & 1), g.err, abort, false);
-    }
-    ok = __syncthreads_and(ok && !abort_s);
-    tc_after();
-
-    if (ok) {
-        // ---- epilogue: warp w reads TMEM lanes 32*(w%4).., columns of half w/4
-        const int q = warp & 3, half = warp >> 2;
-        const long long line = line0 + q * 32 + lane;
-        const int cols_half = g.NP / 2;
-        float* out = g.out + (long long)batch * g.SB;
-        for (int c0 = half * cols_half; c0 < (half + 1) * cols_half; c0 += 8) {
-            float v[8];
-            tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-            if (line >= g.L) continue;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int k = c0 + t;
-                float x = v[t];
-                if constexpr (EPI == PE_SCALE) {
-                    x = x * g.scale;
-                } else if constexpr (EPI == PE_POISSON_REF || EPI == PE_POISSON_ACC) {
-                    int kx, ky, kz;
-                    if (g.pz_layout == 1) { kx = (int)line; ky = k; kz = 0; }
-                    else { kx = (int)(line % g.W); ky = (int)(line / g.W); kz = k; }
-                    x = x * 8.f;
-                    if (kx == 0 && ky == 0 && kz == 0) {
-                        x = 0.f;
-                    } else if (k < g.NA) {
-                        if constexpr (EPI == PE_POISSON_REF) {
-                            double den = (g.D > 1 ? 6.0 : 4.0) - 2.0 * (double)g.cosk0[kx] -
-                                         2.0 * (double)g.cosk1[ky];
-                            if (g.D > 1) den -= 2.0 * (double)g.cosk2[kz];
-                            x = x / (float)den;
-                        } else {
-                            float den = g.eig0[kx] + g.eig1[ky];
-                            if (g.D > 1) den = den + g.eig2[kz];
-                            x = x / den;
-                        }
-                    }
-                }
-                v[t] = x;
-            }
-            if constexpr (AXIS == PA_X) {
-                // out[line][k]: 8 consecutive values of one line
-                float* dst = out + line * g.SL + c0;
-                if (c0 + 8 <= g.NA) {
-                    *(float4*)dst = make_float4(v[0], v[1], v[2], v[3]);
-                    *(float4*)(dst + 4) = make_float4(v[4], v[5], v[6], v[7]);
-                } else {
-                    for (int t = 0; t < 8 && c0 + t < g.NA; ++t) dst[t] = v[t];
-                }
-            } else {
-#pragma unroll
-                for (int t = 0; t < 8; ++t)
-                    if (c0 + t < g.NA) out[line * g.SL + (long long)(c0 + t) * g.sn] = v[t];
-            }
+    // ---- error exit: let issued copies land and issued MMAs finish before TMEM and
+    // shared memory go away (bounded waits; nothing is pending on the normal path)
+    if (abort_s) {
+        if (tid == 0 && mma_chunks_s > 0) {
+            const int c = mma_chunks_s - 1;
+            mwait(&empty[c % P_STAGES], (uint32_t)((c / P_STAGES) & 1), g.err, abort, false);
+        }
+        if (tid == 32) {
+            for (int c = consumed_s; c < issued_s; ++c)
+                mwait(&full[c % P_STAGES], (uint32_t)((c / P_STAGES) & 1), g.err, abort, false);
         }
     }
     tc_before();
@@ -456,9 +524,11 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
                      : "memory");
 }
 
+// Both modes ask for the BF16x3 footprint (over half of an SM's shared memory), so
+// that no SM holds two of these CTAs: each allocates all 512 TMEM columns.
 template <int MODE>
 constexpr size_t pipe_smem() {
-    return (size_t)P_STAGES * PGeo<MODE>::STAGE + 1024;
+    return (size_t)PGeo<PM_BF16X3>::NS * PGeo<PM_BF16X3>::STAGE + 1024;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
@@ -501,8 +571,14 @@ void launch_axis(const PArgs& a, int batches, int epi, cudaStream_t st) {
         TGV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured[epi & 3] = true;
     }
-    const dim3 grid((unsigned)ceil_div((size_t)a.L, P_M), (unsigned)batches);
-    k<<<grid, P_THREADS, smem, st>>>(a);
+    int dev = 0, sms = 0;
+    TGV_CUDA(cudaGetDevice(&dev));
+    TGV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PArgs b = a;
+    b.batches = batches;
+    const long long tiles = (long long)ceil_div((size_t)a.L, P_M) * batches;
+    const unsigned grid = (unsigned)(tiles < sms ? tiles : sms);  // one persistent CTA per SM
+    k<<<grid, P_THREADS, smem, st>>>(b);
     TGV_CHECK_LAUNCH();
 }
 
@@ -625,6 +701,9 @@ bool pass_pipe(DctPlan* p, int axis, bool inverse, const float* in, float* out, 
     a.eig1 = p->eig[1];
     a.eig2 = p->eig[2];
     a.err = p->dev_err;
+    a.fx0 = p->cosk_fx[0];
+    a.fx1 = p->cosk_fx[1];
+    a.fx2 = p->cosk_fx[2];
     const int dir = inverse ? 1 : 0;
     a.bimg = (const uint8_t*)p->pipe_img[mode][dir][axis];
     a.nchunks = p->pipe_chunks[mode][dir][axis];

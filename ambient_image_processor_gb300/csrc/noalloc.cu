@@ -91,6 +91,12 @@ extern "C" tgvdct_status tgvdct_integrate_poisson_noalloc_dev(
         TGV_REQUIRE(poisson_eigen == TGVDCT_EIGEN_REFERENCE ||
                         poisson_eigen == TGVDCT_EIGEN_ACCURATE,
                     "unknown Poisson eigenvalue mode");
+        // the tensor-core modes keep their matrices in allocations of a context's plan
+        if (dct_mode != TGVDCT_DCT_FP32) {
+            set_error("tgvdct_integrate_poisson_noalloc_dev: only TGVDCT_DCT_FP32 runs without "
+                      "allocating (the tensor-core modes need a context's plan)");
+            return TGVDCT_ERR_UNSUPPORTED;
+        }
         float* base = scratch_for_current_device();
         cudaStream_t s = (cudaStream_t)stream;
         DctPlan view;

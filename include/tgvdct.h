@@ -291,7 +291,8 @@ tgvdct_status tgvdct_check_device_error(tgvdct_context* ctx, void* stream);
    stream capture).  All calls share the one array: calls that overlap on the
    GPU (different streams, no ordering between them) race and corrupt each
    other's results, so order them, e.g. on one stream.  The caller passes v on
-   the device (v_z_dev may be NULL when depth == 1) and the output l_dev. */
+   the device (v_z_dev may be NULL when depth == 1) and the output l_dev.  Only
+   dct_mode TGVDCT_DCT_FP32 is available here (TGVDCT_ERR_UNSUPPORTED otherwise). */
 #define TGVDCT_NOALLOC_MAX_VOXELS (1u << 21)
 #define TGVDCT_NOALLOC_MAX_SIDE 256u
 tgvdct_status tgvdct_integrate_poisson_noalloc_dev(const float* v_x_dev, const float* v_y_dev,
