@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <memory>
 #include <string>
 
@@ -50,6 +51,17 @@ struct TgvStencilFields {
 };
 
 enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
+
+// cudaFuncAttributeMaxDynamicSharedMemorySize is per device: raise it for `kern` once
+// on every device that launches it (`done` holds one bit per device ordinal).
+inline void smem_attr_once(const void* kern, size_t smem, std::atomic<uint64_t>& done) {
+    int dev = 0;
+    TGV_CUDA(cudaGetDevice(&dev));
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    TGV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    done.fetch_or(bit, std::memory_order_release);
+}
 
 // Device state of one volume.  Fields are planar (structure of arrays), x fastest.
 // The two-pass kernels update set[0] in place.  The fused kernel reads set[cur]

@@ -429,11 +429,8 @@ template <int MODE, bool DIV, int EPI>
 void launch(const TcArgs& g, int batches, cudaStream_t st) {
     constexpr size_t smem = 2 * (size_t)stage_bytes<MODE>() + 1024;
     auto k = dct_tc_kernel<MODE, DIV, EPI>;
-    static bool configured = false;
-    if (!configured) {
-        TGV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    static std::atomic<uint64_t> configured{0};
+    smem_attr_once((const void*)k, smem, configured);
     const dim3 grid(ceil_div((size_t)g.L, TC_M), batches);
     k<<<grid, TC_THREADS, smem, st>>>(g);
     TGV_CHECK_LAUNCH();

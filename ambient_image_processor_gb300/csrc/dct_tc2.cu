@@ -566,11 +566,8 @@ void launch_axis(const PArgs& a, int batches, int epi, cudaStream_t st) {
     };
     auto k = pick();
     constexpr size_t smem = pipe_smem<MODE>();
-    static bool configured[4] = {false, false, false, false};
-    if (!configured[epi & 3]) {
-        TGV_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured[epi & 3] = true;
-    }
+    static std::atomic<uint64_t> configured[4] = {};
+    smem_attr_once((const void*)k, smem, configured[epi & 3]);
     int dev = 0, sms = 0;
     TGV_CUDA(cudaGetDevice(&dev));
     TGV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

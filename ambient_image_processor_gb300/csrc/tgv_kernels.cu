@@ -1204,11 +1204,8 @@ void launch_fused(const FusedArgs<typename Dual<PREC>::T>& a, int D, cudaStream_
     constexpr int TY = FUSED_TY;
     constexpr size_t smem = fused_smem_floats<TY, THREE>() * sizeof(float);
     auto kern = tgv_fused_kernel<PREC, THREE, DATA, TY>;
-    static bool configured = false;  // per template instance
-    if (!configured) {
-        TGV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    static std::atomic<uint64_t> configured{0};  // per template instance
+    smem_attr_once((const void*)kern, smem, configured);
     const dim3 grid(ceil_div(a.W, FX), ceil_div(a.H, TY), ceil_div(D, a.zchunk));
     kern<<<grid, fused_threads<TY>(), smem, st>>>(a);
     TGV_CHECK_LAUNCH();
@@ -1313,12 +1310,8 @@ void launch_tma(const tma::Args<typename Dual<PREC>::T>& a, cudaStream_t st) {
     auto kern = a.dom ? tgv_fused_tma_kernel<PREC, THREE, DATA, NS, true>
                       : tgv_fused_tma_kernel<PREC, THREE, DATA, NS, false>;
     const size_t smem = tma_smem_bytes<PREC>();
-    static bool configured[2] = {false, false};
-    bool& done = configured[a.dom ? 1 : 0];
-    if (!done) {
-        TGV_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        done = true;
-    }
+    static std::atomic<uint64_t> configured[2] = {};
+    smem_attr_once((const void*)kern, smem, configured[a.dom ? 1 : 0]);
     const dim3 grid(ceil_div(a.W, tma::TX), ceil_div(a.H, tma::TY), ceil_div(a.D, a.zchunk));
     kern<<<grid, tma::NTHREADS, smem, st>>>(a);
     TGV_CHECK_LAUNCH();

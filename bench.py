@@ -110,6 +110,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, dist, device):
+    """Time-like figure of the slowest rank (every rank calls; all receive the max).
+    dist is torch.distributed or None (one process)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, ms):
+    """Whole-job units per second: every replica processes units_per_rank in ms (the
+    slowest rank's time)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as fh:
@@ -317,12 +334,8 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     ctx.check_device_error(sh)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * V * iters / (ms * 1e-3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, dev)
+    value = replica_throughput(V * iters, world, ms)
     ctx.close()
 
     # ---- roofline of the iteration kernel, timed alone on its stream
@@ -353,7 +366,9 @@ def run_ours(args):
             if k > 0:
                 times.append(time.perf_counter() - t0)
         e2e_ms = 1e3 * float(np.median(times))
-    e2e_value = world * V * iters / (e2e_ms * 1e-3) if e2e_ms else None
+    if not args.no_e2e:
+        e2e_ms = max_over_ranks(e2e_ms, dist, dev)
+    e2e_value = replica_throughput(V * iters, world, e2e_ms) if e2e_ms else None
 
     line = None
     if rank == 0:
