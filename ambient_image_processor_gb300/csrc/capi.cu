@@ -32,6 +32,14 @@ struct tgvdct_context {
     // derived from it (voxels with mask >= 1 are iterated)
     float* domain_mask = nullptr;
     uint8_t* domain = nullptr;
+    // CUDA graph of kGraphChunk iterations (an even number, so the ping-pong parity
+    // of the state is unchanged after a replay), captured on a private stream and
+    // replayed on the caller's; rebuilt when the step or the state changes
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    TgvStep graph_step{};
+    const void* graph_domain = nullptr;
+    int graph_cur = -1, graph_zchunk = 0;
     // reverse mode: checkpoints of the last checkpointed forward run, the states of
     // one recomputed segment, and the adjoint state with its scratch fields
     void* ckpt_block = nullptr;
@@ -183,22 +191,91 @@ int deliver(tgvdct_context* c, tgvdct_iteration_callback cb, void* user, uint32_
     return cb(it, c->prm.iteration_count, dst[0], dst[1], dst[2], dst[3], user);
 }
 
+constexpr uint32_t kGraphChunk = 32;  // iterations per graph replay (even)
+
+bool same_step(const TgvStep& a, const TgvStep& b) {
+    return a.tau == b.tau && a.sigma == b.sigma && a.theta == b.theta && a.lambda == b.lambda &&
+           a.alpha0 == b.alpha0 && a.alpha1 == b.alpha1 && a.data_term == b.data_term;
+}
+
+// A graph of kGraphChunk iterations for the state's current parity and step, built
+// on first use (the first iteration of the loop has already run outside capture, so
+// every kernel attribute is set).  Null when capture is not possible.
+cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
+    if (c->graph && same_step(c->graph_step, k) && c->graph_domain == c->st.domain &&
+        c->graph_cur == c->st.cur && c->graph_zchunk == c->st.zchunk)
+        return c->graph;
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    if (!c->capture_stream &&
+        cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const int cur = c->st.cur;
+    for (uint32_t i = 0; i < kGraphChunk; ++i) tgv_iterate(c->st, k, c->capture_stream);
+    const cudaError_t e = cudaStreamEndCapture(c->capture_stream, &g);
+    TGV_REQUIRE(c->st.cur == cur, "a graph chunk must keep the state's parity");
+    if (e != cudaSuccess || !g) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        cudaGetLastError();
+        c->graph = nullptr;
+        return nullptr;
+    }
+    c->graph_step = k;
+    c->graph_domain = c->st.domain;
+    c->graph_cur = cur;
+    c->graph_zchunk = c->st.zchunk;
+    return c->graph;
+}
+
 // The iteration loop on the context's state (st.f already holds the input).
-// `on_iteration` decides what a callback sees; returns true if stopped.
+// `on_iteration` decides what a callback sees; returns true if stopped.  Stretches
+// of kGraphChunk iterations with no callback due run as one CUDA graph replay (the
+// small-volume loops are launch-bound otherwise).
 template <class OnIteration>
 bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration) {
     const TgvStep k = step_of(c->prm);
     tgv_state_init(c->st, s);
     const uint32_t n_it = c->prm.iteration_count, paint = c->prm.paint_iteration_interval;
+    const bool cb_on = have_cb && paint > 0;
     c->iterations_run = 0;
-    for (uint32_t it = 0; it < n_it; ++it) {
+    for (uint32_t it = 0; it < n_it;) {
+        // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384)
+        if (it > 0 && it + kGraphChunk <= n_it) {
+            bool due = false;
+            if (cb_on) {
+                const uint32_t next = (it % paint == 0) ? it : (it / paint + 1) * paint;
+                due = next < it + kGraphChunk;
+            }
+            if (!due) {
+                if (cudaGraphExec_t g = loop_graph(c, k)) {
+                    TGV_CUDA(cudaGraphLaunch(g, s));
+                    it += kGraphChunk;
+                    continue;
+                }
+            }
+        }
         tgv_iterate(c->st, k, s);
-        if (have_cb && paint > 0 && it > 0 && it % paint == 0) {  // tgv2_common.cu:381-384
+        if (cb_on && it > 0 && it % paint == 0) {
             if (on_iteration(it)) {
                 c->iterations_run = it + 1;
                 return true;
             }
         }
+        ++it;
     }
     c->iterations_run = n_it;
     return false;
@@ -253,6 +330,8 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->domain_mask) cudaFree(c->domain_mask);
     if (c->domain) cudaFree(c->domain);
     if (c->host_cb) cudaFreeHost(c->host_cb);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
     dct_plan_destroy(c->plan);
     delete c;
 }

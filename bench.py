@@ -244,6 +244,51 @@ def time_dct_poisson(pkg, torch, stream, n=256, reps=10):
     return res
 
 
+def time_other_configs(pkg, torch, stream):
+    """The remaining configurations of the reference's benchmark set, device-timed:
+    the 2-D 512x512 TGV2-L1 denoise (rectangles-and-ellipses phantom, noise 0.05,
+    1000 iterations, tau = sigma = 1/sqrt(12), the 2-D operators) and the whole 3-D
+    deshade of the 128^3 tissue phantom in the log domain (2000 iterations + DCT)."""
+    import math
+    from ambient_image_processor_gb300.phantoms import rectangles_ellipses_2d, tissue_phantom_3d
+    res = {}
+    f2 = torch.from_numpy(rectangles_ellipses_2d(512, 512, seed=1)).cuda()
+    prm = pkg.default_params(width=512, height=512, depth=1, iteration_count=1000,
+                             geometry=pkg.GEOMETRY_2D)
+    prm.tau = prm.sigma = 1.0 / math.sqrt(12.0)
+    u, vx, vy = (torch.empty_like(f2) for _ in range(3))
+    with pkg.Context(prm) as ctx:
+        run = lambda: ctx.run_dev(f2.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(),
+                                  None, stream=stream.cuda_stream)
+        run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    res["denoise2d_512x512_1000it"] = {"ms": ms, "pixel_iters_per_s": 512 * 512 * 1000 / (ms * 1e-3)}
+    f3 = torch.from_numpy(tissue_phantom_3d(128, 128, 128, seed=2)).cuda()
+    prm = pkg.default_params(width=128, height=128, depth=128, iteration_count=2000)
+    u, l, r = (torch.empty_like(f3) for _ in range(3))
+    with pkg.Context(prm) as ctx:
+        run = lambda: ctx.process_dev(f3.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
+                                      set_negative_values_to_zero=False, log_domain=True,
+                                      stream=stream.cuda_stream)
+        run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    res["deshade_128x128x128_2000it"] = {"ms": ms,
+                                          "voxel_iters_per_s": 128 ** 3 * 2000 / (ms * 1e-3)}
+    return res
+
+
 def time_adjoint(pkg, torch, stream, n=96, K=200, every=20):
     """Backward over forward time of the checkpointed reverse mode (96^3, K = 200)."""
     from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
@@ -384,6 +429,7 @@ def run_ours(args):
             extra["iteration_variants"] = var
             extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
             extra["adjoint"] = time_adjoint(pkg, torch, stream)
+            extra["other_configs"] = time_other_configs(pkg, torch, stream)
         cpu = None
         if not args.no_cpu_baseline:
             rate, cores, dt = cpu_reference(args, f_host, args.cpu_sample_iterations)
