@@ -84,6 +84,7 @@ _SIGS = {
     "tgvdct_divergence_launch": [_f32p, _f32p, _vp, _u32, _u32, _u32, _f32p],
     "tgvdct_divergence_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp],
     "tgvdct_set_domain_mask_dev": [_vp, _vp, _vp],
+    "tgvdct_poisson_integrate_adjoint_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_convergence_test": [ctypes.POINTER(Params), _f32p, _vp, _u32, _vp, _vp, _u32,
                                 ctypes.POINTER(_u32), _vp],
     "tgvdct_convergence_optimization": [ctypes.POINTER(Params), _f32p, _vp, _i32,
@@ -510,6 +511,10 @@ class Context:
     def poisson_integrate_dev(self, vx_ptr, vy_ptr, vz_ptr, l_ptr, stream=None):
         _check(lib().tgvdct_poisson_integrate_dev(self._ctx, vx_ptr, vy_ptr, vz_ptr, l_ptr,
                                                   stream), allow_stop=False)
+
+    def poisson_integrate_adjoint_dev(self, grad_l_ptr, gvx_ptr, gvy_ptr, gvz_ptr, stream=None):
+        _check(lib().tgvdct_poisson_integrate_adjoint_dev(self._ctx, grad_l_ptr, gvx_ptr, gvy_ptr,
+                                                          gvz_ptr, stream), allow_stop=False)
 
     def poisson_solve_dev(self, rhs_ptr, l_ptr, stream=None):
         _check(lib().tgvdct_poisson_solve_dev(self._ctx, rhs_ptr, l_ptr, stream),

@@ -986,6 +986,26 @@ tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* c, const float* rhs_dev, 
     });
 }
 
+tgvdct_status tgvdct_poisson_integrate_adjoint_dev(tgvdct_context* c, const float* grad_l_dev,
+                                                   float* grad_v_x_dev, float* grad_v_y_dev,
+                                                   float* grad_v_z_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(grad_l_dev && grad_v_x_dev && grad_v_y_dev &&
+                        (grad_v_z_dev || c->prm.depth == 1),
+                    "null device buffer");
+        const size_t n = voxels(c->prm);
+        DevBuf scratch(n);
+        cudaStream_t s = (cudaStream_t)stream;
+        poisson_integrate_adjoint(plan_of(c), grad_l_dev, scratch.p, grad_v_x_dev, grad_v_y_dev,
+                                  grad_v_z_dev, c->prm.dct_mode, c->prm.poisson_eigen, s);
+        if (grad_v_z_dev && c->prm.depth == 1)
+            TGV_CUDA(cudaMemsetAsync(grad_v_z_dev, 0, n * 4, s));
+        TGV_CUDA(cudaStreamSynchronize(s));  // the scratch is freed on return
+        return TGVDCT_OK;
+    });
+}
+
 tgvdct_status tgvdct_check_device_error(tgvdct_context* c, void* stream) {
     return guarded([&] {
         TGV_REQUIRE(c != nullptr, "null context");

@@ -233,6 +233,11 @@ __device__ __forceinline__ float poisson_den_ref(int three, const long long* t0,
 // to slot[0..1] (FP64 device memory).  sums: 8 zeroed doubles of scratch, left zeroed.
 void convergence_metrics(const float* l, const float* l_before, size_t n, double* sums,
                          double* slot, cudaStream_t st);
+// Adjoint of poisson_integrate: (gvx, gvy, gvz) = B^T M gl, M the DCT Poisson solve
+// (symmetric); scratch: V floats distinct from the plan's.  gvz unused when D == 1.
+void poisson_integrate_adjoint(DctPlan* p, const float* gl, float* scratch, float* gvx,
+                               float* gvy, float* gvz, int dct_mode, int eigen_mode,
+                               cudaStream_t st);
 void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,
                       bool clamp, bool add_back, float* r, cudaStream_t st,
                       bool mask_again = false);

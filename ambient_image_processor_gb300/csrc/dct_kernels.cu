@@ -307,6 +307,25 @@ __global__ void divergence_kernel(const float* __restrict__ vx, const float* __r
     }
 }
 
+// Transpose of the divergence above, per component: (B_a^T g)[j] = g[j + e_a] - g[j]
+// below the last slice of axis a and -g[j] on it (B_a w = w[i - e_a] - w[i], and -w[i]
+// on the first slice).  gz is written only when D > 1 (the 2-D divergence has no z term).
+__global__ void divergence_transpose_kernel(const float* __restrict__ g, int W, int H, int D,
+                                            float* __restrict__ gx, float* __restrict__ gy,
+                                            float* __restrict__ gz) {
+    const size_t n = (size_t)W * H * D, WH = (size_t)W * H;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(idx % W);
+        const int y = (int)((idx / W) % H);
+        const int z = (int)(idx / WH);
+        const float gi = g[idx];
+        gx[idx] = (x + 1 < W ? g[idx + 1] : 0.f) - gi;
+        gy[idx] = (y + 1 < H ? g[idx + W] : 0.f) - gi;
+        if (D > 1) gz[idx] = (z + 1 < D ? g[idx + WH] : 0.f) - gi;
+    }
+}
+
 __global__ void poisson_kernel(const float* __restrict__ in, float* __restrict__ out, int W, int H,
                                int D, const float* cx, const float* cy, const float* cz,
                                const float* ex, const float* ey, const float* ez, int accurate) {
@@ -578,6 +597,17 @@ void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float
         any_pass(p, 1, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 2, true, t0, l, EPI_SCALE, s, dct_mode, st);
     }
+}
+
+void poisson_integrate_adjoint(DctPlan* p, const float* gl, float* scratch, float* gvx,
+                               float* gvy, float* gvz, int dct_mode, int eigen_mode,
+                               cudaStream_t st) {
+    // l = M B v with M = S diag(1/eig) C symmetric (S = C^T W): the adjoint is B^T M g
+    poisson_solve(p, gl, scratch, dct_mode, eigen_mode, st);
+    const size_t n = (size_t)p->W * p->H * p->D;
+    divergence_transpose_kernel<<<ew_grid(n), 256, 0, st>>>(scratch, p->W, p->H, p->D, gvx, gvy,
+                                                             gvz);
+    TGV_CHECK_LAUNCH();
 }
 
 void deshade_epilogue(const float* u, float* l, const float* mask, size_t n, bool mask_shading,

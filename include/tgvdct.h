@@ -273,6 +273,15 @@ tgvdct_status tgvdct_poisson_integrate_dev(tgvdct_context* ctx, const float* v_x
    poisson_eigen; device buffers, stream-ordered. */
 tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* ctx, const float* rhs_dev, float* l_dev,
                                        void* stream);
+/* Adjoint of tgvdct_poisson_integrate_dev (no counterpart in the reference): given
+   dL/dl, writes dL/dv = B^T M dL/dl, where l = M (B_x v_x + B_y v_y + B_z v_z), B the
+   negated backward differences and M the DCT Poisson solve (a symmetric operator).
+   Uses the context's dct_mode and poisson_eigen; grad_v_z_dev may be NULL when
+   depth == 1 (the 2-D divergence has no z term; it is zeroed otherwise).  Synchronises
+   the stream. */
+tgvdct_status tgvdct_poisson_integrate_adjoint_dev(tgvdct_context* ctx, const float* grad_l_dev,
+                                                   float* grad_v_x_dev, float* grad_v_y_dev,
+                                                   float* grad_v_z_dev, void* stream);
 /* Reads and clears the device error flag of the tensor-core DCT passes of a context
    (set when one of their bounded waits timed out); synchronises the stream.
    Returns TGVDCT_ERR_CUDA if the flag was set. */

@@ -148,3 +148,54 @@ def test_adjoint_finite_differences_96cube(gpu_lib):
     hh = 1e-6
     fd = (loss64(f64 + hh * delta) - loss64(f64 - hh * delta)) / (2 * hh)
     assert abs(fd - float(np.sum(gf * delta))) <= 1e-4 * abs(fd), (fd, np.sum(gf * delta))
+
+
+def test_poisson_integration_adjoint_identity(gpu_lib):
+    """<g, M B v> = <B^T M g, v> for the integration and its adjoint."""
+    import torch
+    pkg_ctx = pkg.Context(pkg.default_params(width=32, height=24, depth=16))
+    rng = np.random.default_rng(7)
+    v = [torch.from_numpy(rng.standard_normal((16, 24, 32)).astype(np.float32)).cuda()
+         for _ in range(3)]
+    g = torch.from_numpy(rng.standard_normal((16, 24, 32)).astype(np.float32)).cuda()
+    l = torch.empty_like(g)
+    gv = [torch.empty_like(g) for _ in range(3)]
+    pkg_ctx.poisson_integrate_dev(v[0].data_ptr(), v[1].data_ptr(), v[2].data_ptr(), l.data_ptr())
+    pkg_ctx.poisson_integrate_adjoint_dev(g.data_ptr(), gv[0].data_ptr(), gv[1].data_ptr(),
+                                          gv[2].data_ptr())
+    torch.cuda.synchronize()
+    lhs = float((g.double() * l.double()).sum())
+    rhs = float(sum((a.double() * b.double()).sum() for a, b in zip(gv, v)))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), 1.0)
+    pkg_ctx.close()
+
+
+def test_deshade_gradient_through_the_shading_field(gpu_lib):
+    """Loss on u and l of tgv_deshade; its derivative along a random direction of f
+    against the FP64 forward (TGV loop + Poisson-DCT integration) at h = 1e-6."""
+    import torch
+    from ambient_image_processor_gb300.autograd import tgv_deshade
+
+    shape = (8, 12, 16)
+    noisy, clean, _ = tissue_phantom_3d(*shape, bias=True, noise=0.05, rician=False, seed=5,
+                                        return_parts=True)
+    f = np.log(np.maximum(noisy, 0.05)).astype(np.float64)
+    rng = np.random.default_rng(8)
+    gu = rng.standard_normal(shape)
+    gl = rng.standard_normal(shape)
+    K, a0, a1, lam = 40, 2.0, 1.0, 1.0
+    ft = _tensors(f)[0].requires_grad_(True)
+    u, v, l = tgv_deshade(ft, a0, a1, lam, K, 10, pkg.DATA_L2)
+    loss = (u * _tensors(gu)[0]).sum() + (l * _tensors(gl)[0]).sum()
+    loss.backward()
+    grad = ft.grad.cpu().numpy().astype(np.float64)
+
+    def loss64(fa):
+        uu, vx, vy, vz = oracle.tgv2_deshade(fa, lam, a0, a1, K, data_term="l2", dtype=np.float64)
+        ll = oracle.integrate_poisson_dct(vx, vy, vz)
+        return float(np.sum(uu * gu) + np.sum(ll * gl))
+
+    delta = rng.choice([-1.0, 1.0], size=shape)
+    h = 1e-6
+    fd = (loss64(f + h * delta) - loss64(f - h * delta)) / (2 * h)
+    assert abs(fd - float(np.sum(grad * delta))) <= 1e-4 * abs(fd), (fd, np.sum(grad * delta))
