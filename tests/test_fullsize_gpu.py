@@ -1,0 +1,106 @@
+"""Size-independent properties at the benchmark's full sizes and beyond, where the
+oracle would take too long: kernel agreement, the Poisson identity, the DCT round
+trip, and the callback / stop contract on a large volume."""
+import numpy as np
+import pytest
+
+import ambient_image_processor_gb300 as pkg
+from ambient_image_processor_gb300.phantoms import cosine_modes_rhs, tissue_phantom_3d
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(f, kernel, iterations, precision=pkg.STATE_FP32):
+    import torch
+    d, h, w = f.shape
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iterations,
+                             iteration_kernel=kernel, state_precision=precision)
+    u, vx, vy, vz = (torch.empty_like(f) for _ in range(4))
+    with pkg.Context(prm) as ctx:
+        ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr())
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+    return u, vx, vy, vz
+
+
+@pytest.mark.parametrize("shape,iterations", [((192, 256, 256), 40), ((256, 512, 512), 8)])
+def test_fused_equals_two_pass_at_full_size(gpu_lib, shape, iterations):
+    """The benchmark volume, and a 512x512x256 volume (67 M voxels, 8.3 GB of state):
+    the TMA-pipelined fused kernel and the two-pass kernels give identical bits."""
+    import torch
+    if shape[0] <= 192:
+        f = torch.from_numpy(np.log(tissue_phantom_3d(*shape, seed=2))).cuda()
+    else:  # a seeded random field: any input exercises the kernels' indexing
+        g = torch.Generator(device="cuda").manual_seed(12)
+        f = torch.randn(shape, generator=g, device="cuda", dtype=torch.float32)
+    a = _run(f, pkg.KERNEL_FUSED, iterations)
+    b = _run(f, pkg.KERNEL_TWO_PASS, iterations)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+
+
+def test_poisson_identity_at_256_cubed(gpu_lib):
+    """l = solve(rhs) at 256^3 (the DCT-alone configuration): FP32 satisfies
+    -Lap_N l = rhs - mean(rhs) (the Laplacian multiplies the rounding of l's
+    high-frequency part by up to 12 / lambda_min, hence 1e-3) and mean(l) = 0; the
+    tensor-core modes match the FP32 solution within their precision."""
+    import torch
+    n = 256
+    rhs = cosine_modes_rhs(n, n, n, seed=3)
+    rt = torch.from_numpy(rhs).cuda()
+    sols = {}
+    for mode in (pkg.DCT_FP32, pkg.DCT_BF16X3, pkg.DCT_TF32):
+        prm = pkg.default_params(width=n, height=n, depth=n, dct_mode=mode,
+                                 poisson_eigen=pkg.EIGEN_ACCURATE)
+        out = torch.empty_like(rt)
+        with pkg.Context(prm) as ctx:
+            ctx.poisson_solve_dev(rt.data_ptr(), out.data_ptr())
+            torch.cuda.synchronize()
+            ctx.check_device_error()
+        sols[mode] = out.double()
+    l = sols[pkg.DCT_FP32]
+    lap = torch.zeros_like(l)
+    for axis in range(3):  # Neumann 7-point Laplacian: sum of second differences
+        d = torch.diff(l, dim=axis)
+        lap_axis = torch.zeros_like(l)
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[axis] = slice(0, -1)
+        hi[axis] = slice(1, None)
+        lap_axis[tuple(lo)] += d
+        lap_axis[tuple(hi)] -= d
+        lap += lap_axis
+    target = rt.double() - rt.double().mean()
+    assert rel_l2((-lap).cpu().numpy(), target.cpu().numpy()) < 1e-3
+    for mode, tol in ((pkg.DCT_FP32, 0), (pkg.DCT_BF16X3, 3e-5), (pkg.DCT_TF32, 5e-3)):
+        x = sols[mode]
+        assert abs(float(x.mean())) < 1e-6 * float(x.abs().max())
+        if tol:
+            assert rel_l2(x.cpu().numpy(), l.cpu().numpy()) < tol, mode
+
+
+def test_dct_round_trip_at_full_size(gpu_lib):
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((192, 256, 256)).astype(np.float32)
+    for mode, tol in ((pkg.DCT_FP32, 1e-6), (pkg.DCT_BF16X3, 2e-5), (pkg.DCT_TF32, 5e-3)):
+        y = pkg.inverse_cosine_transform_kernel_launch(
+            pkg.cosine_transform_kernel_launch(x, mode), mode)
+        assert rel_l2(y, x) < tol, mode
+
+
+def test_callback_stop_on_a_large_volume(gpu_lib):
+    """A callback returning true stops the loop after that iteration; the outputs are
+    the state then (the reference's `return true`)."""
+    f = tissue_phantom_3d(64, 128, 128, seed=5, n_ellipsoids=8)
+    calls = []
+
+    def cb(i, count, u, vx, vy, vz):
+        calls.append(i)
+        return i >= 60
+
+    u_stop, *_ = pkg.tgv2_l1_deshade_launch(f, 1.0, 500, paint_iteration_interval=20,
+                                            iteration_finished_callback=cb)
+    assert calls == [20, 40, 60]
+    u61, *_ = pkg.tgv2_l1_deshade_launch(f, 1.0, 61)
+    assert np.array_equal(u_stop, u61)
