@@ -16,8 +16,11 @@
 //       out: a(p) = J_P^T a(p'),  a(q) = J_Q^T a(q')
 //   R3  out: a(ubar) = sigma F^T a(p),  a(vbar) = -sigma a(p) + sigma E^T a(q)
 // with (F_a^T g)[j] = g[j-e] (j_a >= 1) - g[j] (j_a < N-1) and
-// (B_a^T g)[j] = g[j+e] (j_a < N-1) - g[j].  The FP64 restatement of the same
-// algebra is the checker's reference gradient (central differences pin it).
+// (B_a^T g)[j] = g[j+e] (j_a < N-1) - g[j].  R3 of iteration k and R1 of iteration
+// k-1 are pointwise in a(ubar), a(vbar), so inside a segment they run as one kernel
+// (adjoint_r3r1) and those four fields never reach memory: per voxel and iteration
+// the adjoint moves 63 fields (252 bytes).  An FP64 restatement of the same algebra
+// in the oracle gives the reference gradient (central differences pin it).
 #include "common.cuh"
 
 namespace tgvdct {
@@ -54,52 +57,106 @@ __device__ __forceinline__ void block_add(double* dst, float v) {
     __syncthreads();
 }
 
+// R1 at voxel i, with a(ubar) and a(vbar) of S_{k+1} given: returns the d/dlambda term.
+__device__ __forceinline__ float r1_at(const AdjArgs& a, int x, int y, int z, size_t i,
+                                       float aub, const float* avb) {
+    const size_t W = a.W, WH = a.WH;
+    float glam = 0.f;
+    // u~ exactly as the forward primal pass computed it
+    const float pxi = a.S1.p[0][i], pyi = a.S1.p[1][i], pzi = a.S1.p[2][i];
+    const float bx = (x > 0 ? a.S1.p[0][i - 1] : 0.f) - pxi;
+    const float by = (y > 0 ? a.S1.p[1][i - W] : 0.f) - pyi;
+    float div = bx + by;
+    const float bz = (z > 0 ? a.S1.p[2][i - WH] : 0.f) - pzi;
+    if (!a.skip_bz) div = div + bz;
+    const float uo = a.S.u[i], fi = a.f[i];
+    const float ut = uo - a.tau * div;
+    const float ua = a.A.u[i] + (1.f + a.theta) * aub;
+    float uta, gf = 0.f;
+    if (a.data_term == TGVDCT_DATA_L1) {
+        const float dd = ut - fi;
+        if (dd > a.tau_lambda) {
+            uta = ua;
+            glam = -a.tau * ua;
+        } else if (dd < -a.tau_lambda) {
+            uta = ua;
+            glam = a.tau * ua;
+        } else {
+            uta = 0.f;
+            gf = ua;
+        }
+    } else {
+        const float den = 1.f + a.tau_lambda;
+        uta = ua / den;
+        gf = a.tau_lambda * ua / den;
+        glam = ua * a.tau * (fi - ut) / (den * den);
+    }
+    a.A.u[i] = -a.theta * aub + uta;
+    a.uta[i] = uta;
+    if (gf != 0.f) a.grad_f[i] += gf;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float va = a.A.v[c][i] + (1.f + a.theta) * avb[c];
+        a.va[c][i] = va;
+        a.A.v[c][i] = va - a.theta * avb[c];
+    }
+    return glam;
+}
+
+// R3 at voxel i: a(ubar) and a(vbar) of S_k from a(p), a(q) (after R2).
+__device__ __forceinline__ void r3_at(const AdjArgs& a, int x, int y, int z, size_t i,
+                                      float& aub, float* avb) {
+    const size_t W = a.W, WH = a.WH;
+    const bool xl = x + 1 < a.W, yl = y + 1 < a.H, zl = z + 1 < a.D;
+    const bool xf = x > 0, yf = y > 0, zf = z > 0;
+    // a(ubar) = sigma sum_c F_c^T a(p)_c
+    const float* P0 = a.A.p[0];
+    const float* P1 = a.A.p[1];
+    const float* P2 = a.A.p[2];
+    const float p0 = P0[i], p1 = P1[i], p2 = P2[i];
+    const float ftx = (xf ? P0[i - 1] : 0.f) - (xl ? p0 : 0.f);
+    const float fty = (yf ? P1[i - W] : 0.f) - (yl ? p1 : 0.f);
+    const float ftz = (zf ? P2[i - WH] : 0.f) - (zl ? p2 : 0.f);
+    aub = a.sigma * ((ftx + fty) + ftz);
+    // a(vbar)_c = -sigma a(p)_c + sigma sum_a w B_a^T a(q)_{c a}
+    auto bt = [&](const float* g, int axis) {
+        const float g0 = g[i];
+        if (axis == 0) return (xl ? g[i + 1] : 0.f) - g0;
+        if (axis == 1) return (yl ? g[i + W] : 0.f) - g0;
+        return (zl ? g[i + WH] : 0.f) - g0;
+    };
+    const float* const* Q = a.A.q;  // xx yy zz xy xz yz
+    const float ex = bt(Q[0], 0) + 0.5f * bt(Q[3], 1) + 0.5f * bt(Q[4], 2);
+    const float ey = 0.5f * bt(Q[3], 0) + bt(Q[1], 1) + 0.5f * bt(Q[5], 2);
+    const float ez = 0.5f * bt(Q[4], 0) + 0.5f * bt(Q[5], 1) + bt(Q[2], 2);
+    avb[0] = -a.sigma * p0 + a.sigma * ex;
+    avb[1] = -a.sigma * p1 + a.sigma * ey;
+    avb[2] = -a.sigma * p2 + a.sigma * ez;
+}
+
 __global__ void __launch_bounds__(BX* BY) adjoint_r1(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z = blockIdx.z;
     float glam = 0.f;
     if (x < a.W && y < a.H) {
-        const size_t W = a.W, WH = a.WH, i = ((size_t)z * a.H + y) * W + x;
-        // u~ exactly as the forward primal pass computed it
-        const float pxi = a.S1.p[0][i], pyi = a.S1.p[1][i], pzi = a.S1.p[2][i];
-        const float bx = (x > 0 ? a.S1.p[0][i - 1] : 0.f) - pxi;
-        const float by = (y > 0 ? a.S1.p[1][i - W] : 0.f) - pyi;
-        float div = bx + by;
-        const float bz = (z > 0 ? a.S1.p[2][i - WH] : 0.f) - pzi;
-        if (!a.skip_bz) div = div + bz;
-        const float uo = a.S.u[i], fi = a.f[i];
-        const float ut = uo - a.tau * div;
-        const float aub = a.A.ubar[i];
-        const float ua = a.A.u[i] + (1.f + a.theta) * aub;
-        float uta, gf = 0.f;
-        if (a.data_term == TGVDCT_DATA_L1) {
-            const float dd = ut - fi;
-            if (dd > a.tau_lambda) {
-                uta = ua;
-                glam = -a.tau * ua;
-            } else if (dd < -a.tau_lambda) {
-                uta = ua;
-                glam = a.tau * ua;
-            } else {
-                uta = 0.f;
-                gf = ua;
-            }
-        } else {
-            const float den = 1.f + a.tau_lambda;
-            uta = ua / den;
-            gf = a.tau_lambda * ua / den;
-            glam = ua * a.tau * (fi - ut) / (den * den);
-        }
-        a.A.u[i] = -a.theta * aub + uta;
-        a.uta[i] = uta;
-        a.grad_f[i] += gf;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float avb = a.A.vbar[c][i];
-            const float va = a.A.v[c][i] + (1.f + a.theta) * avb;
-            a.va[c][i] = va;
-            a.A.v[c][i] = va - a.theta * avb;
-        }
+        const size_t i = ((size_t)z * a.H + y) * a.W + x;
+        const float avb[3] = {a.A.vbar[0][i], a.A.vbar[1][i], a.A.vbar[2][i]};
+        glam = r1_at(a, x, y, z, i, a.A.ubar[i], avb);
+    }
+    block_add(&a.gp[0], glam);
+}
+
+// R3 of iteration k followed by R1 of iteration k-1 (S = S_{k-1}, S1 = S_k): a(ubar)
+// and a(vbar) stay in registers.
+__global__ void __launch_bounds__(BX* BY) adjoint_r3r1(AdjArgs a) {
+    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+    const int z = blockIdx.z;
+    float glam = 0.f;
+    if (x < a.W && y < a.H) {
+        const size_t i = ((size_t)z * a.H + y) * a.W + x;
+        float aub, avb[3];
+        r3_at(a, x, y, z, i, aub, avb);
+        glam = r1_at(a, x, y, z, i, aub, avb);
     }
     block_add(&a.gp[0], glam);
 }
@@ -196,32 +253,12 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r3(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z = blockIdx.z;
     if (x >= a.W || y >= a.H) return;
-    const size_t W = a.W, WH = a.WH, i = ((size_t)z * a.H + y) * W + x;
-    const bool xl = x + 1 < a.W, yl = y + 1 < a.H, zl = z + 1 < a.D;
-    const bool xf = x > 0, yf = y > 0, zf = z > 0;
-    // a(ubar) = sigma sum_c F_c^T a(p)_c
-    const float* P0 = a.A.p[0];
-    const float* P1 = a.A.p[1];
-    const float* P2 = a.A.p[2];
-    const float p0 = P0[i], p1 = P1[i], p2 = P2[i];
-    const float ftx = (xf ? P0[i - 1] : 0.f) - (xl ? p0 : 0.f);
-    const float fty = (yf ? P1[i - W] : 0.f) - (yl ? p1 : 0.f);
-    const float ftz = (zf ? P2[i - WH] : 0.f) - (zl ? p2 : 0.f);
-    a.A.ubar[i] = a.sigma * ((ftx + fty) + ftz);
-    // a(vbar)_c = -sigma a(p)_c + sigma sum_a w B_a^T a(q)_{c a}
-    auto bt = [&](const float* g, int axis) {
-        const float g0 = g[i];
-        if (axis == 0) return (xl ? g[i + 1] : 0.f) - g0;
-        if (axis == 1) return (yl ? g[i + W] : 0.f) - g0;
-        return (zl ? g[i + WH] : 0.f) - g0;
-    };
-    const float* const* Q = a.A.q;  // xx yy zz xy xz yz
-    const float ex = bt(Q[0], 0) + 0.5f * bt(Q[3], 1) + 0.5f * bt(Q[4], 2);
-    const float ey = 0.5f * bt(Q[3], 0) + bt(Q[1], 1) + 0.5f * bt(Q[5], 2);
-    const float ez = 0.5f * bt(Q[4], 0) + 0.5f * bt(Q[5], 1) + bt(Q[2], 2);
-    a.A.vbar[0][i] = -a.sigma * p0 + a.sigma * ex;
-    a.A.vbar[1][i] = -a.sigma * p1 + a.sigma * ey;
-    a.A.vbar[2][i] = -a.sigma * p2 + a.sigma * ez;
+    const size_t i = ((size_t)z * a.H + y) * a.W + x;
+    float aub, avb[3];
+    r3_at(a, x, y, z, i, aub, avb);
+    a.A.ubar[i] = aub;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a.A.vbar[c][i] = avb[c];
 }
 
 __global__ void finish_grad_f(float* gf, const float* au, const float* aub, size_t n) {
@@ -257,17 +294,15 @@ void tgv_full_state_zero(const TgvFullDev& s, size_t n, cudaStream_t st) {
     TGV_CUDA(cudaMemsetAsync(s.u, 0, tgv_full_state_bytes(n), st));
 }
 
-void tgv_adjoint_iteration(const TgvState& s, const TgvStep& k, const TgvFullDev& Sk,
-                           const TgvFullDev& Sk1, const TgvFullDev& A, float* uta,
-                           float* const* va, float* grad_f, double* gp, cudaStream_t st) {
+void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* states,
+                         int len, const TgvFullDev& A, float* uta, float* const* va,
+                         float* grad_f, double* gp, cudaStream_t st) {
     AdjArgs a;
     a.W = s.W;
     a.H = s.H;
     a.D = s.D;
     a.WH = (size_t)s.W * s.H;
     a.f = s.f;
-    a.S = Sk;
-    a.S1 = Sk1;
     a.A = A;
     a.uta = uta;
     for (int c = 0; c < 3; ++c) a.va[c] = va[c];
@@ -283,9 +318,22 @@ void tgv_adjoint_iteration(const TgvState& s, const TgvStep& k, const TgvFullDev
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
     const dim3 block(BX, BY, 1);
     const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
+    // iteration j of the segment maps states[j] -> states[j + 1]
+    a.S = states[len - 1];
+    a.S1 = states[len];
     adjoint_r1<<<grid, block, 0, st>>>(a);
-    adjoint_r2<<<grid, block, 0, st>>>(a);
-    adjoint_r3<<<grid, block, 0, st>>>(a);
+    for (int j = len - 1; j >= 0; --j) {
+        a.S = states[j];
+        a.S1 = states[j + 1];
+        adjoint_r2<<<grid, block, 0, st>>>(a);
+        if (j > 0) {
+            a.S = states[j - 1];
+            a.S1 = states[j];
+            adjoint_r3r1<<<grid, block, 0, st>>>(a);
+        } else {
+            adjoint_r3<<<grid, block, 0, st>>>(a);
+        }
+    }
     TGV_CHECK_LAUNCH();
 }
 

@@ -50,6 +50,7 @@ struct tgvdct_context {
     size_t seg_bytes = 0;
     void* adj_block = nullptr;
     size_t adj_bytes = 0;
+    std::shared_ptr<void> step_cache;  // tensor maps of the recompute steps
 };
 
 namespace {
@@ -337,13 +338,15 @@ void destroy_ctx(tgvdct_context* c) {
 }
 
 // (re)allocates a context-owned device block of at least `bytes`
-void ensure_block(void** block, size_t* have, size_t bytes) {
-    if (*have >= bytes && *block) return;
+// Grows *block to at least `bytes`; returns whether it was reallocated.
+bool ensure_block(void** block, size_t* have, size_t bytes) {
+    if (*have >= bytes && *block) return false;
     if (*block) cudaFree(*block);
     *block = nullptr;
     *have = 0;
     TGV_CUDA(cudaMalloc(block, bytes));
     *have = bytes;
+    return true;
 }
 
 TgvFullDev full_state_at(void* block, size_t index, size_t n) {
@@ -638,8 +641,10 @@ tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const floa
         const uint32_t K = c->prm.iteration_count;
         const uint32_t count = (K + checkpoint_every - 1) / checkpoint_every;
         c->have_ckpt = false;
-        ensure_block(&c->ckpt_block, &c->ckpt_bytes,
-                     (size_t)(count ? count : 1) * tgv_full_state_bytes(n));
+        // the states at iterations 0, k, 2k, ... and the final state (index count)
+        if (ensure_block(&c->ckpt_block, &c->ckpt_bytes,
+                         (size_t)(count + 1) * tgv_full_state_bytes(n)))
+            c->step_cache.reset();
         TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
         tgv_state_init(c->st, s);
         const TgvStep k = step_of(c->prm);
@@ -648,6 +653,7 @@ tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const floa
                 tgv_save_state(c->st, full_state_at(c->ckpt_block, it / checkpoint_every, n), s);
             tgv_iterate(c->st, k, s);
         }
+        tgv_save_state(c->st, full_state_at(c->ckpt_block, count, n), s);
         c->iterations_run = K;
         TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
         float* vo[3] = {v_x_dev, v_y_dev, v_z_dev};
@@ -673,7 +679,11 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_de
         cudaStream_t s = (cudaStream_t)stream;
         const size_t n = voxels(c->prm);
         const uint32_t every = c->ckpt_every, K = c->ckpt_K;
-        ensure_block(&c->seg_block, &c->seg_bytes, (size_t)(every + 1) * tgv_full_state_bytes(n));
+        // a segment [k0, k1) reads S_k0 and S_k1 from the checkpoints and recomputes
+        // the k1 - k0 - 1 states between them
+        if (every > 1 &&
+            ensure_block(&c->seg_block, &c->seg_bytes, (size_t)(every - 1) * tgv_full_state_bytes(n)))
+            c->step_cache.reset();
         const size_t field = (n * 4 + 255) & ~size_t(255);
         ensure_block(&c->adj_block, &c->adj_bytes, tgv_full_state_bytes(n) + 4 * field);
         TgvFullDev A = full_state_at(c->adj_block, 0, n);
@@ -689,18 +699,17 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_de
         TGV_CUDA(cudaMemsetAsync(grad_f_dev, 0, n * 4, s));
         TGV_CUDA(cudaMemsetAsync(grad_params_dev, 0, 3 * sizeof(double), s));
         const TgvStep k = step_of(c->prm);
+        std::vector<TgvFullDev> states(every + 1);
         for (int seg = (int)c->ckpt_count - 1; seg >= 0; --seg) {
             const uint32_t k0 = (uint32_t)seg * every, k1 = k0 + every < K ? k0 + every : K;
-            TGV_CUDA(cudaMemcpyAsync(full_state_at(c->seg_block, 0, n).u,
-                                     full_state_at(c->ckpt_block, seg, n).u,
-                                     tgv_full_state_bytes(n), cudaMemcpyDeviceToDevice, s));
-            for (uint32_t it = k0; it < k1; ++it)
-                tgv_step_fp32(c->st, k, full_state_at(c->seg_block, it - k0, n),
-                              full_state_at(c->seg_block, it - k0 + 1, n), s);
-            for (uint32_t it = k1; it-- > k0;)
-                tgv_adjoint_iteration(c->st, k, full_state_at(c->seg_block, it - k0, n),
-                                      full_state_at(c->seg_block, it - k0 + 1, n), A, uta, va,
-                                      grad_f_dev, grad_params_dev, s);
+            const int len = (int)(k1 - k0);
+            states[0] = full_state_at(c->ckpt_block, seg, n);
+            for (int j = 1; j < len; ++j) states[j] = full_state_at(c->seg_block, j - 1, n);
+            states[len] = full_state_at(c->ckpt_block, seg + 1, n);
+            for (int j = 0; j + 1 < len; ++j)
+                tgv_step_fp32(c->st, k, states[j], states[j + 1], c->step_cache, s);
+            tgv_adjoint_segment(c->st, k, states.data(), len, A, uta, va, grad_f_dev,
+                                grad_params_dev, s);
         }
         tgv_adjoint_finish(grad_f_dev, A, n, s);
         return TGVDCT_OK;

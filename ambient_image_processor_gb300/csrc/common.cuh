@@ -126,15 +126,18 @@ void tgv_full_state_zero(const TgvFullDev& s, size_t n, cudaStream_t st);
 // Copies the loop's current state (u, v and the current stencil set) into `out`.
 void tgv_save_state(const TgvState& s, const TgvFullDev& out, cudaStream_t st);
 // One FP32 iteration from `in` to `out` (distinct buffers), the same arithmetic as
-// every forward kernel (they agree bit for bit).
+// every forward kernel (they agree bit for bit). Where the shape allows TMA it runs
+// the TMA kernel, whose tensor maps of each (in, out) pair are encoded once and kept
+// in `cache`; otherwise the two-pass kernels.
 void tgv_step_fp32(const TgvState& s, const TgvStep& k, const TgvFullDev& in,
-                   const TgvFullDev& out, cudaStream_t st);
-// Adjoint of the iteration S_k -> S_{k+1}: A holds the adjoint of S_{k+1} on entry
-// and of S_k on return; accumulates d/df into grad_f and d/d(lambda, alpha0, alpha1)
-// into gp[0..2]; uta and va are scratch (1 + 3 fields).
-void tgv_adjoint_iteration(const TgvState& s, const TgvStep& k, const TgvFullDev& Sk,
-                           const TgvFullDev& Sk1, const TgvFullDev& A, float* uta,
-                           float* const* va, float* grad_f, double* gp, cudaStream_t st);
+                   const TgvFullDev& out, std::shared_ptr<void>& cache, cudaStream_t st);
+// Adjoint of the `len` iterations states[0] -> ... -> states[len] (len + 1 states):
+// A holds the adjoint of states[len] on entry and of states[0] on return; accumulates
+// d/df into grad_f and d/d(lambda, alpha0, alpha1) into gp[0..2]; uta and va are
+// scratch (1 + 3 fields).
+void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* states,
+                         int len, const TgvFullDev& A, float* uta, float* const* va,
+                         float* grad_f, double* gp, cudaStream_t st);
 // grad_f += a(u_0) + a(ubar_0) (the loop starts from u = ubar = f).
 void tgv_adjoint_finish(float* grad_f, const TgvFullDev& A, size_t n, cudaStream_t st);
 

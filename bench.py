@@ -289,12 +289,14 @@ def time_other_configs(pkg, torch, stream):
     return res
 
 
-def time_adjoint(pkg, torch, stream, n=96, K=200, every=20):
-    """Backward over forward time of the checkpointed reverse mode (96^3, K = 200)."""
+def time_adjoint(pkg, torch, stream, shape=(96, 96, 96), K=200, every=20):
+    """Backward over forward time of the checkpointed reverse mode (default: 96^3,
+    K = 200, checkpoints every 20)."""
     from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
-    f = torch.from_numpy(tissue_phantom_3d(n, n, n, bias=False, noise=0.05, rician=False,
+    d, h, w = shape
+    f = torch.from_numpy(tissue_phantom_3d(d, h, w, bias=False, noise=0.05, rician=False,
                                            seed=4)).cuda()
-    prm = pkg.default_params(width=n, height=n, depth=n, iteration_count=K)
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=K)
     u, vx, vy, vz, gu, gf = (torch.empty_like(f) for _ in range(6))
     gu.normal_()
     gp = torch.empty(3, dtype=torch.float64, device=f.device)
@@ -321,7 +323,7 @@ def time_adjoint(pkg, torch, stream, n=96, K=200, every=20):
             torch.cuda.synchronize()
             out[name + "_ms"] = e0.elapsed_time(e1)
     out["backward_over_forward"] = out["backward_ms"] / out["forward_ms"]
-    out["workload"] = f"{n}^3, K = {K}, checkpoints every {every}"
+    out["workload"] = f"{w}x{h}x{d}, K = {K}, checkpoints every {every}"
     return out
 
 
@@ -429,6 +431,8 @@ def run_ours(args):
             extra["iteration_variants"] = var
             extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
             extra["adjoint"] = time_adjoint(pkg, torch, stream)
+            extra["adjoint_256x256x192"] = time_adjoint(pkg, torch, stream, (192, 256, 256),
+                                                        K=100, every=20)
             extra["other_configs"] = time_other_configs(pkg, torch, stream)
         cpu = None
         if not args.no_cpu_baseline:
