@@ -114,10 +114,20 @@ _SIGS = {
     "tgvdct_process_tgv2_l1": [ctypes.POINTER(Params), _f32p, _vp, _i32, _i32, _i32, CALLBACK,
                                _vp, _f32p, _f32p, _f32p],
     "tgvdct_process_dev": [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+    "tgvdct_resize_bspline3": [_f32p, _u32, _u32, _u32, _f32p, _u32, _u32, _u32],
+    "tgvdct_resize_bspline3_dev": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _u32, _vp],
+    "tgvdct_resize_factor_extent": [_u32, _flt],
+    "tgvdct_process_tgvk_l1_downsampled": [_f32p, _vp, _u32, _u32, _u32, _flt, _flt, _u32, _f32p,
+                                           _u32, _i32, _i32, _i32, _u32, CALLBACK, _vp, _f32p,
+                                           _f32p, _f32p, _vp],
+    "tgvdct_process_tgvk_l1_downsampled_dev": [_vp, _vp, _u32, _u32, _u32, _flt, _flt, _u32,
+                                               _f32p, _u32, _i32, _i32, _i32, _u32, CALLBACK,
+                                               _vp, _vp, _vp, _vp, _vp, _vp],
 }
 _RESTYPES = {"tgvdct_params_init": None, "tgvdct_workspace_bytes": ctypes.c_size_t,
              "tgvdct_iterations_run": ctypes.c_uint32, "tgvdct_version": ctypes.c_char_p,
-             "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p}
+             "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p,
+             "tgvdct_resize_factor_extent": ctypes.c_uint32}
 
 # symbols of include/tgvdct.h (checked by the CPU test suite)
 EXPORTED = sorted(set(_SIGS) | {"tgvdct_version", "tgvdct_last_error", "tgvdct_status_string"})
@@ -450,6 +460,115 @@ def tgv2_l1_deshade_masked_launch(f, mask, lambda_, iteration_count, alpha0, alp
                                                       -1, CALLBACK(), None, alpha0, alpha1, u,
                                                       vx, vy, vz.ctypes.data_as(_vp)))
     return u, vx, vy, vz
+
+
+# ---------------------------------------------------------------------------
+# Down-sampled deshade (reference: resize/ResizeProcessor.cpp,
+# tgvk_deshade_downsampled/TGVKDeshadeDownsampled*Processor.cpp)
+BSPLINE3 = "BSpline3"
+
+
+def _shape_of(a: np.ndarray):
+    """(depth, height, width) of a 2-D (H, W) or 3-D (D, H, W) image."""
+    return (1,) + a.shape if a.ndim == 2 else a.shape
+
+
+class ResizeProcessor:
+    """Mirror of the reference's ResizeProcessor (resize/ResizeProcessor.h) for its
+    BSpline3 interpolation method, over numpy images."""
+
+    InterpolationMethod = type("InterpolationMethod", (), {"BSpline3": BSPLINE3})
+
+    @staticmethod
+    def size_for_factor(shape, size_factor):
+        """(depth, height, width) of process(image, size_factor) (ResizeProcessor.cpp:35-47)."""
+        e = lib().tgvdct_resize_factor_extent
+        return tuple(int(e(int(n), float(size_factor))) for n in shape)
+
+    @staticmethod
+    def process(image, size_factor_or_width, height=None, depth=None,
+                interpolation_method=BSPLINE3):
+        """process(image, size_factor, method) or process(image, width, height, depth,
+        method) (ResizeProcessor.cpp:35-143), cubic B-spline through the GPU.  A 2-D
+        (H, W) image stays 2-D when depth is 1."""
+        if interpolation_method != BSPLINE3:
+            raise ValueError("only the BSpline3 interpolation method is built")
+        x = _f32(image)
+        w, h, d = _dims(x)
+        if height is None:
+            D, H, W = ResizeProcessor.size_for_factor((d, h, w), size_factor_or_width)
+        else:
+            W, H, D = int(size_factor_or_width), int(height), int(depth if depth else 1)
+        out = np.empty((H, W) if (x.ndim == 2 and D == 1) else (D, H, W), dtype=np.float32)
+        _check(lib().tgvdct_resize_bspline3(x, w, h, d, out, W, H, D))
+        return out
+
+
+def _downsampled(not_masked, input_image, downsampling_factor, lambda_, order, alpha,
+                 iteration_count, mask, set_negative_values_to_zero, add_background_back,
+                 paint_iteration_interval, iteration_finished_callback, calculate_div_v):
+    f = _f32(input_image)
+    w, h, d = _dims(f)
+    m = None if mask is None else _f32(mask)
+    if m is not None and m.shape != f.shape:
+        raise ValueError("mask shape differs from the image shape")
+    a = _f32(np.asarray(alpha, dtype=np.float32).reshape(-1))
+    if a.size < 2:
+        raise ValueError("alpha needs order entries")
+    u, l, r = (np.empty_like(f) for _ in range(3))
+    dv = np.empty_like(f) if calculate_div_v else None
+    if downsampling_factor == 1:
+        small = _shape_of(f)
+    else:
+        small = ResizeProcessor.size_for_factor(_shape_of(f), downsampling_factor)
+    cb, keep = _make_callback(iteration_finished_callback,
+                              small if f.ndim == 3 else small[1:], 3)
+    _check(lib().tgvdct_process_tgvk_l1_downsampled(
+        f, None if m is None else m.ctypes.data_as(_vp), w, h, d, float(downsampling_factor),
+        float(lambda_), int(order), a, int(iteration_count), int(set_negative_values_to_zero),
+        int(add_background_back), int(not_masked), int(paint_iteration_interval), cb, None, u, l,
+        r, None if dv is None else dv.ctypes.data_as(_vp)))
+    del keep
+    return u, l, r, dv
+
+
+class TGVKDeshadeDownsampledProcessor:
+    """Mirror of the reference's TGVKDeshadeDownsampledProcessor
+    (tgvk_deshade_downsampled/TGVKDeshadeDownsampledProcessor.h) over numpy images."""
+
+    @staticmethod
+    def processTGVKL1Cuda(input_image, downsampling_factor, lambda_, order, alpha,
+                          iteration_count, mask=None, set_negative_values_to_zero=True,
+                          add_background_back=False, paint_iteration_interval=0,
+                          iteration_finished_callback=None, calculate_div_v=False):
+        """processTGVKL1Cuda (TGVKDeshadeDownsampledProcessor.cpp:30-129): the image
+        (times the mask) and the mask are resized by downsampling_factor with cubic
+        B-splines, deshaded there by the masked TGV2 processor (order 2; alpha0 =
+        alpha[1], alpha1 = alpha[0]), and the denoised image and the shading resized
+        back.  Returns (denoised_image, shading_image, deshaded_image, div_v_image or
+        None); the callback gets the down-sampled (iteration, count, u, l, r)."""
+        return _downsampled(False, input_image, downsampling_factor, lambda_, order, alpha,
+                            iteration_count, mask, set_negative_values_to_zero,
+                            add_background_back, paint_iteration_interval,
+                            iteration_finished_callback, calculate_div_v)
+
+
+class TGVKDeshadeDownsampledNotMaskedProcessor:
+    """Mirror of the reference's TGVKDeshadeDownsampledNotMaskedProcessor
+    (tgvk_deshade_downsampled/TGVKDeshadeDownsampledNotMaskedProcessor.h)."""
+
+    @staticmethod
+    def processTGVKL1Cuda(input_image, downsampling_factor, lambda_, order, alpha,
+                          iteration_count, mask=None, set_negative_values_to_zero=True,
+                          add_background_back=False, paint_iteration_interval=0,
+                          iteration_finished_callback=None, calculate_div_v=False):
+        """processTGVKL1Cuda (TGVKDeshadeDownsampledNotMaskedProcessor.cpp:30-129): as
+        the masked variant, but the TGV2 loop runs on every voxel of the resized image
+        and the mask only weights the results."""
+        return _downsampled(True, input_image, downsampling_factor, lambda_, order, alpha,
+                            iteration_count, mask, set_negative_values_to_zero,
+                            add_background_back, paint_iteration_interval,
+                            iteration_finished_callback, calculate_div_v)
 
 
 # ---------------------------------------------------------------------------

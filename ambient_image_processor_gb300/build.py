@@ -5,8 +5,9 @@ parallel, then linked into ``ambient_image_processor_gb300/_build/libtgvdct.so``
 No cmake, no torch extension machinery: the library exposes plain ``extern "C"``
 symbols declared in ``include/tgvdct.h``.  On top of it, g++ builds the host-only
 reference-signature layer ``libtgvdct_refapi.so`` (``include/tgvdct_reference_api.hpp``)
-and the terminal programs ``tgv2_deshade_application`` and
-``tgv2_deshade_convergence_test_application``.
+and the terminal programs ``tgv2_deshade_application``,
+``tgv2_deshade_convergence_test_application`` and
+``tgvk_deshade_downsampled_application``.
 
     python -m ambient_image_processor_gb300.build
 """
@@ -27,6 +28,7 @@ REFAPI = os.path.join(PKG, "refapi")
 REFAPI_LIB = os.path.join(OUT, "libtgvdct_refapi.so")
 CLI = os.path.join(OUT, "tgv2_deshade_application")
 CONVERGENCE_CLI = os.path.join(OUT, "tgv2_deshade_convergence_test_application")
+DOWNSAMPLED_CLI = os.path.join(OUT, "tgvk_deshade_downsampled_application")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
@@ -46,6 +48,9 @@ UNITS = {
     # the adjoint recomputes forward predicates (prox branch, projection activity)
     # and must round exactly like tgv_kernels.cu
     "adjoint.cu": ["-fmad=false"],
+    # the FP64 resize follows ITK's operation sequence, on the device and in its host
+    # tables (g++ contracts a*b+c into FMA on aarch64 unless told not to)
+    "resize.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 
@@ -109,6 +114,10 @@ def build_host(force: bool = False) -> None:
                 os.path.join(REFAPI, "metaimage.cpp")]
     if force or _stale(CONVERGENCE_CLI, [*conv_src, *hdrs, LIB]):
         _run([cxx, *flags, "-o", CONVERGENCE_CLI, *conv_src, *link])
+    ds_src = [os.path.join(REFAPI, "tgvk_deshade_downsampled_main.cpp"),
+              os.path.join(REFAPI, "metaimage.cpp")]
+    if force or _stale(DOWNSAMPLED_CLI, [*ds_src, *hdrs, LIB]):
+        _run([cxx, *flags, "-o", DOWNSAMPLED_CLI, *ds_src, *link])
 
 
 if __name__ == "__main__":

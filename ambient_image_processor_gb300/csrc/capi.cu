@@ -442,6 +442,97 @@ void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_
     }
 }
 
+// TGVKDeshadeDownsampledProcessor::processTGVKL1Cuda
+// (tgvk_deshade_downsampled/TGVKDeshadeDownsampledProcessor.cpp:30-129) and, with
+// not_masked, TGVKDeshadeDownsampledNotMaskedProcessor::processTGVKL1Cuda (same file
+// layout, :30-129), order 2, on device buffers.  Order 2 is what the reference hands
+// to its TGV2 processors with alpha0 = alpha[1] and alpha1 = alpha[0]
+// (TGVKDeshadeMaskedProcessor.cpp:98-103, TGVKDeshadeProcessor.cpp:137-147, 242-250).
+// Returns whether the callback stopped the loop.
+bool downsampled_on_device(const float* f, const float* mask, uint32_t w, uint32_t h, uint32_t d,
+                           float factor, float lambda, const float* alpha, uint32_t iterations,
+                           uint32_t paint_interval, bool clamp, bool add_back, bool not_masked,
+                           tgvdct_iteration_callback cb, void* user, float* u_out, float* l_out,
+                           float* r_out, float* divv_out, cudaStream_t s) {
+    const size_t n = (size_t)w * h * d;
+    const bool same = factor == 1.f;  // the reference skips both resizes (:65-66, :105-106)
+    const uint32_t W = same ? w : resize_factor_extent(w, factor);
+    const uint32_t H = same ? h : resize_factor_extent(h, factor);
+    const uint32_t D = same ? d : resize_factor_extent(d, factor);
+    const size_t m = (size_t)W * H * D;
+    // the masked variant multiplies the input by the mask before resizing (:59-60)
+    DevBuf fin((!not_masked && mask) ? n : 0);
+    const float* src = f;
+    if (!not_masked && mask) {
+        multiply_fields(f, mask, fin.p, n, s);
+        src = fin.p;
+    }
+    const size_t scratch_bytes =
+        same ? 0
+             : std::max(resize_scratch_bytes((int)w, (int)h, (int)d, (int)W, (int)H, (int)D),
+                        resize_scratch_bytes((int)W, (int)H, (int)D, (int)w, (int)h, (int)d));
+    DevBuf scratch((scratch_bytes + 3) / 4);
+    DevBuf ds(same ? 0 : m), dsm((same || !mask) ? 0 : m);
+    const float* ds_p = src;
+    const float* dsm_p = mask;
+    if (!same) {
+        resize_bspline3(src, (int)w, (int)h, (int)d, ds.p, (int)W, (int)H, (int)D, scratch.p, s);
+        ds_p = ds.p;
+        if (mask) {
+            resize_bspline3(mask, (int)w, (int)h, (int)d, dsm.p, (int)W, (int)H, (int)D,
+                            scratch.p, s);
+            dsm_p = dsm.p;
+        }
+    }
+    tgvdct_params q;
+    tgvdct_params_init(&q);
+    q.width = W;
+    q.height = H;
+    q.depth = D;
+    q.lambda = lambda;
+    q.alpha0 = alpha[1];
+    q.alpha1 = alpha[0];
+    q.iteration_count = iterations;
+    q.paint_iteration_interval = paint_interval;
+    q.geometry = D == 1 ? TGVDCT_GEOMETRY_2D : TGVDCT_GEOMETRY_3D;
+    CtxGuard g;
+    create_into(&q, &g.c);
+    tgvdct_context* c = g.c;
+    DevBuf du(m), dl(m), dr(m);
+    if (!not_masked) {
+        // the masked processor: a missing mask means every voxel (TGVDeshadeMaskedProcessor.cpp:102-106)
+        DevBuf ones(dsm_p ? 0 : m);
+        if (!dsm_p) {
+            fill_field(ones.p, 1.f, m, s);
+            dsm_p = ones.p;
+        }
+        set_domain(c, dsm_p, s);
+        process_on_device(c, ds_p, nullptr, clamp, add_back, false, du.p, dl.p, dr.p, cb, user, s);
+        TGV_CUDA(cudaStreamSynchronize(s));  // `ones` is freed on return
+    } else {
+        process_on_device(c, ds_p, dsm_p, clamp, add_back, false, du.p, dl.p, dr.p, cb, user, s);
+    }
+    check_tgv_flag(c, s);
+    const bool stopped = c->iterations_run < iterations;
+    DevBuf ddiv((divv_out && !same) ? m : 0);
+    if (divv_out)
+        divergence(plan_of(c), c->st.v[0], c->st.v[1], D > 1 ? c->st.v[2] : nullptr,
+                   same ? divv_out : ddiv.p, s);
+    if (same) {
+        TGV_CUDA(cudaMemcpyAsync(u_out, du.p, n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(l_out, dl.p, n * 4, cudaMemcpyDeviceToDevice, s));
+    } else {
+        resize_bspline3(du.p, (int)W, (int)H, (int)D, u_out, (int)w, (int)h, (int)d, scratch.p, s);
+        resize_bspline3(dl.p, (int)W, (int)H, (int)D, l_out, (int)w, (int)h, (int)d, scratch.p, s);
+        if (divv_out)
+            resize_bspline3(ddiv.p, (int)W, (int)H, (int)D, divv_out, (int)w, (int)h, (int)d,
+                            scratch.p, s);
+    }
+    downsampled_tail(f, mask, l_out, r_out, n, not_masked, clamp, add_back, s);
+    TGV_CUDA(cudaStreamSynchronize(s));  // the scratch buffers are freed on return
+    return stopped;
+}
+
 }  // namespace
 
 namespace {
@@ -1285,6 +1376,118 @@ tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host
             return TGVDCT_ERR_CUDA;
         }
         return c->iterations_run < p->iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_resize_bspline3_dev(const float* in_dev, uint32_t width, uint32_t height,
+                                         uint32_t depth, float* out_dev, uint32_t out_width,
+                                         uint32_t out_height, uint32_t out_depth, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(in_dev && out_dev, "null device buffer");
+        TGV_REQUIRE(width >= 1 && height >= 1 && depth >= 1 && out_width >= 1 &&
+                        out_height >= 1 && out_depth >= 1,
+                    "extents must be >= 1");
+        check_device();
+        cudaStream_t s = (cudaStream_t)stream;
+        DevBuf scratch((resize_scratch_bytes((int)width, (int)height, (int)depth, (int)out_width,
+                                             (int)out_height, (int)out_depth) +
+                        3) /
+                       4);
+        resize_bspline3(in_dev, (int)width, (int)height, (int)depth, out_dev, (int)out_width,
+                        (int)out_height, (int)out_depth, scratch.p, s);
+        TGV_CUDA(cudaStreamSynchronize(s));
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_resize_bspline3(const float* in_host, uint32_t width, uint32_t height,
+                                     uint32_t depth, float* out_host, uint32_t out_width,
+                                     uint32_t out_height, uint32_t out_depth) {
+    return guarded([&] {
+        TGV_REQUIRE(in_host && out_host, "null host buffer");
+        TGV_REQUIRE(width >= 1 && height >= 1 && depth >= 1 && out_width >= 1 &&
+                        out_height >= 1 && out_depth >= 1,
+                    "extents must be >= 1");
+        check_device();
+        const size_t n = (size_t)width * height * depth;
+        const size_t m = (size_t)out_width * out_height * out_depth;
+        DevBuf a(n), b(m);
+        DevBuf scratch((resize_scratch_bytes((int)width, (int)height, (int)depth, (int)out_width,
+                                             (int)out_height, (int)out_depth) +
+                        3) /
+                       4);
+        TGV_CUDA(cudaMemcpy(a.p, in_host, n * 4, cudaMemcpyHostToDevice));
+        resize_bspline3(a.p, (int)width, (int)height, (int)depth, b.p, (int)out_width,
+                        (int)out_height, (int)out_depth, scratch.p, 0);
+        TGV_CUDA(cudaMemcpy(out_host, b.p, m * 4, cudaMemcpyDeviceToHost));
+        return TGVDCT_OK;
+    });
+}
+
+uint32_t tgvdct_resize_factor_extent(uint32_t n, float factor) {
+    return resize_factor_extent(n, factor);
+}
+
+namespace {
+void check_downsampled_args(uint32_t width, uint32_t height, uint32_t depth, float factor,
+                            uint32_t order, const float* alpha) {
+    TGV_REQUIRE(width >= 1 && height >= 1 && depth >= 1, "width, height, depth must be >= 1");
+    TGV_REQUIRE(factor > 0.f, "downsampling_factor must be > 0");
+    TGV_REQUIRE(alpha != nullptr, "null alpha array");
+    if (order != 2) {
+        set_error("order " + std::to_string(order) +
+                  ": only order 2 is built (the reference runs its TGV2 processors for it); "
+                  "TGVk of other orders is not part of this library");
+        throw Error{TGVDCT_ERR_UNSUPPORTED};
+    }
+}
+}  // namespace
+
+tgvdct_status tgvdct_process_tgvk_l1_downsampled_dev(
+    const float* f_dev, const float* mask_dev, uint32_t width, uint32_t height, uint32_t depth,
+    float downsampling_factor, float lambda, uint32_t order, const float* alpha,
+    uint32_t iteration_count, int32_t set_negative_values_to_zero, int32_t add_background_back,
+    int32_t not_masked, uint32_t paint_iteration_interval, tgvdct_iteration_callback callback,
+    void* user, float* denoised_dev, float* shading_dev, float* deshaded_dev, float* div_v_dev,
+    void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(f_dev && denoised_dev && shading_dev && deshaded_dev, "null device buffer");
+        check_downsampled_args(width, height, depth, downsampling_factor, order, alpha);
+        check_device();
+        const bool stopped = downsampled_on_device(
+            f_dev, mask_dev, width, height, depth, downsampling_factor, lambda, alpha,
+            iteration_count, paint_iteration_interval, set_negative_values_to_zero != 0,
+            add_background_back != 0, not_masked != 0, callback, user, denoised_dev, shading_dev,
+            deshaded_dev, div_v_dev, (cudaStream_t)stream);
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_process_tgvk_l1_downsampled(
+    const float* f_host, const float* mask_host, uint32_t width, uint32_t height, uint32_t depth,
+    float downsampling_factor, float lambda, uint32_t order, const float* alpha,
+    uint32_t iteration_count, int32_t set_negative_values_to_zero, int32_t add_background_back,
+    int32_t not_masked, uint32_t paint_iteration_interval, tgvdct_iteration_callback callback,
+    void* user, float* denoised_host, float* shading_host, float* deshaded_host,
+    float* div_v_host) {
+    return guarded([&] {
+        TGV_REQUIRE(f_host && denoised_host && shading_host && deshaded_host, "null host buffer");
+        check_downsampled_args(width, height, depth, downsampling_factor, order, alpha);
+        check_device();
+        const size_t n = (size_t)width * height * depth;
+        DevBuf f(n), m(mask_host ? n : 0), u(n), l(n), r(n), dv(div_v_host ? n : 0);
+        TGV_CUDA(cudaMemcpy(f.p, f_host, n * 4, cudaMemcpyHostToDevice));
+        if (mask_host) TGV_CUDA(cudaMemcpy(m.p, mask_host, n * 4, cudaMemcpyHostToDevice));
+        const bool stopped = downsampled_on_device(
+            f.p, mask_host ? m.p : nullptr, width, height, depth, downsampling_factor, lambda,
+            alpha, iteration_count, paint_iteration_interval, set_negative_values_to_zero != 0,
+            add_background_back != 0, not_masked != 0, callback, user, u.p, l.p, r.p,
+            div_v_host ? dv.p : nullptr, 0);
+        TGV_CUDA(cudaMemcpy(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost));
+        TGV_CUDA(cudaMemcpy(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost));
+        TGV_CUDA(cudaMemcpy(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost));
+        if (div_v_host) TGV_CUDA(cudaMemcpy(div_v_host, dv.p, n * 4, cudaMemcpyDeviceToHost));
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
 

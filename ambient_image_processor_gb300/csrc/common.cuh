@@ -141,6 +141,22 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
 // grad_f += a(u_0) + a(ubar_0) (the loop starts from u = ubar = f).
 void tgv_adjoint_finish(float* grad_f, const TgvFullDev& A, size_t n, cudaStream_t st);
 
+// ---- cubic B-spline resize (resize.cu) -------------------------------------------
+// ceil(n * factor) in float, at least 1: ResizeProcessor::process(image, factor).
+unsigned resize_factor_extent(unsigned n, float factor);
+// Device scratch of resize_bspline3 (FP64 coefficients of the input and the tables).
+size_t resize_scratch_bytes(int w, int h, int d, int W, int H, int D);
+// ResizeProcessor::process(image, W, H, D, BSpline3): in is w x h x d, out W x H x D.
+void resize_bspline3(const float* in, int w, int h, int d, float* out, int W, int H, int D,
+                     void* scratch, cudaStream_t st);
+// The down-sampled deshade's tail at full resolution: r from the input f, the
+// up-sampled shading (multiplied by the mask in place in the masked variant), the
+// mask (may be null), the background add-back and the clamp.
+void downsampled_tail(const float* f, const float* mask, float* shading, float* r, size_t n,
+                      bool not_masked, bool clamp, bool add_back, cudaStream_t st);
+void multiply_fields(const float* a, const float* b, float* out, size_t n, cudaStream_t st);
+void fill_field(float* out, float v, size_t n, cudaStream_t st);
+
 // ---- Poisson integration -------------------------------------------------------
 // Per-shape cosine tables and scratch of the Poisson integration.
 struct DctPlan {

@@ -289,6 +289,54 @@ def time_other_configs(pkg, torch, stream):
     return res
 
 
+def time_downsampled(pkg, torch, stream):
+    """The down-sampled deshade (TGVKDeshadeDownsampledProcessor, order 2) of the
+    256x256x192 tissue phantom at factor 1/2, 1500 iterations, with an ellipsoid mask,
+    the clamp and the background add-back (the reference CLI's settings), device-timed
+    end to end; and the cubic B-spline resizes alone (down 256x256x192 -> 128x128x96,
+    up back)."""
+    import ctypes
+    import numpy as np
+    from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
+    d, h, w = 192, 256, 256
+    f = torch.from_numpy(tissue_phantom_3d(d, h, w, seed=2)).cuda()
+    z, y, x = np.meshgrid(np.linspace(-1, 1, d), np.linspace(-1, 1, h), np.linspace(-1, 1, w),
+                          indexing="ij")
+    mask = torch.from_numpy(((x / 0.9) ** 2 + (y / 0.85) ** 2 + (z / 0.95) ** 2 < 1)
+                            .astype(np.float32)).cuda()
+    u, l, r = (torch.empty_like(f) for _ in range(3))
+    alpha = np.array([1.0, 2.0], dtype=np.float32)
+    sh = stream.cuda_stream
+    L = pkg.lib()
+
+    def run():
+        pkg._check(L.tgvdct_process_tgvk_l1_downsampled_dev(
+            f.data_ptr(), mask.data_ptr(), w, h, d, 0.5, 1.0, 2, alpha, 1500, 1, 1, 0, 0,
+            pkg.CALLBACK(), None, u.data_ptr(), l.data_ptr(), r.data_ptr(), None, sh))
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    res = {"workload": "256x256x192 tissue phantom, factor 0.5 (128x128x96 loop), 1500 "
+                       "iterations, ellipsoid mask, clamp and add-back"}
+    ms = timed(run)
+    res["ms"] = ms
+    res["full_res_voxel_iters_per_s"] = w * h * d * 1500 / (ms * 1e-3)
+    small = torch.empty((96, 128, 128), device="cuda")
+    res["resize_down_ms"] = timed(lambda: pkg._check(L.tgvdct_resize_bspline3_dev(
+        f.data_ptr(), w, h, d, small.data_ptr(), 128, 128, 96, sh)))
+    res["resize_up_ms"] = timed(lambda: pkg._check(L.tgvdct_resize_bspline3_dev(
+        small.data_ptr(), 128, 128, 96, u.data_ptr(), w, h, d, sh)))
+    return res
+
+
 def time_adjoint(pkg, torch, stream, shape=(96, 96, 96), K=200, every=20):
     """Backward over forward time of the checkpointed reverse mode (default: 96^3,
     K = 200, checkpoints every 20)."""
@@ -434,6 +482,7 @@ def run_ours(args):
             extra["adjoint_256x256x192"] = time_adjoint(pkg, torch, stream, (192, 256, 256),
                                                         K=100, every=20)
             extra["other_configs"] = time_other_configs(pkg, torch, stream)
+            extra["downsampled_deshade"] = time_downsampled(pkg, torch, stream)
         cpu = None
         if not args.no_cpu_baseline:
             rate, cores, dt = cpu_reference(args, f_host, args.cpu_sample_iterations)

@@ -405,6 +405,51 @@ tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
     int cuda_block_dimension, tgvdct_iteration_callback callback, void* user, float alpha0,
     float alpha1, float* u_host, float* v_x_host, float* v_y_host, float* v_z_host);
 
+/* ---- down-sampled deshade (tgvk_deshade_downsampled/, resize/) ---------------- */
+/* Replaces ResizeProcessor::process(image, width, height, depth, BSpline3)
+   (resize/ResizeProcessor.cpp:49-143): ITK's cubic B-spline resample as that function
+   sets it up (output spacing = input spacing / (float)(out / in) per axis, origin 0;
+   when any axis grows, a grid two samples longer per axis of which the first
+   out_width x out_height x out_depth are kept).  FP64 coefficients and sums, like
+   ITK; float out.  Device form: stream-ordered, synchronises before returning. */
+tgvdct_status tgvdct_resize_bspline3(const float* in_host, uint32_t width, uint32_t height,
+                                     uint32_t depth, float* out_host, uint32_t out_width,
+                                     uint32_t out_height, uint32_t out_depth);
+tgvdct_status tgvdct_resize_bspline3_dev(const float* in_dev, uint32_t width, uint32_t height,
+                                         uint32_t depth, float* out_dev, uint32_t out_width,
+                                         uint32_t out_height, uint32_t out_depth, void* stream);
+/* ceil(n * factor) in float, at least 1: the extent ResizeProcessor::process(image,
+   size_factor, ...) gives (ResizeProcessor.cpp:35-47). */
+uint32_t tgvdct_resize_factor_extent(uint32_t n, float factor);
+
+/* Replaces TGVKDeshadeDownsampledProcessor::processTGVKL1Cuda
+   (tgvk_deshade_downsampled/TGVKDeshadeDownsampledProcessor.cpp:30-129) and, with
+   not_masked = 1, TGVKDeshadeDownsampledNotMaskedProcessor::processTGVKL1Cuda
+   (TGVKDeshadeDownsampledNotMaskedProcessor.cpp:30-129): resize the image (the masked
+   variant: the image times the mask) and the mask by downsampling_factor, deshade
+   there, resize the denoised image and the shading back, and form the deshaded image
+   at full resolution.  The inner deshade is the masked TGV2 processor (masked
+   variant) or the plain one with the mask in its epilogue (not_masked), which is what
+   the reference runs for order 2, with alpha0 = alpha[1] and alpha1 = alpha[0]
+   (TGVKDeshadeMaskedProcessor.cpp:98-103, TGVKDeshadeProcessor.cpp:137-147).  Other
+   orders return TGVDCT_ERR_UNSUPPORTED.  mask and div_v may be NULL; div_v is the
+   up-sampled divergence of v (calculate_div_v).  The callback sees the down-sampled
+   u, l, r.  A factor of 1 skips both resizes, as the reference does. */
+tgvdct_status tgvdct_process_tgvk_l1_downsampled(
+    const float* f_host, const float* mask_host, uint32_t width, uint32_t height, uint32_t depth,
+    float downsampling_factor, float lambda, uint32_t order, const float* alpha,
+    uint32_t iteration_count, int32_t set_negative_values_to_zero, int32_t add_background_back,
+    int32_t not_masked, uint32_t paint_iteration_interval, tgvdct_iteration_callback callback,
+    void* user, float* denoised_host, float* shading_host, float* deshaded_host,
+    float* div_v_host);
+tgvdct_status tgvdct_process_tgvk_l1_downsampled_dev(
+    const float* f_dev, const float* mask_dev, uint32_t width, uint32_t height, uint32_t depth,
+    float downsampling_factor, float lambda, uint32_t order, const float* alpha,
+    uint32_t iteration_count, int32_t set_negative_values_to_zero, int32_t add_background_back,
+    int32_t not_masked, uint32_t paint_iteration_interval, tgvdct_iteration_callback callback,
+    void* user, float* denoised_dev, float* shading_dev, float* deshaded_dev, float* div_v_dev,
+    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

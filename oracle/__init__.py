@@ -65,6 +65,9 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = [p, p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int,
                            ctypes.c_int, p, p, p, p]
             fn.restype = _u
+        L.oracle_resize_bspline3_f32.argtypes = [_f32p, _u, _u, _u, _f32p, _u, _u, _u]
+        L.oracle_resize_factor_extent.argtypes = [_u, ctypes.c_float]
+        L.oracle_resize_factor_extent.restype = _u
         vp = ctypes.c_void_p
         L.oracle_tgv2_gradient_f64.argtypes = [_f64p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d,
                                                ctypes.c_int, vp, vp, vp, vp, _f64p, _f64p, vp]
@@ -265,6 +268,103 @@ def tgv2_gradient(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=10, *, grad
 
 # ---------------------------------------------------------------------------
 # The reference's own kernels compiled for the CPU (available where they were built).
+
+def resize_factor_shape(shape, factor):
+    """Output (depth, height, width) of ResizeProcessor::process(image, factor)
+    (ResizeProcessor.cpp:35-47)."""
+    d, h, w = shape
+    e = lib().oracle_resize_factor_extent
+    return (e(d, factor), e(h, factor), e(w, factor))
+
+
+def resize_bspline3(image, shape):
+    """ResizeProcessor::process(image, width, height, depth, BSpline3) restated with
+    ITK's cubic B-spline resample (resize_oracle.hpp).  shape is (depth, height,
+    width); float32 in and out, FP64 inside."""
+    x = np.ascontiguousarray(image, dtype=np.float32)
+    w, h, d = _shape3(x)
+    D, H, W = shape
+    out = np.empty((D, H, W) if x.ndim == 3 else (H, W), dtype=np.float32)
+    lib().oracle_resize_bspline3_f32(x, w, h, d, out, W, H, D)
+    return out
+
+
+def process_tgvk_l1_downsampled(f, downsampling_factor, lambda_, order, alpha, iterations, *,
+                                mask=None, set_negative_values_to_zero=True,
+                                add_background_back=False, not_masked=False,
+                                calculate_div_v=False):
+    """TGVKDeshadeDownsampledProcessor::processTGVKL1Cuda
+    (tgvk_deshade_downsampled/TGVKDeshadeDownsampledProcessor.cpp:30-129), or with
+    not_masked the NotMasked variant (TGVKDeshadeDownsampledNotMaskedProcessor.cpp:30-129),
+    for order 2, the order the reference hands to its TGV2 processors
+    (TGVKDeshadeMaskedProcessor.cpp:98-103, TGVKDeshadeProcessor.cpp:137-147: alpha0 =
+    alpha[1], alpha1 = alpha[0]).  Float32 throughout, as the reference's images.
+    Returns (denoised, shading, deshaded, div_v or None)."""
+    if order != 2:
+        raise ValueError("only order 2 (TGV2) is restated")
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    one = np.float32(1)
+    a0, a1 = float(alpha[1]), float(alpha[0])
+    clamp, add_back = set_negative_values_to_zero, add_background_back
+    background = None
+    if not not_masked:
+        if add_back and m is not None:
+            background = f * (one - m)
+        fin = f * m if m is not None else f
+    else:
+        fin = f
+
+    def down(x):
+        if downsampling_factor == 1:
+            return x
+        return resize_bspline3(x, resize_factor_shape(_dhw(x), downsampling_factor))
+
+    ds = down(fin)
+    dsm = None if m is None else down(m)
+    two_d = _dhw(ds)[0] == 1
+    if not not_masked:
+        inner_mask = dsm if dsm is not None else np.ones_like(ds)
+        u, vx, vy, vz = tgv2_deshade_masked(ds, inner_mask, lambda_, a0, a1, iterations,
+                                            dtype=np.float32)
+        l = integrate_poisson_dct(vx, vy, vz)
+        _, l = masked_deshade_epilogue(u, l, inner_mask, clamp, add_back)
+    else:
+        u, vx, vy, vz = tgv2_deshade(ds, lambda_, a0, a1, iterations, two_d=two_d,
+                                     dtype=np.float32)
+        l = integrate_poisson_dct(vx, vy, vz)
+        _, l = deshade_epilogue(u, l, dsm, clamp, add_back)
+    div_v = divergence(vx, vy, vz) if calculate_div_v else None
+
+    def up(x):
+        if downsampling_factor == 1:
+            return x
+        return resize_bspline3(x, _dhw(f))
+
+    denoised = up(u)
+    shading = up(l)
+    deshaded = fin - shading
+    if not not_masked:
+        if m is not None:
+            shading = shading * m
+            deshaded = deshaded * m
+        if add_back and m is not None:
+            deshaded = deshaded + background
+    else:
+        if m is not None:
+            deshaded = deshaded * m
+        if add_back and m is not None:
+            deshaded = deshaded + fin * (one - m)
+    if clamp:
+        deshaded = np.where(deshaded < 0, np.float32(0), deshaded)
+    if div_v is not None:
+        div_v = up(div_v)
+    return denoised, shading, deshaded, div_v
+
+
+def _dhw(x):
+    return (1,) + x.shape if x.ndim == 2 else x.shape
+
 
 def ref_available() -> bool:
     return os.path.exists(_REF_PATH)

@@ -4,6 +4,7 @@
 
 #include "tgv_adjoint.hpp"
 #include "tgv_oracle.hpp"
+#include "resize_oracle.hpp"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -135,6 +136,16 @@ void oracle_tgv2_gradient_f64(const double* f, unsigned w, unsigned h, unsigned 
     k.skip_bz = data_term == oracle::L2 && d == 1;
     const double* gv[3] = {gvx, gvy, gvz};
     oracle::tgv2_gradient<double>(f, dims(w, h, d), k, K, gu, gv, grad_f, grad_params, u_out);
+}
+
+// Cubic B-spline resize as ResizeProcessor runs it through ITK (resize_oracle.hpp).
+void oracle_resize_bspline3_f32(const float* in, unsigned w, unsigned h, unsigned d, float* out,
+                                unsigned W, unsigned H, unsigned D) {
+    oracle::resize_bspline3<float>(in, w, h, d, out, W, H, D);
+}
+
+unsigned oracle_resize_factor_extent(unsigned n, float factor) {
+    return oracle::resize_factor_extent(n, factor);
 }
 
 }  // extern "C"
