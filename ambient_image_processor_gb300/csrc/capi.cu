@@ -51,6 +51,14 @@ struct tgvdct_context {
     void* adj_block = nullptr;
     size_t adj_bytes = 0;
     std::shared_ptr<void> step_cache;  // tensor maps of the recompute steps
+    // the whole backward pass as one CUDA graph, valid while its key holds
+    cudaGraphExec_t bwd_graph = nullptr;
+    struct BwdKey {
+        const void *ckpt = nullptr, *seg = nullptr, *adj = nullptr;
+        uint32_t every = 0, K = 0, count = 0;
+        int zchunk = 0;
+        TgvStep step{};
+    } bwd_key;
 };
 
 namespace {
@@ -97,17 +105,39 @@ int kernel_of(const tgvdct_params& p) {
     }
 }
 
-// Planes per block of the fused kernel: enough blocks to fill the GPU a few
-// times over, few enough that the one-plane prologue of each chunk stays small.
+// Planes per block of the fused kernel.  The blocks of one launch run in waves of
+// (SMs x 2) resident blocks, so a launch whose block count ends just short of a full
+// wave leaves the GPU part-empty at its end; each z-chunk also pays a prologue of
+// about 0.7 planes.  Over balanced chunk counts k (z = ceil(D / k), 12 <= z <= 64)
+// this picks the best (wave fill) x (1 - 0.7 / z).  At 256 x 256 x 192 on 152 SMs:
+// k = 7, z = 28, 1792 blocks = 5.89 waves (measured 333.8 us per iteration, against
+// 338 us at z = 24 and 353 us at z = 32).
 int auto_zchunk(const tgvdct_params& p) {
     if (p.z_chunk > 0) return (int)p.z_chunk;
-    const long long tiles = (long long)((p.width + 31) / 32) * ((p.height + 7) / 8);
-    const long long target_blocks = 152LL * 3 * 4;  // ~4 waves of 3 blocks per SM
-    long long chunks = (target_blocks + tiles - 1) / tiles;
-    if (chunks < 1) chunks = 1;
-    long long z = ((long long)p.depth + chunks - 1) / chunks;
-    if (z < 16) z = 16;
-    return (int)z;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    const double slots = 2.0 * sms;
+    const double tiles = (double)((p.width + 31) / 32) * ((p.height + 7) / 8);
+    const long long D = p.depth;
+    int best_z = (int)std::min<long long>(D, 64);
+    double best = -1.0;
+    for (long long k = 1; k <= D; ++k) {
+        const long long z = (D + k - 1) / k;
+        if (z > 64) continue;
+        if (z < 12 && best >= 0.0) break;
+        const double waves = tiles * (double)k / slots;
+        const double fill = waves / std::ceil(waves);
+        const double score = fill * (1.0 - 0.7 / (double)z);
+        if (score > best + 1e-12) {
+            best = score;
+            best_z = (int)z;
+        }
+    }
+    return best_z;
 }
 
 void check_device() {
@@ -332,6 +362,7 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->domain) cudaFree(c->domain);
     if (c->host_cb) cudaFreeHost(c->host_cb);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->bwd_graph) cudaGraphExecDestroy(c->bwd_graph);
     if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
     dct_plan_destroy(c->plan);
     delete c;
@@ -758,6 +789,85 @@ tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const floa
     });
 }
 
+namespace {
+// The reverse sweep over every segment, last to first, then the u_0 = ubar_0 = f term.
+void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A, float* uta,
+                       float* const* va, float* grad_f, double* gp, cudaStream_t s) {
+    const size_t n = voxels(c->prm);
+    const uint32_t every = c->ckpt_every, K = c->ckpt_K;
+    std::vector<TgvFullDev> states(every + 1);
+    for (int seg = (int)c->ckpt_count - 1; seg >= 0; --seg) {
+        const uint32_t k0 = (uint32_t)seg * every, k1 = k0 + every < K ? k0 + every : K;
+        const int len = (int)(k1 - k0);
+        states[0] = full_state_at(c->ckpt_block, seg, n);
+        for (int j = 1; j < len; ++j) states[j] = full_state_at(c->seg_block, j - 1, n);
+        states[len] = full_state_at(c->ckpt_block, seg + 1, n);
+        for (int j = 0; j + 1 < len; ++j)
+            tgv_step_fp32(c->st, k, states[j], states[j + 1], c->step_cache, s);
+        tgv_adjoint_segment(c->st, k, states.data(), len, A, uta, va, grad_f, gp, s);
+    }
+    tgv_adjoint_finish(grad_f, A, n, s);
+}
+
+// The backward sweep as a CUDA graph (a few hundred launches of tens of microseconds
+// each at small volumes), captured on first use and replayed while the buffers, the
+// segmentation, the step and the z-chunk stay the same.  Null when capture fails; the
+// caller then runs the sweep directly.  The iteration kernel's shared-memory
+// attribute was set by the checkpointed forward that every backward follows.
+cudaGraphExec_t backward_graph(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A,
+                               float* uta, float* const* va, float* grad_f, double* gp) {
+    tgvdct_context::BwdKey key;
+    key.ckpt = c->ckpt_block;
+    key.seg = c->seg_block;
+    key.adj = c->adj_block;
+    key.every = c->ckpt_every;
+    key.K = c->ckpt_K;
+    key.count = c->ckpt_count;
+    key.zchunk = c->st.zchunk;
+    key.step = k;
+    const auto& o = c->bwd_key;
+    if (c->bwd_graph && o.ckpt == key.ckpt && o.seg == key.seg && o.adj == key.adj &&
+        o.every == key.every && o.K == key.K && o.count == key.count && o.zchunk == key.zchunk &&
+        same_step(o.step, k))
+        return c->bwd_graph;
+    if (c->bwd_graph) {
+        cudaGraphExecDestroy(c->bwd_graph);
+        c->bwd_graph = nullptr;
+    }
+    if (!c->capture_stream &&
+        cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    bool built = true;
+    try {
+        backward_segments(c, k, A, uta, va, grad_f, gp, c->capture_stream);
+    } catch (...) {
+        built = false;
+    }
+    const cudaError_t e = cudaStreamEndCapture(c->capture_stream, &g);
+    if (!built || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return nullptr;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->bwd_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        cudaGetLastError();
+        c->bwd_graph = nullptr;
+        return nullptr;
+    }
+    c->bwd_key = key;
+    return c->bwd_graph;
+}
+}  // namespace
+
 tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_dev,
                                        const float* grad_v_x_dev, const float* grad_v_y_dev,
                                        const float* grad_v_z_dev, float* grad_f_dev,
@@ -769,40 +879,39 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_de
         require_reverse_mode(c);
         cudaStream_t s = (cudaStream_t)stream;
         const size_t n = voxels(c->prm);
-        const uint32_t every = c->ckpt_every, K = c->ckpt_K;
+        const uint32_t every = c->ckpt_every;
         // a segment [k0, k1) reads S_k0 and S_k1 from the checkpoints and recomputes
         // the k1 - k0 - 1 states between them
         if (every > 1 &&
             ensure_block(&c->seg_block, &c->seg_bytes, (size_t)(every - 1) * tgv_full_state_bytes(n)))
             c->step_cache.reset();
+        // adjoint state, scratch a(u~) and a(v'), and the sweep's own d/df and
+        // d/d(lambda, alpha0, alpha1) (copied to the caller's buffers at the end, so a
+        // captured sweep does not depend on them)
         const size_t field = (n * 4 + 255) & ~size_t(255);
-        ensure_block(&c->adj_block, &c->adj_bytes, tgv_full_state_bytes(n) + 4 * field);
+        ensure_block(&c->adj_block, &c->adj_bytes, tgv_full_state_bytes(n) + 5 * field + 256);
         TgvFullDev A = full_state_at(c->adj_block, 0, n);
-        float* scratch = (float*)((char*)c->adj_block + tgv_full_state_bytes(n));
-        float* uta = scratch;
-        float* va[3] = {(float*)((char*)scratch + field), (float*)((char*)scratch + 2 * field),
-                        (float*)((char*)scratch + 3 * field)};
+        char* scratch = (char*)c->adj_block + tgv_full_state_bytes(n);
+        float* uta = (float*)scratch;
+        float* va[3] = {(float*)(scratch + field), (float*)(scratch + 2 * field),
+                        (float*)(scratch + 3 * field)};
+        float* gf = (float*)(scratch + 4 * field);
+        double* gp = (double*)(scratch + 5 * field);
         tgv_full_state_zero(A, n, s);
         if (grad_u_dev) TGV_CUDA(cudaMemcpyAsync(A.u, grad_u_dev, n * 4, cudaMemcpyDeviceToDevice, s));
         const float* gv[3] = {grad_v_x_dev, grad_v_y_dev, grad_v_z_dev};
         for (int a = 0; a < 3; ++a)
             if (gv[a]) TGV_CUDA(cudaMemcpyAsync(A.v[a], gv[a], n * 4, cudaMemcpyDeviceToDevice, s));
-        TGV_CUDA(cudaMemsetAsync(grad_f_dev, 0, n * 4, s));
-        TGV_CUDA(cudaMemsetAsync(grad_params_dev, 0, 3 * sizeof(double), s));
+        TGV_CUDA(cudaMemsetAsync(gf, 0, n * 4, s));
+        TGV_CUDA(cudaMemsetAsync(gp, 0, 3 * sizeof(double), s));
         const TgvStep k = step_of(c->prm);
-        std::vector<TgvFullDev> states(every + 1);
-        for (int seg = (int)c->ckpt_count - 1; seg >= 0; --seg) {
-            const uint32_t k0 = (uint32_t)seg * every, k1 = k0 + every < K ? k0 + every : K;
-            const int len = (int)(k1 - k0);
-            states[0] = full_state_at(c->ckpt_block, seg, n);
-            for (int j = 1; j < len; ++j) states[j] = full_state_at(c->seg_block, j - 1, n);
-            states[len] = full_state_at(c->ckpt_block, seg + 1, n);
-            for (int j = 0; j + 1 < len; ++j)
-                tgv_step_fp32(c->st, k, states[j], states[j + 1], c->step_cache, s);
-            tgv_adjoint_segment(c->st, k, states.data(), len, A, uta, va, grad_f_dev,
-                                grad_params_dev, s);
-        }
-        tgv_adjoint_finish(grad_f_dev, A, n, s);
+        if (cudaGraphExec_t g = backward_graph(c, k, A, uta, va, gf, gp))
+            TGV_CUDA(cudaGraphLaunch(g, s));
+        else
+            backward_segments(c, k, A, uta, va, gf, gp, s);
+        TGV_CUDA(cudaMemcpyAsync(grad_f_dev, gf, n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(grad_params_dev, gp, 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 s));
         return TGVDCT_OK;
     });
 }

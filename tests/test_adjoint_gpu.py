@@ -199,3 +199,39 @@ def test_deshade_gradient_through_the_shading_field(gpu_lib):
     h = 1e-6
     fd = (loss64(f + h * delta) - loss64(f - h * delta)) / (2 * h)
     assert abs(fd - float(np.sum(grad * delta))) <= 1e-4 * abs(fd), (fd, np.sum(grad * delta))
+
+
+def test_backward_graph_replay_and_rebuild(gpu_lib):
+    """The backward sweep is captured as a CUDA graph on a context's first backward and
+    replayed after; a new step (lambda) or a new checkpoint stride rebuilds it.  Every
+    call must give the gradient a fresh context gives."""
+    import torch
+    f = torch.from_numpy(np.log(tissue_phantom_3d(10, 12, 16, seed=15))).cuda()
+    gu = torch.from_numpy(np.random.default_rng(4).standard_normal((10, 12, 16))
+                          .astype(np.float32)).cuda()
+
+    def run(ctx, every):
+        u, vx, vy, vz, gf = (torch.empty_like(f) for _ in range(5))
+        gp = torch.empty(3, dtype=torch.float64, device="cuda")
+        ctx.forward_checkpointed_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(),
+                                     vz.data_ptr(), every)
+        ctx.backward_dev(gu.data_ptr(), None, None, None, gf.data_ptr(), gp.data_ptr())
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+        return gf.cpu().numpy(), gp.cpu().numpy()
+
+    def fresh(lam, every):
+        with pkg.Context(pkg.default_params(width=16, height=12, depth=10, iteration_count=24,
+                                            lambda_=lam)) as c:
+            return run(c, every)
+
+    ref1, ref2, ref3 = fresh(1.0, 5), fresh(0.7, 5), fresh(0.7, 3)
+    with pkg.Context(pkg.default_params(width=16, height=12, depth=10, iteration_count=24,
+                                        lambda_=1.0)) as ctx:
+        for want, (lam, every) in ((ref1, (1.0, 5)), (ref1, (1.0, 5)), (ref2, (0.7, 5)),
+                                   (ref3, (0.7, 3)), (ref3, (0.7, 3))):
+            ctx.set_params(pkg.default_params(width=16, height=12, depth=10,
+                                              iteration_count=24, lambda_=lam))
+            gf, gp = run(ctx, every)
+            assert np.array_equal(gf, want[0])
+            assert np.allclose(gp, want[1], rtol=1e-9, atol=0)
