@@ -447,8 +447,11 @@ def run_ours(args):
     # ---- e2e through the host-buffer C-ABI call (reference-facing)
     e2e_ms = None
     if not args.no_e2e:
-        fh = np.ascontiguousarray(f_host)
-        uo, lo, ro = (np.empty_like(fh) for _ in range(3))
+        # pinned host buffers (numpy views of page-locked torch tensors), as a caller
+        # streaming volumes through the library would hold them
+        pinned = [torch.from_numpy(np.ascontiguousarray(f_host)).pin_memory()]
+        pinned += [torch.empty(f_host.shape, dtype=torch.float32).pin_memory() for _ in range(3)]
+        fh, uo, lo, ro = (t.numpy() for t in pinned)
         times = []
         for k in range(args.e2e_steps + 1):
             torch.cuda.synchronize()
