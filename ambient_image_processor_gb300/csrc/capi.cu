@@ -97,11 +97,16 @@ void validate(const tgvdct_params* p) {
     TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
 }
 
+// The automatic choice: the fused z-marching pass for volumes; the two-pass kernels
+// for a single plane, where the fused pass has no planes to pipeline (at 512^2,
+// 1024^2 and 2048^2 the two passes take 6.2, 15.5 and 87 ms per 1000 iterations
+// against 11.0, 39.8 and 164 ms).  Every kernel gives the same bits.
 int kernel_of(const tgvdct_params& p) {
     switch (p.iteration_kernel) {
         case TGVDCT_KERNEL_TWO_PASS: return TGV_KERNEL_TWO_PASS;
         case TGVDCT_KERNEL_FUSED_REGISTER: return TGV_KERNEL_FUSED_REGISTER;
-        default: return TGV_KERNEL_FUSED;
+        case TGVDCT_KERNEL_FUSED: return TGV_KERNEL_FUSED;
+        default: return p.depth == 1 ? TGV_KERNEL_TWO_PASS : TGV_KERNEL_FUSED;
     }
 }
 
