@@ -19,7 +19,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_build", "libtgvdct.so")
 
 # enums of include/tgvdct.h
-OK, ERR_BAD_ARG, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, STOPPED = range(7)
+OK, ERR_BAD_ARG, ERR_OOM, ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, STOPPED, ERR_TIMEOUT = range(8)
 DATA_L1, DATA_L2 = 0, 1
 GEOMETRY_3D, GEOMETRY_2D = 0, 1
 STATE_FP32, STATE_BF16_DUAL, STATE_FX16_DUAL = 0, 1, 2
@@ -29,7 +29,8 @@ KERNEL_AUTO, KERNEL_TWO_PASS, KERNEL_FUSED, KERNEL_FUSED_REGISTER = 0, 1, 2, 3
 
 _STATUS_NAMES = {OK: "ok", ERR_BAD_ARG: "bad argument", ERR_OOM: "out of memory",
                  ERR_CUDA: "CUDA error", ERR_NO_DEVICE: "no suitable CUDA device",
-                 ERR_UNSUPPORTED: "unsupported mode", STOPPED: "stopped by callback"}
+                 ERR_UNSUPPORTED: "unsupported mode", STOPPED: "stopped early",
+                 ERR_TIMEOUT: "a bounded wait in a kernel ran out"}
 
 
 class TgvdctError(RuntimeError):
@@ -50,7 +51,9 @@ class Params(ctypes.Structure):
                 ("poisson_eigen", ctypes.c_int32),
                 ("paint_iteration_interval", ctypes.c_uint32),
                 ("callback_on_device", ctypes.c_int32),
-                ("iteration_kernel", ctypes.c_int32), ("z_chunk", ctypes.c_int32)]
+                ("iteration_kernel", ctypes.c_int32), ("z_chunk", ctypes.c_int32),
+                ("energy_check_interval", ctypes.c_uint32),
+                ("energy_tolerance", ctypes.c_float)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
@@ -114,6 +117,11 @@ _SIGS = {
     "tgvdct_process_tgv2_l1": [ctypes.POINTER(Params), _f32p, _vp, _i32, _i32, _i32, CALLBACK,
                                _vp, _f32p, _f32p, _f32p],
     "tgvdct_process_dev": [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+    "tgvdct_tgv2_energy": [ctypes.POINTER(Params), _f32p, _f32p, _f32p, _f32p, _vp,
+                           np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")],
+    "tgvdct_tgv2_energy_dev": [ctypes.POINTER(Params), _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "tgvdct_energy_history": [_vp, _vp, _u32, ctypes.POINTER(_u32)],
+    "tgvdct_request_stop": [_vp],
     "tgvdct_resize_bspline3": [_f32p, _u32, _u32, _u32, _f32p, _u32, _u32, _u32],
     "tgvdct_resize_bspline3_dev": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _u32, _vp],
     "tgvdct_resize_factor_extent": [_u32, _flt],
@@ -462,6 +470,24 @@ def tgv2_l1_deshade_masked_launch(f, mask, lambda_, iteration_count, alpha0, alp
     return u, vx, vy, vz
 
 
+def tgv2_energy(f, u, v_x, v_y, v_z=None, *, lambda_=1.0, alpha0=2.0, alpha1=1.0,
+                data_term=DATA_L1, geometry=None):
+    """TGV2 primal energy of (u, v) for f (tgvdct_tgv2_energy): returns
+    [lambda-weighted data term, alpha1 sum |F u - v|, alpha0 sum |E v|, total], FP64
+    sums of the FP32 per-voxel terms on the device.  No counterpart in the reference."""
+    f = _f32(f)
+    w, h, d = _dims(f)
+    if geometry is None:
+        geometry = GEOMETRY_2D if d == 1 and v_z is None else GEOMETRY_3D
+    p = default_params(width=w, height=h, depth=d, lambda_=lambda_, alpha0=alpha0,
+                       alpha1=alpha1, data_term=data_term, geometry=geometry)
+    out = np.zeros(4, dtype=np.float64)
+    vz = None if v_z is None else _f32(v_z)
+    _check(lib().tgvdct_tgv2_energy(ctypes.byref(p), f, _f32(u), _f32(v_x), _f32(v_y),
+                                    None if vz is None else vz.ctypes.data_as(_vp), out))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # Down-sampled deshade (reference: resize/ResizeProcessor.cpp,
 # tgvk_deshade_downsampled/TGVKDeshadeDownsampled*Processor.cpp)
@@ -643,6 +669,20 @@ class Context:
         """Restrict the loop to voxels with mask >= 1 (None clears); see
         tgvdct_set_domain_mask_dev."""
         _check(lib().tgvdct_set_domain_mask_dev(self._ctx, mask_ptr, stream), allow_stop=False)
+
+    def energy_history(self) -> np.ndarray:
+        """The weighted TGV2 energies of the last loop's energy checks, in order."""
+        n = _u32()
+        _check(lib().tgvdct_energy_history(self._ctx, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        if n.value:
+            _check(lib().tgvdct_energy_history(self._ctx, out.ctypes.data_as(_vp), n.value,
+                                               ctypes.byref(n)))
+        return out
+
+    def request_stop(self):
+        """Ask the loop running on this context (or the next one) to stop; thread-safe."""
+        _check(lib().tgvdct_request_stop(self._ctx))
 
     def check_device_error(self, stream=None):
         _check(lib().tgvdct_check_device_error(self._ctx, stream), allow_stop=False)

@@ -1,6 +1,7 @@
 // C ABI of the TGV-DCT path (include/tgvdct.h): contexts, status codes, the
 // iteration loop with its callback, and the host-buffer drop-in launchers.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -23,6 +24,10 @@ struct tgvdct_context {
     void* state_block = nullptr;
     DctPlan* plan = nullptr;
     uint32_t iterations_run = 0;
+    // stopping: a request from any thread, and the energy checks of the last loop
+    std::atomic<bool> stop_requested{false};
+    double* energy_dev = nullptr;  // 3 sums of one energy evaluation
+    std::vector<double> energy_history;
     // pinned host buffers for callbacks that receive host copies
     float* host_cb = nullptr;
     size_t host_cb_count = 0;
@@ -95,6 +100,8 @@ void validate(const tgvdct_params* p) {
                     p->iteration_kernel <= TGVDCT_KERNEL_FUSED_REGISTER,
                 "unknown iteration kernel");
     TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
+    TGV_REQUIRE(p->energy_tolerance >= 0.f && std::isfinite(p->energy_tolerance),
+                "energy_tolerance must be finite and >= 0");
 }
 
 // The automatic choice: the fused z-marching pass for volumes; the two-pass kernels
@@ -281,21 +288,47 @@ cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
 // `on_iteration` decides what a callback sees; returns true if stopped.  Stretches
 // of kGraphChunk iterations with no callback due run as one CUDA graph replay (the
 // small-volume loops are launch-bound otherwise).
+// The weighted primal energy of the loop's current (u, v) (synchronous).
+double state_energy(tgvdct_context* c, cudaStream_t s) {
+    if (!c->energy_dev) TGV_CUDA(cudaMalloc(&c->energy_dev, 3 * sizeof(double)));
+    const auto& p = c->prm;
+    tgv_energy_terms(c->st.f, c->st.u, c->st.v[0], c->st.v[1], c->st.v[2], (int)p.width,
+                     (int)p.height, (int)p.depth, c->st.three, p.data_term, c->energy_dev, s);
+    double h[3];
+    TGV_CUDA(cudaMemcpyAsync(h, c->energy_dev, sizeof(h), cudaMemcpyDeviceToHost, s));
+    TGV_CUDA(cudaStreamSynchronize(s));
+    return (double)p.lambda * h[0] + (double)p.alpha1 * h[1] + (double)p.alpha0 * h[2];
+}
+
+// The iteration loop on the context's state (st.f already holds the input).
+// `on_iteration` decides what a callback sees; returns true if stopped.  Stretches
+// of kGraphChunk iterations with no callback or energy check due run as one CUDA
+// graph replay (the small-volume loops are launch-bound otherwise).  A stop request
+// is honoured between host-side steps; the energy test after its checks.
 template <class OnIteration>
 bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration) {
     const TgvStep k = step_of(c->prm);
     tgv_state_init(c->st, s);
     const uint32_t n_it = c->prm.iteration_count, paint = c->prm.paint_iteration_interval;
+    const uint32_t check = c->prm.energy_check_interval;
+    const double tol = c->prm.energy_tolerance;
     const bool cb_on = have_cb && paint > 0;
+    auto next_multiple = [](uint32_t it, uint32_t m) {
+        return (it % m == 0) ? it : (it / m + 1) * m;
+    };
     c->iterations_run = 0;
+    c->energy_history.clear();
     for (uint32_t it = 0; it < n_it;) {
-        // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384)
+        if (c->stop_requested.exchange(false)) {
+            c->iterations_run = it;
+            return true;
+        }
+        // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384),
+        // energy checks after iterations j > 0 with j % check == 0
         if (it > 0 && it + kGraphChunk <= n_it) {
             bool due = false;
-            if (cb_on) {
-                const uint32_t next = (it % paint == 0) ? it : (it / paint + 1) * paint;
-                due = next < it + kGraphChunk;
-            }
+            if (cb_on) due = next_multiple(it, paint) < it + kGraphChunk;
+            if (check > 0) due = due || next_multiple(it, check) < it + kGraphChunk;
             if (!due) {
                 if (cudaGraphExec_t g = loop_graph(c, k)) {
                     TGV_CUDA(cudaGraphLaunch(g, s));
@@ -307,6 +340,16 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
         tgv_iterate(c->st, k, s);
         if (cb_on && it > 0 && it % paint == 0) {
             if (on_iteration(it)) {
+                c->iterations_run = it + 1;
+                return true;
+            }
+        }
+        if (check > 0 && it > 0 && it % check == 0) {
+            const double e = state_energy(c, s);
+            const bool settled = tol > 0.0 && !c->energy_history.empty() &&
+                                 std::fabs(e - c->energy_history.back()) <= tol * std::fabs(e);
+            c->energy_history.push_back(e);
+            if (settled) {
                 c->iterations_run = it + 1;
                 return true;
             }
@@ -326,7 +369,7 @@ void check_tgv_flag(tgvdct_context* c, cudaStream_t s) {
     if (h) {
         TGV_CUDA(cudaMemsetAsync(c->st.err, 0, sizeof(int), s));
         set_error("a TGV iteration kernel timed out waiting on its load pipeline");
-        throw Error{TGVDCT_ERR_CUDA};
+        throw Error{TGVDCT_ERR_TIMEOUT};
     }
 }
 
@@ -368,6 +411,7 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->host_cb) cudaFreeHost(c->host_cb);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->bwd_graph) cudaGraphExecDestroy(c->bwd_graph);
+    if (c->energy_dev) cudaFree(c->energy_dev);
     if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
     dct_plan_destroy(c->plan);
     delete c;
@@ -643,7 +687,7 @@ tgvdct_status with_plan(uint32_t w, uint32_t h, uint32_t d, Body&& body) {
         TGV_CUDA(cudaStreamSynchronize(0));
         if (!dct_tc_check(plan, 0)) {
             set_error("a tensor-core DCT pass timed out waiting on its pipeline");
-            return TGVDCT_ERR_CUDA;
+            return TGVDCT_ERR_TIMEOUT;
         }
         return TGVDCT_OK;
     });
@@ -662,7 +706,8 @@ const char* tgvdct_status_string(tgvdct_status s) {
         case TGVDCT_ERR_CUDA: return "CUDA error";
         case TGVDCT_ERR_NO_DEVICE: return "no suitable CUDA device";
         case TGVDCT_ERR_UNSUPPORTED: return "unsupported mode";
-        case TGVDCT_STOPPED: return "stopped by the iteration callback";
+        case TGVDCT_STOPPED: return "stopped before the iteration count";
+        case TGVDCT_ERR_TIMEOUT: return "a bounded wait in a kernel ran out";
     }
     return "unknown status";
 }
@@ -1226,7 +1271,7 @@ tgvdct_status tgvdct_check_device_error(tgvdct_context* c, void* stream) {
         check_tgv_flag(c, (cudaStream_t)stream);
         if (c->plan && !dct_tc_check(c->plan, (cudaStream_t)stream)) {
             set_error("a tensor-core DCT pass timed out waiting on its pipeline");
-            return TGVDCT_ERR_CUDA;
+            return TGVDCT_ERR_TIMEOUT;
         }
         TGV_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
         return TGVDCT_OK;
@@ -1487,7 +1532,7 @@ tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host
         check_tgv_flag(c, s);
         if (c->plan && !dct_tc_check(c->plan, s)) {
             set_error("a tensor-core DCT pass timed out waiting on its pipeline");
-            return TGVDCT_ERR_CUDA;
+            return TGVDCT_ERR_TIMEOUT;
         }
         return c->iterations_run < p->iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
     });
@@ -1603,6 +1648,82 @@ tgvdct_status tgvdct_process_tgvk_l1_downsampled(
         if (div_v_host) TGV_CUDA(cudaMemcpy(div_v_host, dv.p, n * 4, cudaMemcpyDeviceToHost));
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
+}
+
+namespace {
+void check_energy_args(const tgvdct_params* p) {
+    validate(p);
+    TGV_REQUIRE(p->lambda >= 0.f && p->alpha0 >= 0.f && p->alpha1 >= 0.f,
+                "energy weights must be >= 0");
+}
+bool energy_three(const tgvdct_params* p) { return p->geometry != TGVDCT_GEOMETRY_2D; }
+}  // namespace
+
+tgvdct_status tgvdct_tgv2_energy_dev(const tgvdct_params* p, const float* f_dev,
+                                     const float* u_dev, const float* v_x_dev,
+                                     const float* v_y_dev, const float* v_z_dev,
+                                     double* energy_dev, void* stream) {
+    return guarded([&] {
+        check_energy_args(p);
+        const bool three = energy_three(p);
+        TGV_REQUIRE(f_dev && u_dev && v_x_dev && v_y_dev && (v_z_dev || !three) && energy_dev,
+                    "null device buffer");
+        check_device();
+        tgv_energy_terms(f_dev, u_dev, v_x_dev, v_y_dev, three ? v_z_dev : nullptr,
+                         (int)p->width, (int)p->height, (int)p->depth, three, p->data_term,
+                         energy_dev, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_energy(const tgvdct_params* p, const float* f_host,
+                                 const float* u_host, const float* v_x_host,
+                                 const float* v_y_host, const float* v_z_host, double* energy) {
+    return guarded([&] {
+        check_energy_args(p);
+        const bool three = energy_three(p);
+        TGV_REQUIRE(f_host && u_host && v_x_host && v_y_host && (v_z_host || !three) && energy,
+                    "null host buffer");
+        check_device();
+        const size_t n = voxels(*p);
+        DevBuf f(n), u(n), vx(n), vy(n), vz(three ? n : 0), sums(2 * 3);
+        TGV_CUDA(cudaMemcpy(f.p, f_host, n * 4, cudaMemcpyHostToDevice));
+        TGV_CUDA(cudaMemcpy(u.p, u_host, n * 4, cudaMemcpyHostToDevice));
+        TGV_CUDA(cudaMemcpy(vx.p, v_x_host, n * 4, cudaMemcpyHostToDevice));
+        TGV_CUDA(cudaMemcpy(vy.p, v_y_host, n * 4, cudaMemcpyHostToDevice));
+        if (three) TGV_CUDA(cudaMemcpy(vz.p, v_z_host, n * 4, cudaMemcpyHostToDevice));
+        double* d = (double*)sums.p;
+        tgv_energy_terms(f.p, u.p, vx.p, vy.p, three ? vz.p : nullptr, (int)p->width,
+                         (int)p->height, (int)p->depth, three, p->data_term, d, 0);
+        double h[3];
+        TGV_CUDA(cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost));
+        energy[0] = (double)p->lambda * h[0];
+        energy[1] = (double)p->alpha1 * h[1];
+        energy[2] = (double)p->alpha0 * h[2];
+        energy[3] = energy[0] + energy[1] + energy[2];
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_energy_history(tgvdct_context* c, double* out, uint32_t capacity,
+                                    uint32_t* count) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(count != nullptr && (out != nullptr || capacity == 0), "null output");
+        const size_t m = c->energy_history.size();
+        *count = (uint32_t)m;
+        for (size_t i = 0; i < m && i < capacity; ++i) out[i] = c->energy_history[i];
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_request_stop(tgvdct_context* c) {
+    if (!c) {
+        tgvdct::set_error("null context");
+        return TGVDCT_ERR_BAD_ARG;
+    }
+    c->stop_requested.store(true);
+    return TGVDCT_OK;
 }
 
 }  // extern "C"

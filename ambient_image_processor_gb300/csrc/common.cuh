@@ -141,6 +141,14 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
 // grad_f += a(u_0) + a(ubar_0) (the loop starts from u = ubar = f).
 void tgv_adjoint_finish(float* grad_f, const TgvFullDev& A, size_t n, cudaStream_t st);
 
+// ---- TGV2 primal energy (metrics.cu) ------------------------------------------------
+// sums[0..2] = sum |u - f| (L1) or (u - f)^2 / 2 (L2), sum |F u - v|, sum |E v|_F over
+// every voxel (FP64 sums of FP32 terms); the energy is lambda sums[0] + alpha1 sums[1]
+// + alpha0 sums[2].  vz is unused when !three.
+void tgv_energy_terms(const float* f, const float* u, const float* vx, const float* vy,
+                      const float* vz, int W, int H, int D, bool three, int data_term,
+                      double* sums, cudaStream_t st);
+
 // ---- cubic B-spline resize (resize.cu) -------------------------------------------
 // ceil(n * factor) in float, at least 1: ResizeProcessor::process(image, factor).
 unsigned resize_factor_extent(unsigned n, float factor);

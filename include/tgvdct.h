@@ -43,8 +43,14 @@ typedef enum tgvdct_status {
     TGVDCT_ERR_CUDA = 3,        /* a CUDA runtime call or kernel launch failed */
     TGVDCT_ERR_NO_DEVICE = 4,   /* no CUDA device, or not an sm_103 device */
     TGVDCT_ERR_UNSUPPORTED = 5, /* a mode this build does not provide */
-    TGVDCT_STOPPED = 6          /* the iteration callback asked to stop; outputs hold
-                                   the state after the iteration it was called for */
+    TGVDCT_STOPPED = 6,         /* the loop ended early: the iteration callback or
+                                   tgvdct_request_stop asked to stop, or the energy
+                                   tolerance was met; outputs hold the state after
+                                   the last iteration run (tgvdct_iterations_run) */
+    TGVDCT_ERR_TIMEOUT = 7      /* a bounded wait inside a kernel ran out (a TMA
+                                   pipeline stage that never landed); the kernel
+                                   returned without finishing and the context is
+                                   still usable */
 } tgvdct_status;
 
 typedef enum tgvdct_data_term {
@@ -120,6 +126,15 @@ typedef struct tgvdct_params {
                                           behaviour); 1: device pointers */
     int32_t iteration_kernel;          /* tgvdct_iteration_kernel */
     int32_t z_chunk;                   /* planes per block of the fused kernel; 0 = auto */
+    /* Stopping on the primal energy (no counterpart in the reference, which always
+       runs iteration_count iterations): every energy_check_interval iterations
+       (0 = never) the loop evaluates the TGV2 energy of (u, v) (tgvdct_tgv2_energy)
+       and, when energy_tolerance > 0, stops after the first check whose energy
+       differs from the previous check's by at most energy_tolerance x |energy|.  The
+       call then returns TGVDCT_STOPPED; tgvdct_iterations_run gives the count and
+       tgvdct_energy_history the energies. */
+    uint32_t energy_check_interval;
+    float energy_tolerance;
 } tgvdct_params;
 
 /* Called after iteration `iteration_index` when iteration_index > 0 and
@@ -405,6 +420,36 @@ tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
     float lambda, uint32_t iteration_count, uint32_t paint_iteration_interval,
     int cuda_block_dimension, tgvdct_iteration_callback callback, void* user, float alpha0,
     float alpha1, float* u_host, float* v_x_host, float* v_y_host, float* v_z_host);
+
+/* ---- energy, stopping ------------------------------------------------------------ */
+/* TGV2 primal energy of (u, v) for f with p's shape, geometry, data term and weights,
+   using the operators as the reference implements them: F forward differences with
+   Neumann ends, E from the negated backward differences with 1/2 on the mixed
+   entries, Frobenius norm with weight 2 off the diagonal (tgv2_common.cu:96-276).
+   energy[0] = lambda sum |u - f| (L1) or lambda sum (u - f)^2 / 2 (L2),
+   energy[1] = alpha1 sum |F u - v|, energy[2] = alpha0 sum |E v|, energy[3] = their
+   sum.  FP32 per voxel, FP64 sums on the device.  No counterpart in the reference.
+   v_z may be NULL for 2-D geometry.  Host buffers; energy is host memory. */
+tgvdct_status tgvdct_tgv2_energy(const tgvdct_params* p, const float* f_host,
+                                 const float* u_host, const float* v_x_host,
+                                 const float* v_y_host, const float* v_z_host, double* energy);
+/* Device form: f, u, v device buffers; energy_dev receives the 3 unweighted sums
+   (sum |u - f| or sum (u - f)^2 / 2, sum |F u - v|, sum |E v|).  Stream-ordered. */
+tgvdct_status tgvdct_tgv2_energy_dev(const tgvdct_params* p, const float* f_dev,
+                                     const float* u_dev, const float* v_x_dev,
+                                     const float* v_y_dev, const float* v_z_dev,
+                                     double* energy_dev, void* stream);
+/* The energies (weighted totals) of the energy checks of the context's last loop, in
+   order; *count receives how many there were (at most capacity are copied). */
+tgvdct_status tgvdct_energy_history(tgvdct_context* ctx, double* out, uint32_t capacity,
+                                    uint32_t* count);
+/* Asks the loop running on ctx (or the next one started on it) to stop: it is polled
+   between host-side launch steps (every iteration, or every 32 iterations where the
+   loop replays them as one CUDA graph) and at callback and energy checks.  Safe to
+   call from another thread.  The call that stops returns TGVDCT_STOPPED and clears
+   the request.  No counterpart in the reference (whose callback return is the only
+   way to stop). */
+tgvdct_status tgvdct_request_stop(tgvdct_context* ctx);
 
 /* ---- down-sampled deshade (tgvk_deshade_downsampled/, resize/) ---------------- */
 /* Replaces ResizeProcessor::process(image, width, height, depth, BSpline3)
