@@ -122,6 +122,10 @@ _SIGS = {
     "tgvdct_tgv2_energy_dev": [ctypes.POINTER(Params), _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_energy_history": [_vp, _vp, _u32, ctypes.POINTER(_u32)],
     "tgvdct_request_stop": [_vp],
+    "tgvdct_state_bytes": [_vp],
+    "tgvdct_state_save_dev": [_vp, _vp, _vp],
+    "tgvdct_state_load_dev": [_vp, _vp, _vp],
+    "tgvdct_tgv2_resume_dev": [_vp, _vp, _vp, _vp, _vp, CALLBACK, _vp, _vp],
     "tgvdct_resize_bspline3": [_f32p, _u32, _u32, _u32, _f32p, _u32, _u32, _u32],
     "tgvdct_resize_bspline3_dev": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _u32, _vp],
     "tgvdct_resize_factor_extent": [_u32, _flt],
@@ -135,7 +139,8 @@ _SIGS = {
 _RESTYPES = {"tgvdct_params_init": None, "tgvdct_workspace_bytes": ctypes.c_size_t,
              "tgvdct_iterations_run": ctypes.c_uint32, "tgvdct_version": ctypes.c_char_p,
              "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p,
-             "tgvdct_resize_factor_extent": ctypes.c_uint32}
+             "tgvdct_resize_factor_extent": ctypes.c_uint32,
+             "tgvdct_state_bytes": ctypes.c_size_t}
 
 # symbols of include/tgvdct.h (checked by the CPU test suite)
 EXPORTED = sorted(set(_SIGS) | {"tgvdct_version", "tgvdct_last_error", "tgvdct_status_string"})
@@ -679,6 +684,21 @@ class Context:
             _check(lib().tgvdct_energy_history(self._ctx, out.ctypes.data_as(_vp), n.value,
                                                ctypes.byref(n)))
         return out
+
+    def state_bytes(self) -> int:
+        return int(lib().tgvdct_state_bytes(self._ctx))
+
+    def save_state_dev(self, dst_ptr, stream=None):
+        """Snapshot of the loop state into a device buffer of state_bytes()."""
+        _check(lib().tgvdct_state_save_dev(self._ctx, dst_ptr, stream), allow_stop=False)
+
+    def load_state_dev(self, src_ptr, stream=None):
+        _check(lib().tgvdct_state_load_dev(self._ctx, src_ptr, stream), allow_stop=False)
+
+    def resume_dev(self, u_ptr, vx_ptr, vy_ptr, vz_ptr=None, stream=None, callback=None) -> int:
+        """iteration_count more iterations from the current state."""
+        return _check(lib().tgvdct_tgv2_resume_dev(self._ctx, u_ptr, vx_ptr, vy_ptr, vz_ptr,
+                                                   callback or CALLBACK(), None, stream))
 
     def request_stop(self):
         """Ask the loop running on this context (or the next one) to stop; thread-safe."""

@@ -306,9 +306,11 @@ double state_energy(tgvdct_context* c, cudaStream_t s) {
 // graph replay (the small-volume loops are launch-bound otherwise).  A stop request
 // is honoured between host-side steps; the energy test after its checks.
 template <class OnIteration>
-bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration) {
+bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration,
+              bool from_initial_state = true) {
+    NvtxRange range("tgvdct loop");
     const TgvStep k = step_of(c->prm);
-    tgv_state_init(c->st, s);
+    if (from_initial_state) tgv_state_init(c->st, s);
     const uint32_t n_it = c->prm.iteration_count, paint = c->prm.paint_iteration_interval;
     const uint32_t check = c->prm.energy_check_interval;
     const double tol = c->prm.energy_tolerance;
@@ -490,6 +492,7 @@ struct DevBuf {
 void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_dev, bool clamp,
                        bool add_back, bool log_domain, float* u_dev, float* l_dev, float* r_dev,
                        tgvdct_iteration_callback cb, void* user, cudaStream_t s) {
+    NvtxRange range("tgvdct deshade");
     const size_t n = voxels(c->prm);
     TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
     if (log_domain) log_inplace(c->st.f, n, s);
@@ -534,6 +537,7 @@ bool downsampled_on_device(const float* f, const float* mask, uint32_t w, uint32
                            uint32_t paint_interval, bool clamp, bool add_back, bool not_masked,
                            tgvdct_iteration_callback cb, void* user, float* u_out, float* l_out,
                            float* r_out, float* divv_out, cudaStream_t s) {
+    NvtxRange range("tgvdct downsampled deshade");
     const size_t n = (size_t)w * h * d;
     const bool same = factor == 1.f;  // the reference skips both resizes (:65-66, :105-106)
     const uint32_t W = same ? w : resize_factor_extent(w, factor);
@@ -799,6 +803,57 @@ tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* c, const float* f_dev, float* 
     });
 }
 
+size_t tgvdct_state_bytes(const tgvdct_context* c) {
+    return c ? tgv_snapshot_bytes(c->st) : 0;
+}
+
+tgvdct_status tgvdct_state_save_dev(tgvdct_context* c, void* dst_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(dst_dev != nullptr, "null device buffer");
+        tgv_snapshot_save(c->st, dst_dev, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_state_load_dev(tgvdct_context* c, const void* src_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(src_dev != nullptr, "null device buffer");
+        tgv_snapshot_load(c->st, src_dev, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* c, float* u_dev, float* v_x_dev,
+                                     float* v_y_dev, float* v_z_dev,
+                                     tgvdct_iteration_callback cb, void* user, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(u_dev && v_x_dev && v_y_dev, "null device buffer");
+        TGV_REQUIRE(v_z_dev || !c->st.three, "v_z is required for 3-D geometry");
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t n = voxels(c->prm);
+        const bool stopped = run_loop(
+            c, s, cb != nullptr,
+            [&](uint32_t it) {
+                return deliver(c, cb, user, it, c->st.u, c->st.v[0], c->st.v[1],
+                               c->st.three ? c->st.v[2] : nullptr, s) != 0;
+            },
+            false);
+        TGV_CUDA(cudaMemcpyAsync(u_dev, c->st.u, n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(v_x_dev, c->st.v[0], n * 4, cudaMemcpyDeviceToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(v_y_dev, c->st.v[1], n * 4, cudaMemcpyDeviceToDevice, s));
+        if (v_z_dev) {
+            if (c->st.three)
+                TGV_CUDA(cudaMemcpyAsync(v_z_dev, c->st.v[2], n * 4, cudaMemcpyDeviceToDevice, s));
+            else
+                TGV_CUDA(cudaMemsetAsync(v_z_dev, 0, n * 4, s));
+        }
+        return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
 tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const float* f_dev,
                                                    float* u_dev, float* v_x_dev,
                                                    float* v_y_dev, float* v_z_dev,
@@ -843,6 +898,7 @@ namespace {
 // The reverse sweep over every segment, last to first, then the u_0 = ubar_0 = f term.
 void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A, float* uta,
                        float* const* va, float* grad_f, double* gp, cudaStream_t s) {
+    NvtxRange range("tgvdct reverse sweep");
     const size_t n = voxels(c->prm);
     const uint32_t every = c->ckpt_every, K = c->ckpt_K;
     std::vector<TgvFullDev> states(every + 1);

@@ -9,6 +9,8 @@
 #include <memory>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "tgvdct.h"
 
 namespace tgvdct {
@@ -51,6 +53,15 @@ struct TgvStencilFields {
 };
 
 enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
+
+// An NVTX range over a host-side phase (deshade, loop, Poisson integration, resize,
+// reverse sweep), for profilers that show ranges; free when none is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // cudaFuncAttributeMaxDynamicSharedMemorySize is per device: raise it for `kern` once
 // on every device that launches it (`done` holds one bit per device ordinal).
@@ -103,6 +114,11 @@ void tgv_state_bind(TgvState& s, char* base);
 void tgv_state_init(TgvState& s, cudaStream_t st);
 // domain[i] = mask[i] >= 1 (the masked processor's test, TGVDeshadeMaskedProcessor.cpp:347).
 void build_domain(const float* mask, size_t n, uint8_t* domain, cudaStream_t st);
+// Snapshot of the whole loop state (f, u, v, and the current stencil set ubar, vbar,
+// p, q) into or out of one contiguous device buffer of tgv_snapshot_bytes.
+size_t tgv_snapshot_bytes(const TgvState& s);
+void tgv_snapshot_save(const TgvState& s, void* dst, cudaStream_t st);
+void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st);
 // One primal-dual iteration (advances s.cur for the fused kernel).
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.

@@ -571,6 +571,7 @@ void poisson_solve(DctPlan* p, const float* rhs, float* l, int dct_mode, int eig
 
 void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float* vz, float* l,
                        int dct_mode, int eigen_mode, cudaStream_t st) {
+    NvtxRange range("tgvdct poisson integration");
     check_mode(p, dct_mode);
     const int epi = eigen_mode == TGVDCT_EIGEN_ACCURATE ? EPI_POISSON_ACC : EPI_POISSON_REF;
     const float s = (float)(1.0 / ((double)p->W * p->H * p->D * 8.0));

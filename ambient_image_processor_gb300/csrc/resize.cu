@@ -259,6 +259,7 @@ size_t resize_scratch_bytes(int w, int h, int d, int W, int H, int D) {
 
 void resize_bspline3(const float* in, int w, int h, int d, float* out, int W, int H, int D,
                      void* scratch, cudaStream_t st) {
+    NvtxRange range("tgvdct resize");
     TGV_REQUIRE(w >= 1 && h >= 1 && d >= 1 && W >= 1 && H >= 1 && D >= 1,
                 "resize extents must be >= 1");
     const bool up = W > w || H > h || D > d;

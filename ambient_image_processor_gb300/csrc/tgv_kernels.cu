@@ -1602,6 +1602,55 @@ void tgv_save_state(const TgvState& s, const TgvFullDev& out, cudaStream_t st) {
         TGV_CUDA(cudaMemcpyAsync(out.q[c], F.q[c], b, cudaMemcpyDeviceToDevice, st));
 }
 
+namespace {
+// The fields of a snapshot, in order: f, u, v[..] (FP32), then ubar, vbar[..] (FP32),
+// p[..], q[..] (dual element size) of stencil set `set`; only the allocated ones.
+template <class Fn>
+void for_each_snapshot_field(const TgvState& s, int set, Fn&& fn) {
+    const size_t n = (size_t)s.W * s.H * s.D, e = elem_bytes(s.precision);
+    const TgvStencilFields& F = s.set[set];
+    fn((void*)s.f, n * 4);
+    fn((void*)s.u, n * 4);
+    for (int k = 0; k < 3; ++k)
+        if (s.v[k]) fn((void*)s.v[k], n * 4);
+    fn((void*)F.ubar, n * 4);
+    for (int k = 0; k < 3; ++k)
+        if (F.vbar[k]) fn((void*)F.vbar[k], n * 4);
+    for (int k = 0; k < 3; ++k)
+        if (F.p[k]) fn((void*)F.p[k], n * e);
+    for (int k = 0; k < 6; ++k)
+        if (F.q[k]) fn((void*)F.q[k], n * e);
+}
+}  // namespace
+
+size_t tgv_snapshot_bytes(const TgvState& s) {
+    size_t b = 0;
+    for_each_snapshot_field(s, 0, [&](void*, size_t bytes) { b += bytes; });
+    return b;
+}
+
+void tgv_snapshot_save(const TgvState& s, void* dst, cudaStream_t st) {
+    char* d = (char*)dst;
+    for_each_snapshot_field(s, s.cur, [&](void* field, size_t bytes) {
+        TGV_CUDA(cudaMemcpyAsync(d, field, bytes, cudaMemcpyDeviceToDevice, st));
+        d += bytes;
+    });
+}
+
+void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st) {
+    // both stencil sets get the snapshot (a masked run reads the frozen outside
+    // values from either set), and the loop continues from set 0
+    for (int set = 0; set < 2; ++set) {
+        if (!s.set[set].ubar) continue;
+        const char* p = (const char*)src;
+        for_each_snapshot_field(s, set, [&](void* field, size_t bytes) {
+            TGV_CUDA(cudaMemcpyAsync(field, p, bytes, cudaMemcpyDeviceToDevice, st));
+            p += bytes;
+        });
+    }
+    s.cur = 0;
+}
+
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     if (tma_shape_ok(s)) {
         TGV_REQUIRE(s.err != nullptr, "TMA kernel needs a device error flag");

@@ -451,6 +451,26 @@ tgvdct_status tgvdct_energy_history(tgvdct_context* ctx, double* out, uint32_t c
    way to stop). */
 tgvdct_status tgvdct_request_stop(tgvdct_context* ctx);
 
+/* ---- checkpoint / resume (no counterpart in the reference, which cannot resume) - */
+/* Bytes of one snapshot of a context's loop state: f, u, v and the current ubar,
+   vbar, p, q (p, q in the context's dual storage precision). */
+size_t tgvdct_state_bytes(const tgvdct_context* ctx);
+/* Copies the loop state left by the last run (or load) into dst_dev, a device buffer
+   of tgvdct_state_bytes.  Stream-ordered. */
+tgvdct_status tgvdct_state_save_dev(tgvdct_context* ctx, void* dst_dev, void* stream);
+/* Replaces the context's loop state by a snapshot saved from a context with the same
+   shape, geometry and dual precision.  Stream-ordered. */
+tgvdct_status tgvdct_state_load_dev(tgvdct_context* ctx, const void* src_dev, void* stream);
+/* Runs the context's iteration_count more iterations from its current state (after
+   a run, or a load) instead of from u = f, p = q = v = 0, and writes u and v as
+   tgvdct_tgv2_run_dev does.  A run of K1 iterations, then a resume of K2, gives the
+   bits of one run of K1 + K2.  Callback and energy-check indices count from the
+   start of the resumed run. */
+tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* ctx, float* u_dev, float* v_x_dev,
+                                     float* v_y_dev, float* v_z_dev,
+                                     tgvdct_iteration_callback callback, void* user,
+                                     void* stream);
+
 /* ---- down-sampled deshade (tgvk_deshade_downsampled/, resize/) ---------------- */
 /* Replaces ResizeProcessor::process(image, width, height, depth, BSpline3)
    (resize/ResizeProcessor.cpp:49-143): ITK's cubic B-spline resample as that function
