@@ -123,6 +123,7 @@ _SIGS = {
     "tgvdct_energy_history": [_vp, _vp, _u32, ctypes.POINTER(_u32)],
     "tgvdct_request_stop": [_vp],
     "tgvdct_state_bytes": [_vp],
+    "tgvdct_bounds_check": [ctypes.POINTER(ctypes.c_uint64)],
     "tgvdct_state_save_dev": [_vp, _vp, _vp],
     "tgvdct_state_load_dev": [_vp, _vp, _vp],
     "tgvdct_tgv2_resume_dev": [_vp, _vp, _vp, _vp, _vp, CALLBACK, _vp, _vp],
@@ -165,6 +166,27 @@ def lib() -> ctypes.CDLL:
         L.tgvdct_status_string.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+_lib_checked = None
+
+
+def lib_checked() -> ctypes.CDLL:
+    """The bounds-checking build of the library (libtgvdct_checked.so), compiled on
+    first use; same entry points as lib(), plus a working tgvdct_bounds_check."""
+    global _lib_checked
+    if _lib_checked is None:
+        from . import build as _build
+        path = _build.build(checked=True)
+        L = ctypes.CDLL(path)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        L.tgvdct_last_error.restype = ctypes.c_char_p
+        L.tgvdct_last_error.argtypes = []
+        _lib_checked = L
+    return _lib_checked
 
 
 def version() -> str:

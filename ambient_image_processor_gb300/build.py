@@ -26,6 +26,8 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libtgvdct.so")
 REFAPI = os.path.join(PKG, "refapi")
 REFAPI_LIB = os.path.join(OUT, "libtgvdct_refapi.so")
+OUT_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(OUT_CHECKED, "libtgvdct_checked.so")
 CLI = os.path.join(OUT, "tgv2_deshade_application")
 CONVERGENCE_CLI = os.path.join(OUT, "tgv2_deshade_convergence_test_application")
 DOWNSAMPLED_CLI = os.path.join(OUT, "tgvk_deshade_downsampled_application")
@@ -76,25 +78,33 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False, jobs: int = 8) -> str:
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, jobs: int = 8,
+          checked: bool = False) -> str:
+    """Compile libtgvdct.so and the host tools; with checked=True, instead compile
+    libtgvdct_checked.so (kernels with bounds checks, -DTGV_CHECK_BOUNDS) into
+    _build_checked/."""
+    out = OUT_CHECKED if checked else OUT
+    lib = LIB_CHECKED if checked else LIB
+    os.makedirs(out, exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     headers.append(os.path.join(INCLUDE, "tgvdct.h"))
     objs, cmds = [], []
     for unit, extra in UNITS.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(OUT, unit + ".o")
+        obj = os.path.join(out, unit + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, *headers, __file__]):
-            cmds.append([nvcc(), *ARCH, *NVCC_COMMON, *extra, "-c", src, "-o", obj])
+            flags = [*extra, "-DTGV_CHECK_BOUNDS"] if checked else extra
+            cmds.append([nvcc(), *ARCH, *NVCC_COMMON, *flags, "-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         for r in ex.map(_run, cmds):
             if verbose and r.stderr:
                 print(r.stderr)
-    if force or cmds or _stale(LIB, objs):
-        _run([nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs])
-    build_host(force)
-    return LIB
+    if force or cmds or _stale(lib, objs):
+        _run([nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", lib, *objs])
+    if not checked:
+        build_host(force)
+    return lib
 
 
 def build_host(force: bool = False) -> None:

@@ -25,6 +25,10 @@
 
 #include "common.cuh"
 
+// first bad index of a bounds-checking build (see TGV_IN_BOUNDS)
+static __device__ unsigned long long g_bounds_adj;
+#define TGV_BOUNDS_WORD g_bounds_adj
+
 namespace tgvdct {
 namespace {
 
@@ -183,8 +187,8 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r1(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z = blockIdx.z;
     float glam = 0.f;
-    if (x < a.W && y < a.H) {
-        const size_t i = ((size_t)z * a.H + y) * a.W + x;
+    const size_t i = ((size_t)z * a.H + y) * a.W + x;
+    if (x < a.W && y < a.H && TGV_IN_BOUNDS(i, a.WH * a.D, 30)) {
         R1In in;
         r1_load(a, i, x > 0, y > 0, in);
         in.pz = z > 0 ? a.S1.p[2][i - a.WH] : 0.f;
@@ -199,6 +203,7 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r3(AdjArgs a) {
     const int z = blockIdx.z;
     if (x >= a.W || y >= a.H) return;
     const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
+    if (!TGV_IN_BOUNDS(i, WH * a.D, 31)) return;
     const bool zl = z + 1 < a.D;
     R3In in;
     r3_load(a, i, x > 0, y > 0, x + 1 < a.W, y + 1 < a.H, in);
@@ -228,8 +233,8 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r3r1(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z = blockIdx.z;
     float glam = 0.f;
-    if (x < a.W && y < a.H) {
-        const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
+    const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
+    if (x < a.W && y < a.H && TGV_IN_BOUNDS(i, WH * a.D, 32)) {
         const bool xl = x + 1 < a.W, yl = y + 1 < a.H, zl = z + 1 < a.D;
         const bool xf = x > 0, yf = y > 0, zf = z > 0;
         R3In r3;
@@ -358,8 +363,8 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r2(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z = blockIdx.z;
     float ga0 = 0.f, ga1 = 0.f;
-    if (x < a.W && y < a.H) {
-        const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
+    const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
+    if (x < a.W && y < a.H && TGV_IN_BOUNDS(i, WH * a.D, 33)) {
         const bool xl = x + 1 < a.W, yl = y + 1 < a.H, zl = z + 1 < a.D;
         const bool xf = x > 0, yf = y > 0, zf = z > 0;
         R2In L;
@@ -384,7 +389,9 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r2_zm(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z0 = (int)blockIdx.z * a.zm, z1 = min(a.D, z0 + a.zm);
     float ga0 = 0.f, ga1 = 0.f;
-    if (x < a.W && y < a.H) {
+    const size_t n = a.WH * a.D, i0 = ((size_t)z0 * a.H + y) * a.W + x;
+    if (x < a.W && y < a.H && TGV_IN_BOUNDS(i0, n, 34) &&
+        TGV_IN_BOUNDS(i0 + (size_t)(z1 - 1 - z0) * a.WH, n, 35)) {
         const size_t W = a.W, WH = a.WH;
         const bool xl = x + 1 < a.W, yl = y + 1 < a.H, xf = x > 0, yf = y > 0;
         size_t i = ((size_t)z0 * a.H + y) * W + x;
@@ -441,6 +448,20 @@ __global__ void finish_grad_f(float* gf, const float* au, const float* aub, size
 }
 
 size_t a256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+uint64_t adjoint_bounds_take() {
+    unsigned long long w = 0;
+    TGV_CUDA(cudaMemcpyFromSymbol(&w, g_bounds_adj, sizeof(w)));
+    if (w) {
+        const unsigned long long zero = 0;
+        TGV_CUDA(cudaMemcpyToSymbol(g_bounds_adj, &zero, sizeof(zero)));
+    }
+    return w;
+}
+
+namespace {
 
 // Planes per thread: about (tiles x D) / (16 blocks per SM), between 1 and ZM_MAX.
 int zm_for(const TgvState& s) {

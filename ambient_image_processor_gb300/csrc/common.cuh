@@ -54,6 +54,33 @@ struct TgvStencilFields {
 
 enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
 
+// Bounds-checking builds (-DTGV_CHECK_BOUNDS, libtgvdct_checked.so): kernels check
+// the indices they are about to use and record the first bad one instead of making
+// the access.  Each translation unit keeps its own record word (a file-scope
+// __device__ variable named by TGV_BOUNDS_WORD) and a host function that reads and
+// clears it.  In normal builds the checks compile to nothing.
+#ifdef TGV_CHECK_BOUNDS
+constexpr bool kCheckBounds = true;
+#else
+constexpr bool kCheckBounds = false;
+#endif
+// True when 0 <= i < n; otherwise records (bit 63 set, site in bits 48..62, the
+// index in bits 0..47) into *word unless something is recorded already.
+__device__ __forceinline__ bool bounds_ok(long long i, long long n, int site,
+                                          unsigned long long* word) {
+    if (i >= 0 && i < n) return true;
+    atomicCAS(word, 0ull,
+              (1ull << 63) | ((unsigned long long)(site & 0x7fff) << 48) |
+                  ((unsigned long long)i & 0xffffffffffffull));
+    return false;
+}
+#define TGV_IN_BOUNDS(i, n, site) \
+    (!kCheckBounds || bounds_ok((long long)(i), (long long)(n), (site), &TGV_BOUNDS_WORD))
+// The record words of the units with checks (0 = nothing recorded); each call clears.
+uint64_t tgv_kernels_bounds_take();
+uint64_t adjoint_bounds_take();
+uint64_t resize_bounds_take();
+
 // An NVTX range over a host-side phase (deshade, loop, Poisson integration, resize,
 // reverse sweep), for profilers that show ranges; free when none is attached.
 struct NvtxRange {

@@ -35,6 +35,10 @@
 
 #include "common.cuh"
 
+// first bad index of a bounds-checking build (see TGV_IN_BOUNDS)
+static __device__ unsigned long long g_bounds_rs;
+#define TGV_BOUNDS_WORD g_bounds_rs
+
 namespace tgvdct {
 namespace {
 
@@ -92,6 +96,13 @@ __global__ void prefilter_kernel(double* c, int w, int h, int d, Pole p) {
     const size_t lines = AXIS == 0 ? (size_t)h * d : AXIS == 1 ? (size_t)w * d : wh;
     const size_t l = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (l >= lines) return;
+    if constexpr (kCheckBounds) {  // the line's first and last element
+        const size_t n = wh * d;
+        const size_t first = AXIS == 0 ? l * w : AXIS == 1 ? (l / w) * wh + l % w : l;
+        const size_t last = first + (AXIS == 0 ? (size_t)(w - 1) : AXIS == 1 ? (size_t)(h - 1) * w
+                                                                              : (size_t)(d - 1) * wh);
+        if (!TGV_IN_BOUNDS(first, n, 40) || !TGV_IN_BOUNDS(last, n, 41)) return;
+    }
     if (AXIS == 0) {
         prefilter_line(c + l * w, w, 1, p, p.z2n[0]);
     } else if (AXIS == 1) {
@@ -126,7 +137,9 @@ __global__ void evaluate_kernel(const double* __restrict__ c, int w, int h, int 
                         wgt = wgt * ax.wt[4 * xo + i];
                         wgt = wgt * wy;
                         wgt = wgt * wz;
-                        acc = acc + wgt * c[by + ax.idx[4 * xo + i]];
+                        const size_t q = by + ax.idx[4 * xo + i];
+                        if (!TGV_IN_BOUNDS(q, wh * d, 42)) continue;
+                        acc = acc + wgt * c[q];
                     }
                 }
             }
@@ -245,6 +258,16 @@ void multiply_fields(const float* a, const float* b, float* out, size_t n, cudaS
 void fill_field(float* out, float v, size_t n, cudaStream_t st) {
     fill_kernel<<<grid_for(n, 256), 256, 0, st>>>(out, v, n);
     TGV_CHECK_LAUNCH();
+}
+
+uint64_t resize_bounds_take() {
+    unsigned long long w = 0;
+    TGV_CUDA(cudaMemcpyFromSymbol(&w, g_bounds_rs, sizeof(w)));
+    if (w) {
+        const unsigned long long zero = 0;
+        TGV_CUDA(cudaMemcpyToSymbol(g_bounds_rs, &zero, sizeof(zero)));
+    }
+    return w;
 }
 
 unsigned resize_factor_extent(unsigned n, float factor) {

@@ -31,6 +31,10 @@
 
 #include "common.cuh"
 
+// first bad index of a bounds-checking build (see TGV_IN_BOUNDS)
+static __device__ unsigned long long g_bounds_tgv;
+#define TGV_BOUNDS_WORD g_bounds_tgv
+
 namespace tgvdct {
 namespace {
 
@@ -138,6 +142,7 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
+    if (!TGV_IN_BOUNDS(i, WH * a.D, 1)) return;
     // outside the masked deshade's domain nothing is updated (tgv2_masked_common.cu)
     if (a.dom && !a.dom[i]) return;
 
@@ -211,6 +216,7 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
     if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
+    if (!TGV_IN_BOUNDS(i, WH * a.D, 2)) return;
     const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
     if (a.dom && !a.dom[i]) return;
 
@@ -384,6 +390,15 @@ __global__ void __launch_bounds__(fused_threads<TY>())
     const int z1 = min(D, z0 + a.zchunk);
     const size_t col = in_dom ? (size_t)y * a.W + x : 0;
     auto idx = [&](int z) { return (size_t)z * a.WH + col; };
+    if constexpr (kCheckBounds) {  // the column, its last plane, the staging position
+        bool ok = true;
+        if (in_dom) {
+            ok = TGV_IN_BOUNDS(col, a.WH, 3) && ok;
+            ok = TGV_IN_BOUNDS(idx(z1 - 1), a.WH * (size_t)D, 4) && ok;
+        }
+        if (active) ok = TGV_IN_BOUNDS(ey * EX + ex, NE, 5) && ok;
+        if (__syncthreads_or(!ok)) return;
+    }
 
     auto load = [&](Prefetch<NC, NQ>& r, int s) {
         if (in_dom && s + 1 < D) {
@@ -854,6 +869,37 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     const int of = ey * G::BW_F + ex + G::XO_F - 1;  // offset in FP32 stencil boxes
     const int odp = ey * G::BW_P + ex + G::XO_P - 1;  // offset in p boxes (R_p only)
     const int odq = (ey - 1) * G::BW_Q + ex - 1;      // offset in q boxes (R_q only)
+    if constexpr (kCheckBounds) {
+        // every index this thread's role uses: its column over the chunk, the staged
+        // boxes (with the neighbours the dual steps read) and the p/q rings
+        constexpr int nF = G::BW_F * EYH, nP = G::BW_P * G::PQ_ROWS, nQ = G::BW_Q * G::PQ_ROWS;
+        bool ok = true;
+        if (in_dom) {
+            ok = TGV_IN_BOUNDS(col, a.WH, 10) && ok;
+            ok = TGV_IN_BOUNDS((size_t)(z1 - 1) * a.WH + col, a.WH * (size_t)D, 11) && ok;
+        }
+        if (in_rp) {
+            ok = TGV_IN_BOUNDS(of, nF, 12) && ok;
+            if (xl) ok = TGV_IN_BOUNDS(of + 1, nF, 13) && ok;
+            if (yl) ok = TGV_IN_BOUNDS(of + G::BW_F, nF, 14) && ok;
+            ok = TGV_IN_BOUNDS(odp, nP, 15) && ok;
+            ok = TGV_IN_BOUNDS(e, NE, 16) && ok;
+        }
+        if (in_rq) {
+            ok = TGV_IN_BOUNDS(of, nF, 17) && ok;
+            if (x > 0) ok = TGV_IN_BOUNDS(of - 1, nF, 18) && ok;
+            if (y > 0) ok = TGV_IN_BOUNDS(of - G::BW_F, nF, 19) && ok;
+            ok = TGV_IN_BOUNDS(odq, nQ, 20) && ok;
+            ok = TGV_IN_BOUNDS(e, NE, 21) && ok;
+        }
+        if (interior) {
+            if (x > 0) ok = TGV_IN_BOUNDS(e - 1, NE, 22) && ok;
+            if (y > 0) ok = TGV_IN_BOUNDS(e - EXW, NE, 23) && ok;
+            if (xl) ok = TGV_IN_BOUNDS(e + 1, NE, 24) && ok;
+            if (yl) ok = TGV_IN_BOUNDS(e + EXW, NE, 25) && ok;
+        }
+        if (__syncthreads_or(!ok)) return;
+    }
     auto st_of = [&](int plane) { return stages + ((plane - pbase) % NS) * G::STAGE; };
     // field views of a stage (st: the stage's base)
     auto fb = [&](const uint8_t* st, int field) -> const float* {  // 0 ubar, 1-3 vbar
@@ -1649,6 +1695,16 @@ void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st) {
         });
     }
     s.cur = 0;
+}
+
+uint64_t tgv_kernels_bounds_take() {
+    unsigned long long w = 0;
+    TGV_CUDA(cudaMemcpyFromSymbol(&w, g_bounds_tgv, sizeof(w)));
+    if (w) {
+        const unsigned long long zero = 0;
+        TGV_CUDA(cudaMemcpyToSymbol(g_bounds_tgv, &zero, sizeof(zero)));
+    }
+    return w;
 }
 
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {

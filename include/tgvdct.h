@@ -471,6 +471,15 @@ tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* ctx, float* u_dev, float* v
                                      tgvdct_iteration_callback callback, void* user,
                                      void* stream);
 
+/* ---- bounds checking (compute-sanitizer is not available to this build) -------- */
+/* In libtgvdct_checked.so (built with -DTGV_CHECK_BOUNDS) the iteration, adjoint and
+   resize kernels check the indices they use and record the first bad one instead of
+   making the access.  This call waits for the device, then returns that record
+   (0: none; else bit 63 set, a site number in bits 48..62, the index in bits 0..47)
+   and clears it.  The normal library returns TGVDCT_ERR_UNSUPPORTED.  No counterpart
+   in the reference. */
+tgvdct_status tgvdct_bounds_check(uint64_t* first_bad);
+
 /* ---- down-sampled deshade (tgvk_deshade_downsampled/, resize/) ---------------- */
 /* Replaces ResizeProcessor::process(image, width, height, depth, BSpline3)
    (resize/ResizeProcessor.cpp:49-143): ITK's cubic B-spline resample as that function

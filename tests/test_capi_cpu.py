@@ -86,3 +86,10 @@ def test_workspace_bytes_scale_with_precision():
     n = 64 ** 3
     # 3 + 6 FP32 (u, ubar, f, v, vbar) + 9 dual fields, plus the DCT plan
     assert b32 >= 18 * 4 * n and b16 >= (9 * 4 + 9 * 2) * n and b16 < b32
+
+
+def test_bounds_check_needs_the_checked_build():
+    """The normal library has no bounds checks compiled in and says so."""
+    import ambient_image_processor_gb300 as pkg
+    w = ctypes.c_uint64(0)
+    assert pkg.lib().tgvdct_bounds_check(ctypes.byref(w)) == pkg.ERR_UNSUPPORTED
