@@ -46,9 +46,14 @@ namespace tgvdct {
 namespace {
 
 constexpr int P_M = 128;          // lines per CTA (MMA M)
-constexpr int P_THREADS = 448;    // 14 warps: 8 converters, MMA, producer, 4 epilogue
+// 18 warps: 8 converters, MMA, producer, 8 epilogue.  Two epilogue warps share each
+// TMEM lane quarter (warp % 4) and drain half of the columns each: with the Poisson
+// division in the epilogue, four warps could not keep up with the tensor core (the z
+// pass of a 256^3 solve took 158 us against 63 us with a plain scale).
+constexpr int P_EPI_WARPS = 16;
+constexpr int P_THREADS = 32 * (10 + P_EPI_WARPS);
 constexpr int P_CONV = 256;       // converter threads (warps 0-7)
-constexpr int P_MMA_WARP = 8, P_PROD_WARP = 9;  // epilogue: warps 10-13
+constexpr int P_MMA_WARP = 8, P_PROD_WARP = 9;  // epilogue: warps 10-17
 constexpr int P_STAGES_MAX = 6;
 constexpr int P_RB = 64;          // bytes per row per stage (K slice)
 constexpr int P_NMAX = 256;
@@ -225,6 +230,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
+// Byte offset, in the x pass's FP32 slab ([P_M rows][KE floats]), of the 16-byte chunk
+// c of row r as the TMA swizzle placed it: the chunk index within a 128-byte (64-byte)
+// span is XORed with address bits 7-9 (7-8), i.e. with r & 7 for 128-byte rows and
+// (r >> 1) & 3 for 64-byte rows.
+template <int MODE>
+__device__ __forceinline__ int xslab_off(int r, int c) {
+    if constexpr (MODE == PM_BF16X3) return r * 128 + ((c ^ (r & 7)) << 4);
+    else return r * 64 + ((c ^ ((r >> 1) & 3)) << 4);
+}
 __device__ __forceinline__ uint32_t tile_off(int r, int cb) {
     return (uint32_t)((r >> 3) * 512 + (cb >> 4) * 128 + (r & 7) * 16 + (cb & 15));
 }
@@ -294,7 +308,7 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+            mbar_init(&acc_empty[b], P_EPI_WARPS);  // one arrival per epilogue warp
         }
         abort_s = 0;
         consumed_s = issued_s = mma_chunks_s = 0;
@@ -360,13 +374,16 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
                     const int u = tid + P_CONV * i;             // 512 units: (line, group)
                     float v[8];
                     if constexpr (AXIS == PA_X) {
-                        // slab [128 lines][KE]: lanes cover 8 lines x 4 groups (contiguous)
-                        const int j = u & 3, r = u >> 2;
-                        const float4* src = (const float4*)(raw + r * G::KE + j * GS);
-                        const float4 a = src[0];
+                        // slab [128 lines][KE], swizzled: lanes cover consecutive lines of
+                        // one group, so that neither these reads nor the writes of
+                        // convert_group meet bank conflicts
+                        const int r = u & 127, j = u >> 7;
+                        const uint8_t* rb = (const uint8_t*)raw;
+                        constexpr int CPG = GS / 4;  // 16-byte chunks per group
+                        const float4 a = *(const float4*)(rb + xslab_off<MODE>(r, j * CPG));
                         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
                         if constexpr (GS == 8) {
-                            const float4 b = src[1];
+                            const float4 b = *(const float4*)(rb + xslab_off<MODE>(r, j * CPG + 1));
                             v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
                         }
                         convert_group<MODE>(v, ahi, alo, r, j);
@@ -424,8 +441,14 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
             }
         }
     } else {
-        // ---- epilogue (warps 10-13: TMEM lane quarter q = warp % 4)
+        // ---- epilogue (warps 10..: TMEM lane quarter q = warp % 4; each group of four
+        // takes an equal share of the 8-column groups)
         const int q = warp & 3;
+        constexpr int parts = P_EPI_WARPS / 4;
+        const int ngroups = (g.NP + 7) / 8;
+        const int part = (warp - 10) / 4;
+        const int c_begin = 8 * (ngroups * part / parts);
+        const int c_end = part + 1 == parts ? g.NP : 8 * (ngroups * (part + 1) / parts);
         int ti = 0;
         for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++ti) {
             const int b = ti & 1;
@@ -453,7 +476,7 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
                     pacc = g.pz_layout == 2 ? g.eig0[kx] + g.eig1[ky] : g.eig0[kx];
                 }
             }
-            for (int c0 = 0; c0 < g.NP; c0 += 8) {
+            for (int c0 = c_begin; c0 < c_end; c0 += 8) {
                 float v[8];
                 tmem_ld8(tmem + (uint32_t)b * acols + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
                 if (line >= g.L) continue;
@@ -545,11 +568,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encoder() {
 }
 
 void encode(CUtensorMap* m, const float* base, int rank, const cuuint64_t* dims,
-            const cuuint64_t* strides, const cuuint32_t* box) {
+            const cuuint64_t* strides, const cuuint32_t* box,
+            CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE) {
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, const_cast<float*>(base),
                                  dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                 swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     TGV_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled rejected a DCT operand");
 }
@@ -714,7 +738,10 @@ bool pass_pipe(DctPlan* p, int axis, bool inverse, const float* in, float* out, 
         const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)(H * D)};
         const cuuint64_t strides[1] = {(cuuint64_t)W * 4};
         const cuuint32_t box[2] = {(cuuint32_t)ke, (cuuint32_t)P_M};
-        encode(&a.in_map, in, 2, dims, strides, box);
+        // rows of ke floats (128 or 64 bytes) land swizzled, so that the converters can
+        // read eight consecutive lines at once without bank conflicts (xslab_off)
+        encode(&a.in_map, in, 2, dims, strides, box,
+               mode == PM_BF16X3 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B);
     } else if (axis == 1) {
         a.NA = (int)H;
         a.L = W;
