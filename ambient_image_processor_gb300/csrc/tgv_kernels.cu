@@ -1017,6 +1017,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a.u + i));
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a.f + i));
             for (int c = 0; c < NC; ++c) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.v[c] + i));
+            if constexpr (MASKED) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.dom + i));
         }
     };
 
@@ -1070,6 +1071,15 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         issue(++issued_upto);
     }
 
+    // masked runs: the domain flags of planes t, t + 1, t + 2 of this thread's column,
+    // one new flag read per step
+    auto live_at = [&](int plane) { return plane < D && live(plane); };
+    bool lq0 = true, lq1 = true, lq2 = true;
+    if constexpr (MASKED) {
+        lq0 = live_at(z0);
+        lq1 = live_at(z0 + 1);
+        lq2 = live_at(z0 + 2);
+    }
     // ring positions of plane t + 1 (stage) and of plane t (p ring) / t (q ring)
     int slot1 = (z0 + 1 - pbase) % NS;
     int pslot = z0 & 1, qslot = z0 % 3;
@@ -1093,10 +1103,12 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         advance_tile();
         load_tile(t + 2);
         prefetch_tile(t + TILE_PREFETCH);
+        bool lq3 = true;
+        if constexpr (MASKED) lq3 = live_at(t + 3);
         // ---- duals for the next planes
         float3 pn = make_float3(0.f, 0.f, 0.f);
-        if (in_rp && p_next) pn = dual_p_at(S1, t + 2 < D ? S2 : nullptr, live(t + 1));
-        if (in_rq && q_next) dual_q_at(S2, S1, Qnn, live(t + 2));
+        if (in_rp && p_next) pn = dual_p_at(S1, t + 2 < D ? S2 : nullptr, lq1);
+        if (in_rq && q_next) dual_q_at(S2, S1, Qnn, lq2);
         // ---- primal at (x, y, t)
         if (interior) {
             const size_t i = (size_t)t * a.WH + col;
@@ -1118,7 +1130,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
                 uu = (uu + a.tau_lambda * pf) / (1.f + a.tau_lambda);
             }
             // outside the domain the stored state is already the frozen one
-            const bool lt = live(t);
+            const bool lt = lq0;
             if (lt) {
                 __stcs(a.u_out + i, uu);
                 __stcs(a.ubar_out + i, uu + a.theta * (uu - pu));
@@ -1168,6 +1180,9 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
             Pn[NE + e] = pn.y;
             if constexpr (THREE) Pn[2 * NE + e] = pn.z;
         }
+        lq0 = lq1;
+        lq1 = lq2;
+        lq2 = lq3;
         }  // ok
         // The block's one barrier per plane: the rings written above become readable,
         // and the stage of plane t + 1 is no longer read.
