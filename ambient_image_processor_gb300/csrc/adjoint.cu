@@ -51,14 +51,15 @@ struct AdjArgs {
 };
 
 __device__ __forceinline__ void block_add(double* dst, float v) {
-    __shared__ float red[BX * BY / 32];
+    __shared__ float red[32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int t = threadIdx.y * BX + threadIdx.x;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
     if ((t & 31) == 0) red[t >> 5] = v;
     __syncthreads();
     if (t == 0) {
         float s = 0.f;
-        for (int w = 0; w < BX * BY / 32; ++w) s += red[w];
+        const int warps = (int)(blockDim.x * blockDim.y) / 32;
+        for (int w = 0; w < warps; ++w) s += red[w];
         if (s != 0.f) atomicAdd(dst, (double)s);
     }
     __syncthreads();
@@ -218,19 +219,25 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r3(AdjArgs a) {
     for (int c = 0; c < 3; ++c) a.A.vbar[c][i] = avb[c];
 }
 
-// The projection pass (R2, 26 loads per voxel) marches up to 6 planes per thread
-// with its fields prefetched into L2 ZPF planes ahead: at 256 x 256 x 192 that took
-// it from 429 to 332 us per launch.  Small volumes get fewer planes per thread so
-// that a launch keeps about two waves of blocks (zm_for); at one plane the
-// one-voxel kernel runs (fewer registers, more blocks resident).  The same
-// treatment made R3.R1 (19 loads per voxel) slower (262 -> 288 us), so it stays one
-// voxel per thread.
-constexpr int ZM_MAX = 6, ZPF = 2;
+// The projection pass (R2, 26 loads per voxel) marches up to ZM_MAX planes per
+// thread.  Its fields are prefetched into L2 ZPF planes ahead, and the 18 pointwise
+// fields (a(p), a(q), p, q) of the next plane are loaded into registers while the
+// current plane computes, at three blocks per SM.  At 256 x 256 x 192 the one-voxel
+// kernel took 429 us per launch, the march with the L2 prefetch 367 us and the
+// register queue 324 us (standalone, the same inputs).  Small volumes get fewer
+// planes per thread so that a launch keeps about two waves of blocks (zm_for); at
+// one plane the one-voxel kernel runs.  The march made R3.R1 (19 loads per voxel)
+// slower (262 -> 288 us), so it stays one voxel per thread.
+constexpr int ZM_MAX = 4, ZPF = 1;
 
 // R3 of iteration k followed by R1 of iteration k-1 (S = S_{k-1}, S1 = S_k): a(ubar)
-// and a(vbar) stay in registers.  Each thread marches ZM planes of its column.
+// and a(vbar) stay in registers.  One voxel per thread, TBX x (256 / TBX) blocks:
+// rows of 128 or 256 voxels per block read each field in longer runs, which at
+// 256 x 256 x 192 took it from 241 to 230 us; narrow volumes keep 32 x 8.
+template <int TBX>
 __global__ void __launch_bounds__(BX* BY) adjoint_r3r1(AdjArgs a) {
-    const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+    constexpr int TBY = BX * BY / TBX;
+    const int x = blockIdx.x * TBX + threadIdx.x, y = blockIdx.y * TBY + threadIdx.y;
     const int z = blockIdx.z;
     float glam = 0.f;
     const size_t i = ((size_t)z * a.H + y) * a.W + x, WH = a.WH;
@@ -253,8 +260,25 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r3r1(AdjArgs a) {
     block_add(&a.gp[0], glam);
 }
 
-// R2 inputs at voxel i besides the centres it loads itself: a(u~) and ubar with their
-// +x, +y, +z neighbours, a(v') and vbar with their -x, -y, -z neighbours.
+// R2's pointwise inputs at voxel i: a(p), a(q) (adjoints of S_{k+1}) and p, q of S_k.
+struct R2Pw {
+    float ap[3], aq[6], sp[3], sq[6];
+};
+__device__ __forceinline__ void r2_pw_load(const AdjArgs& a, size_t i, R2Pw& P) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        P.ap[c] = a.A.p[c][i];
+        P.sp[c] = a.S.p[c][i];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        P.aq[k] = a.A.q[k][i];
+        P.sq[k] = a.S.q[k][i];
+    }
+}
+
+// R2's stencil inputs at voxel i: a(u~) and ubar with their +x, +y, +z neighbours,
+// a(v') and vbar with their -x, -y, -z neighbours.
 struct R2In {
     float ut0, utx, uty, utz;
     float va0[3], vax[3], vay[3], vaz[3];
@@ -263,16 +287,16 @@ struct R2In {
 };
 
 // R2 at voxel i: the projection Jacobians; accumulates d/dalpha0, d/dalpha1.
-__device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, bool xl, bool yl, bool zl,
-                                        bool xf, bool yf, bool zf, const R2In& L, float& ga0,
-                                        float& ga1) {
+__device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, const R2Pw& P, bool xl,
+                                        bool yl, bool zl, bool xf, bool yf, bool zf,
+                                        const R2In& L, float& ga0, float& ga1) {
     // a(p') = a(p) + tau a(v') - tau B^T a(u~)
     const float bt[3] = {(xl ? L.utx : 0.f) - L.ut0, (yl ? L.uty : 0.f) - L.ut0,
                          (zl ? L.utz : 0.f) - L.ut0};
     float pa[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        pa[c] = a.A.p[c][i] + a.tau * L.va0[c];
+        pa[c] = P.ap[c] + a.tau * L.va0[c];
         if (!(c == 2 && a.skip_bz)) pa[c] = pa[c] - a.tau * bt[c];
     }
     // a(q') = a(q) - tau divF^T a(v'): (F_a^T g)[i] = g[i-e] (if >= 1) - g[i] (if < N-1)
@@ -285,20 +309,20 @@ __device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, bool xl, boo
         fz[c] = (zf ? L.vaz[c] : 0.f) - (zl ? g0 : 0.f);
     }
     float qa[6];  // xx yy zz xy xz yz
-    qa[0] = a.A.q[0][i] - a.tau * fx[0];
-    qa[1] = a.A.q[1][i] - a.tau * fy[1];
-    qa[2] = a.A.q[2][i] - a.tau * fz[2];
-    qa[3] = a.A.q[3][i] - a.tau * (fy[0] + fx[1]);
-    qa[4] = a.A.q[4][i] - a.tau * (fz[0] + fx[2]);
-    qa[5] = a.A.q[5][i] - a.tau * (fz[1] + fy[2]);
+    qa[0] = P.aq[0] - a.tau * fx[0];
+    qa[1] = P.aq[1] - a.tau * fy[1];
+    qa[2] = P.aq[2] - a.tau * fz[2];
+    qa[3] = P.aq[3] - a.tau * (fy[0] + fx[1]);
+    qa[4] = P.aq[4] - a.tau * (fz[0] + fx[2]);
+    qa[5] = P.aq[5] - a.tau * (fz[1] + fy[2]);
     // y_p of the forward dual pass, bit for bit
     const float gx = xl ? L.ubx - L.u0 : 0.f;
     const float gy = yl ? L.uby - L.u0 : 0.f;
     const float gz = zl ? L.ubz - L.u0 : 0.f;
     const float* vb = L.vb0;
-    const float yp[3] = {__fmaf_rn(a.sigma, gx - vb[0], a.S.p[0][i]),
-                         __fmaf_rn(a.sigma, gy - vb[1], a.S.p[1][i]),
-                         __fmaf_rn(a.sigma, gz - vb[2], a.S.p[2][i])};
+    const float yp[3] = {__fmaf_rn(a.sigma, gx - vb[0], P.sp[0]),
+                         __fmaf_rn(a.sigma, gy - vb[1], P.sp[1]),
+                         __fmaf_rn(a.sigma, gz - vb[2], P.sp[2])};
     const float np = norm3df(yp[0], yp[1], yp[2]);
     if (fmaxf(1.f, np / a.alpha1) > 1.f) {
         const float yg = yp[0] * pa[0] + yp[1] * pa[1] + yp[2] * pa[2];
@@ -320,7 +344,7 @@ __device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, bool xl, boo
                         ((vbz_y - vb[2]) + (vby_z - vb[1])) * 0.5f};
     float yq[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) yq[k] = __fmaf_rn(a.sigma, e[k], a.S.q[k][i]);
+    for (int k = 0; k < 6; ++k) yq[k] = __fmaf_rn(a.sigma, e[k], P.sq[k]);
     float sq = yq[0] * yq[0] + yq[1] * yq[1] + 2.f * yq[3] * yq[3];
     sq = sq + yq[2] * yq[2] + 2.f * yq[4] * yq[4] + 2.f * yq[5] * yq[5];
     const float nq = sqrtf(sq);
@@ -378,14 +402,17 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r2(AdjArgs a) {
             L.vaz[c] = zf ? a.va[c][i - WH] : 0.f;
             L.vbz[c] = zf ? a.S.vbar[c][i - WH] : 0.f;
         }
-        r2_vals(a, i, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
+        R2Pw P;
+        r2_pw_load(a, i, P);
+        r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
     }
     block_add(&a.gp[1], ga0);
     block_add(&a.gp[2], ga1);
 }
 
-// R2 marching a.zm planes per thread with its fields prefetched into L2.
-__global__ void __launch_bounds__(BX* BY) adjoint_r2_zm(AdjArgs a) {
+// R2 marching a.zm planes per thread: the fields prefetched into L2 ZPF planes ahead,
+// the pointwise fields of the next plane queued in registers.
+__global__ void __launch_bounds__(BX* BY, 3) adjoint_r2_zm(AdjArgs a) {
     const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
     const int z0 = (int)blockIdx.z * a.zm, z1 = min(a.D, z0 + a.zm);
     float ga0 = 0.f, ga1 = 0.f;
@@ -421,13 +448,17 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r2_zm(AdjArgs a) {
             L.vaz[c] = z0 > 0 ? a.va[c][i - WH] : 0.f;
             L.vbz[c] = z0 > 0 ? a.S.vbar[c][i - WH] : 0.f;
         }
+        R2Pw P, Pn;
+        r2_pw_load(a, i, P);
         for (int z = z0; z < z1; ++z, i += WH) {
             prefetch_plane(z + ZPF);
+            if (z + 1 < z1) r2_pw_load(a, i + WH, Pn);
             const bool zl = z + 1 < a.D, zf = z > 0;
             r2_load(a, i, xl, yl, xf, yf, L);
             L.utz = zl ? a.uta[i + WH] : 0.f;
             L.ubz = zl ? a.S.ubar[i + WH] : 0.f;
-            r2_vals(a, i, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
+            r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
+            P = Pn;
             L.ut0 = L.utz;
             L.u0 = L.ubz;
 #pragma unroll
@@ -527,6 +558,10 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
     const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
     a.zm = zm_for(s);
     const dim3 zgrid(ceil_div(s.W, BX), ceil_div(s.H, BY), ceil_div(s.D, a.zm));
+    // R3.R1 block rows: the widest of 256, 128, 32 voxels that W fills
+    const int tbx = s.W >= 256 ? 256 : (s.W >= 128 ? 128 : 32);
+    const dim3 rblock(tbx, BX * BY / tbx, 1);
+    const dim3 rgrid(ceil_div(s.W, tbx), ceil_div(s.H, BX * BY / tbx), s.D);
     // iteration j of the segment maps states[j] -> states[j + 1]
     a.S = states[len - 1];
     a.S1 = states[len];
@@ -539,7 +574,9 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
         if (j > 0) {
             a.S = states[j - 1];
             a.S1 = states[j];
-            adjoint_r3r1<<<grid, block, 0, st>>>(a);
+            if (tbx == 256) adjoint_r3r1<256><<<rgrid, rblock, 0, st>>>(a);
+            else if (tbx == 128) adjoint_r3r1<128><<<rgrid, rblock, 0, st>>>(a);
+            else adjoint_r3r1<32><<<rgrid, rblock, 0, st>>>(a);
         } else {
             adjoint_r3<<<grid, block, 0, st>>>(a);
         }
