@@ -122,6 +122,7 @@ _SIGS = {
     "tgvdct_tgv2_energy_dev": [ctypes.POINTER(Params), _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_energy_history": [_vp, _vp, _u32, ctypes.POINTER(_u32)],
     "tgvdct_request_stop": [_vp],
+    "tgvdct_release_cached": [],
     "tgvdct_state_bytes": [_vp],
     "tgvdct_bounds_check": [ctypes.POINTER(ctypes.c_uint64)],
     "tgvdct_state_save_dev": [_vp, _vp, _vp],
@@ -191,6 +192,12 @@ def lib_checked() -> ctypes.CDLL:
 
 def version() -> str:
     return lib().tgvdct_version().decode()
+
+
+def release_cached() -> None:
+    """Frees the context and device buffers the host-buffer one-shot calls keep
+    between calls (tgvdct_release_cached)."""
+    _check(lib().tgvdct_release_cached(), allow_stop=False)
 
 
 def _check(status: int, allow_stop: bool = True) -> int:

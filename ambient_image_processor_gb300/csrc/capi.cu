@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -487,6 +488,113 @@ struct DevBuf {
     ~DevBuf() {
         if (p) cudaFree(p);
     }
+};
+
+// ---- the host-buffer calls' context cache ---------------------------------------------
+// The one-shot host-buffer calls (the reference's per-volume entry points) keep their
+// last context and device buffers, so that a caller streaming volumes of one shape
+// through them pays the state allocation, the DCT plan and the graph captures once
+// (about 4 ms of a 446 ms deshade at 256 x 256 x 192). One entry, keyed by the
+// parameters, the entry point and the device. A call that finds the entry held (by
+// another thread, or by an outer call whose iteration callback re-entered the
+// library) builds a private context; a call that fails drops the entry.
+// tgvdct_release_cached frees it.
+struct HostCache {
+    std::atomic<bool> busy{false};
+    tgvdct_context* c = nullptr;
+    int kind = 0, dev = -1;
+    float* bufs = nullptr;
+    size_t bufs_floats = 0;
+};
+HostCache& host_cache() {
+    static HostCache* h = new HostCache();  // never destroyed: no CUDA calls at exit
+    return *h;
+}
+void host_cache_drop(HostCache& h) {
+    destroy_ctx(h.c);
+    h.c = nullptr;
+    if (h.bufs) cudaFree(h.bufs);
+    h.bufs = nullptr;
+    h.bufs_floats = 0;
+}
+
+// The entry points that lease contexts (the cache key's `kind`).
+enum HostKind {
+    HK_PROCESS = 1,
+    HK_PROCESS_MASKED,
+    HK_DESHADE_LAUNCH,
+    HK_DESHADE_MASKED_LAUNCH,
+    HK_RUN,
+    HK_DENOISE_LAUNCH,
+};
+
+// Exclusive use of the cache entry while it lives (when `owned`).
+struct CacheClaim {
+    bool owned = false;
+    CacheClaim() {
+        bool idle = false;
+        owned = host_cache().busy.compare_exchange_strong(idle, true);
+    }
+    ~CacheClaim() {
+        if (owned) host_cache().busy.store(false);
+    }
+    CacheClaim(const CacheClaim&) = delete;
+    CacheClaim& operator=(const CacheClaim&) = delete;
+};
+
+// A context and `nbuf` device buffers of n floats for one host-buffer call: the
+// cached entry when it is free, else a private context. commit() after a call that
+// succeeded keeps the entry for the next call.
+class HostLease {
+  public:
+    HostLease(const tgvdct_params& p, int kind, int nbuf) : n_(voxels(p)) {
+        if (claim_.owned) {
+            HostCache& h = host_cache();
+            int dev = -1;
+            TGV_CUDA(cudaGetDevice(&dev));
+            if (h.c && (h.kind != kind || h.dev != dev ||
+                        std::memcmp(&h.c->prm, &p, sizeof(tgvdct_params)) != 0))
+                host_cache_drop(h);
+            if (!h.c) {
+                create_into(&p, &h.c);
+                h.kind = kind;
+                h.dev = dev;
+            }
+            const size_t want = (size_t)nbuf * n_;
+            if (h.bufs_floats < want) {
+                if (h.bufs) cudaFree(h.bufs);
+                h.bufs = nullptr;
+                h.bufs_floats = 0;
+                TGV_CUDA(cudaMalloc(&h.bufs, want * sizeof(float)));
+                h.bufs_floats = want;
+            }
+            c = h.c;
+            bufs_ = h.bufs;
+        } else {
+            create_into(&p, &own_.c);
+            c = own_.c;
+            if (nbuf) {
+                own_bufs_ = std::make_unique<DevBuf>((size_t)nbuf * n_);
+                bufs_ = own_bufs_->p;
+            }
+        }
+    }
+    ~HostLease() {
+        if (claim_.owned && !committed_) host_cache_drop(host_cache());
+    }
+    HostLease(const HostLease&) = delete;
+    HostLease& operator=(const HostLease&) = delete;
+    void commit() { committed_ = true; }
+    float* buf(int k) const { return bufs_ + (size_t)k * n_; }
+    tgvdct_context* c = nullptr;
+
+  private:
+    CacheClaim claim_;  // first: released after everything else
+    size_t n_;
+    CtxGuard own_;
+    std::unique_ptr<DevBuf> own_bufs_;
+    float* bufs_ = nullptr;
+    bool committed_ = false;
 };
 
 void process_on_device(tgvdct_context* c, const float* f_dev, const float* mask_dev, bool clamp,
@@ -1043,8 +1151,8 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch(const float* f_host, uint32_t width,
         p.alpha1 = alpha1;
         p.iteration_count = iteration_count;
         p.paint_iteration_interval = paint_iteration_interval;
-        CtxGuard g;
-        create_into(&p, &g.c);
+        validate(&p);
+        HostLease g(p, HK_DESHADE_LAUNCH, 0);
         tgvdct_context* c = g.c;
         const size_t n = voxels(p);
         cudaStream_t s = 0;
@@ -1057,6 +1165,7 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch(const float* f_host, uint32_t width,
         TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_z_host, c->st.v[2], n * 4, cudaMemcpyDeviceToHost, s));
         check_tgv_flag(c, s);
+        g.commit();
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -1081,8 +1190,8 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t wid
         p.alpha1 = alpha1;
         p.iteration_count = iteration_count;
         p.paint_iteration_interval = paint_iteration_interval;
-        CtxGuard g;
-        create_into(&p, &g.c);
+        validate(&p);
+        HostLease g(p, HK_DESHADE_LAUNCH, 0);
         tgvdct_context* c = g.c;
         const size_t n = voxels(p);
         cudaStream_t s = 0;
@@ -1094,6 +1203,7 @@ tgvdct_status tgvdct_tgv2_l1_deshade_launch_2d(const float* f_host, uint32_t wid
         TGV_CUDA(cudaMemcpyAsync(v_x_host, c->st.v[0], n * 4, cudaMemcpyDeviceToHost, s));
         TGV_CUDA(cudaMemcpyAsync(v_y_host, c->st.v[1], n * 4, cudaMemcpyDeviceToHost, s));
         check_tgv_flag(c, s);
+        g.commit();
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -1103,8 +1213,8 @@ tgvdct_status tgvdct_tgv2_run(const tgvdct_params* p, const float* f_host, float
                              tgvdct_iteration_callback callback, void* user) {
     return guarded([&] {
         TGV_REQUIRE(p && f_host && u_host, "null host buffer");
-        CtxGuard g;
-        create_into(p, &g.c);
+        validate(p);
+        HostLease g(*p, HK_RUN, 0);
         tgvdct_context* c = g.c;
         const size_t n = voxels(*p);
         cudaStream_t s = 0;
@@ -1121,6 +1231,7 @@ tgvdct_status tgvdct_tgv2_run(const tgvdct_params* p, const float* f_host, float
             else TGV_CUDA(cudaMemcpyAsync(vh[k], c->st.v[k], n * 4, cudaMemcpyDeviceToHost, s));
         }
         check_tgv_flag(c, s);
+        g.commit();
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -1141,8 +1252,8 @@ tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, ui
         p.alpha0 = alpha0;
         p.alpha1 = alpha1;
         p.iteration_count = iteration_count;
-        CtxGuard g;
-        create_into(&p, &g.c);
+        validate(&p);
+        HostLease g(p, HK_DENOISE_LAUNCH, 0);
         tgvdct_context* c = g.c;
         const size_t n = voxels(p);
         cudaStream_t s = 0;
@@ -1150,6 +1261,7 @@ tgvdct_status tgvdct_tgv2_denoise_launch(const float* f_host, uint32_t width, ui
         run_loop(c, s, false, [](uint32_t) { return false; });
         TGV_CUDA(cudaMemcpyAsync(u_host, c->st.u, n * 4, cudaMemcpyDeviceToHost, s));
         check_tgv_flag(c, s);
+        g.commit();
         return TGVDCT_OK;
     });
 }
@@ -1384,22 +1496,22 @@ tgvdct_status tgvdct_process_tgv2_l1_masked(const tgvdct_params* p, const float*
                     "null host buffer");
         tgvdct_params q = *p;
         if (q.depth == 1) q.geometry = TGVDCT_GEOMETRY_2D;  // TGVDeshadeMaskedProcessor.cpp:94-99
-        CtxGuard g;
-        create_into(&q, &g.c);
+        validate(&q);
+        HostLease g(q, HK_PROCESS_MASKED, 5);
         tgvdct_context* c = g.c;
         const size_t n = voxels(q);
-        DevBuf f(n), m(n), u(n), l(n), r(n);
+        float *f = g.buf(0), *m = g.buf(1), *u = g.buf(2), *l = g.buf(3), *r = g.buf(4);
         cudaStream_t s = 0;
-        TGV_CUDA(cudaMemcpyAsync(f.p, f_host, n * 4, cudaMemcpyHostToDevice, s));
-        TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
-        set_domain(c, m.p, s);
-        process_on_device(c, f.p, nullptr, set_negative_values_to_zero != 0,
-                          add_background_back != 0, log_domain != 0, u.p, l.p, r.p, callback,
-                          user, s);
-        TGV_CUDA(cudaMemcpyAsync(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        TGV_CUDA(cudaMemcpyAsync(m, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        set_domain(c, m, s);
+        process_on_device(c, f, nullptr, set_negative_values_to_zero != 0,
+                          add_background_back != 0, log_domain != 0, u, l, r, callback, user, s);
+        TGV_CUDA(cudaMemcpyAsync(denoised_host, u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(shading_host, l, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r, n * 4, cudaMemcpyDeviceToHost, s));
         check_tgv_flag(c, s);
+        g.commit();
         return c->iterations_run < q.iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -1423,15 +1535,15 @@ tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
         p.iteration_count = iteration_count;
         p.paint_iteration_interval = paint_iteration_interval;
         if (depth == 1) p.geometry = TGVDCT_GEOMETRY_2D;
-        CtxGuard g;
-        create_into(&p, &g.c);
+        validate(&p);
+        HostLease g(p, HK_DESHADE_MASKED_LAUNCH, 1);
         tgvdct_context* c = g.c;
         const size_t n = voxels(p);
-        DevBuf m(n);
+        float* m = g.buf(0);
         cudaStream_t s = 0;
         TGV_CUDA(cudaMemcpyAsync(c->st.f, f_host, n * 4, cudaMemcpyHostToDevice, s));
-        TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
-        set_domain(c, m.p, s);
+        TGV_CUDA(cudaMemcpyAsync(m, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        set_domain(c, m, s);
         const bool stopped = run_loop(c, s, callback != nullptr, [&](uint32_t it) {
             return deliver(c, callback, user, it, c->st.u, c->st.v[0], c->st.v[1],
                            c->st.three ? c->st.v[2] : nullptr, s) != 0;
@@ -1446,6 +1558,7 @@ tgvdct_status tgvdct_tgv2_l1_deshade_masked_launch(
                 std::memset(v_z_host, 0, n * 4);
         }
         check_tgv_flag(c, s);
+        g.commit();
         return stopped ? TGVDCT_STOPPED : TGVDCT_OK;
     });
 }
@@ -1571,26 +1684,36 @@ tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host
                                      float* deshaded_host) {
     return guarded([&] {
         TGV_REQUIRE(f_host && denoised_host && shading_host && deshaded_host, "null host buffer");
-        CtxGuard g;
-        create_into(p, &g.c);
+        validate(p);
+        HostLease g(*p, HK_PROCESS, mask_host ? 5 : 4);
         tgvdct_context* c = g.c;
         const size_t n = voxels(*p);
-        DevBuf f(n), m(mask_host ? n : 0), u(n), l(n), r(n);
+        float *f = g.buf(0), *u = g.buf(1), *l = g.buf(2), *r = g.buf(3);
+        float* m = mask_host ? g.buf(4) : nullptr;
         cudaStream_t s = 0;
-        TGV_CUDA(cudaMemcpyAsync(f.p, f_host, n * 4, cudaMemcpyHostToDevice, s));
-        if (mask_host) TGV_CUDA(cudaMemcpyAsync(m.p, mask_host, n * 4, cudaMemcpyHostToDevice, s));
-        process_on_device(c, f.p, mask_host ? m.p : nullptr, set_negative_values_to_zero != 0,
-                          add_background_back != 0, log_domain != 0, u.p, l.p, r.p, callback, user,
-                          s);
-        TGV_CUDA(cudaMemcpyAsync(denoised_host, u.p, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaMemcpyAsync(shading_host, l.p, n * 4, cudaMemcpyDeviceToHost, s));
-        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r.p, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(f, f_host, n * 4, cudaMemcpyHostToDevice, s));
+        if (mask_host) TGV_CUDA(cudaMemcpyAsync(m, mask_host, n * 4, cudaMemcpyHostToDevice, s));
+        process_on_device(c, f, m, set_negative_values_to_zero != 0, add_background_back != 0,
+                          log_domain != 0, u, l, r, callback, user, s);
+        TGV_CUDA(cudaMemcpyAsync(denoised_host, u, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(shading_host, l, n * 4, cudaMemcpyDeviceToHost, s));
+        TGV_CUDA(cudaMemcpyAsync(deshaded_host, r, n * 4, cudaMemcpyDeviceToHost, s));
         check_tgv_flag(c, s);
         if (c->plan && !dct_tc_check(c->plan, s)) {
             set_error("a tensor-core DCT pass timed out waiting on its pipeline");
             return TGVDCT_ERR_TIMEOUT;
         }
+        g.commit();
         return c->iterations_run < p->iteration_count ? TGVDCT_STOPPED : TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_release_cached(void) {
+    return guarded([&] {
+        CacheClaim claim;
+        TGV_REQUIRE(claim.owned, "the cached context is in use by a running call");
+        host_cache_drop(host_cache());
+        return TGVDCT_OK;
     });
 }
 

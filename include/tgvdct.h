@@ -349,6 +349,18 @@ tgvdct_status tgvdct_process_tgv2_l1(const tgvdct_params* p, const float* f_host
                                      float* denoised_host, float* shading_host,
                                      float* deshaded_host);
 
+/* The host-buffer one-shot calls (tgvdct_process_tgv2_l1, tgvdct_process_tgv2_l1_masked,
+   tgvdct_tgv2_run, tgvdct_tgv2_l1_deshade_launch, tgvdct_tgv2_l1_deshade_launch_2d,
+   tgvdct_tgv2_l1_deshade_masked_launch, tgvdct_tgv2_denoise_launch) keep their last
+   context and its device buffers between calls, so that volumes of one shape streamed
+   through them pay the state allocation, the DCT plan and the graph captures once.
+   One entry, keyed by the parameters, the call and the current device; a concurrent
+   or re-entrant call uses a private context; a failed call drops the entry.  This
+   frees the entry: the TGV state and the call's device buffers.
+   No replacement: the reference allocates and frees inside each call.  Returns
+   TGVDCT_ERR_BAD_ARG while a call holds the entry. */
+tgvdct_status tgvdct_release_cached(void);
+
 /* Device form of the whole deshade on a context (no host copies): f_dev in; u,
    l, r out; mask_dev may be NULL.  Stream-ordered. */
 tgvdct_status tgvdct_process_dev(tgvdct_context* ctx, const float* f_dev, const float* mask_dev,

@@ -93,3 +93,10 @@ def test_bounds_check_needs_the_checked_build():
     import ambient_image_processor_gb300 as pkg
     w = ctypes.c_uint64(0)
     assert pkg.lib().tgvdct_bounds_check(ctypes.byref(w)) == pkg.ERR_UNSUPPORTED
+
+
+def test_release_cached_without_a_cached_context():
+    """Nothing is cached before a host-buffer call: releasing needs no device."""
+    import ambient_image_processor_gb300 as pkg
+    assert pkg.lib().tgvdct_release_cached() == pkg.OK
+    pkg.release_cached()
