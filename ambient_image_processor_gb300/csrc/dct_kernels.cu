@@ -463,9 +463,11 @@ DctPlan* dct_plan_create(int W, int H, int D) {
                                                             inexact);
         se = cudaGetLastError();
     }
+    // The synchronous copy waits for the set-up kernels before it (the same legacy
+    // stream). No device-wide synchronisation: that is refused, and invalidates the
+    // capture, while another thread captures a loop graph.
     int h_inexact = 1;
     if (se == cudaSuccess) se = cudaMemcpy(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost);
-    if (se == cudaSuccess) se = cudaDeviceSynchronize();
     if (se != cudaSuccess) {
         cudaFree(p->block);
         delete p;

@@ -2,7 +2,7 @@
 calls (tgvdct_release_cached frees them).  A call served by the kept context gives
 the bits of a call on a fresh one: for a repeated input, a new input, new
 parameters, a switch between entry points, and a call re-entered from an iteration
-callback."""
+callback, and for concurrent calls from several threads."""
 import numpy as np
 import pytest
 
@@ -84,4 +84,32 @@ def test_reentrant_call_from_the_callback(gpu_lib):
     assert len(inner) >= 3
     for u in inner:
         assert np.array_equal(u, ref_inner)
+    pkg.release_cached()
+
+
+def test_concurrent_calls_from_several_threads(gpu_lib):
+    """Four threads in the host-buffer call at once (ctypes releases the GIL): one gets
+    the kept context, the others private ones; all give the bits of a fresh call."""
+    import threading
+    fs = [tissue_phantom_3d(*SHAPE, seed=40 + k) for k in range(4)]
+    refs = [_fresh(lambda f=f: _deshade(f, it=60)) for f in fs]
+    pkg.release_cached()
+    got = [None] * len(fs)
+    errors = []
+
+    def work(k):
+        try:
+            got[k] = _deshade(fs[k], it=60)
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    for _ in range(2):
+        threads = [threading.Thread(target=work, args=(k,)) for k in range(len(fs))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        for k in range(len(fs)):
+            _same(got[k], refs[k])
     pkg.release_cached()
