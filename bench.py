@@ -43,6 +43,9 @@ WORKLOADS = {
 # vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
 ALGO_BYTES = {0: 140, 1: 104, 2: 104}
 KERNELS = {"fused": 2, "two_pass": 1}
+# the extra measurements a default run adds to its line, in the order they run
+EXTRAS = ["iteration_variants", "dct_poisson_256cube", "adjoint", "adjoint_256x256x192",
+          "other_configs", "downsampled_deshade", "masked_deshade"]
 PREC_NAMES = {0: "fp32", 1: "bf16_dual", 2: "fx16_dual"}
 DCT_MODES = {"fp32": 0, "tf32": 1, "bf16x3": 2}
 
@@ -505,21 +508,32 @@ def run_ours(args):
     if rank == 0:
         extra = {}
         if not args.no_variants:
-            var = {}
-            for kernel, prec in (("two_pass", 0), ("fused", 0), ("two_pass", 2), ("fused", 2),
-                                 ("fused", 1)):
-                t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 40, stream)
-                var[f"{kernel}_{PREC_NAMES[prec]}"] = {
-                    "ms_per_iteration": t, "voxel_iters_per_s": V / (t * 1e-3),
-                    "algorithmic_gbs": ALGO_BYTES[prec] * V / (t * 1e-3) / 1e9}
-            extra["iteration_variants"] = var
-            extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
-            extra["adjoint"] = time_adjoint(pkg, torch, stream)
-            extra["adjoint_256x256x192"] = time_adjoint(pkg, torch, stream, (192, 256, 256),
-                                                        K=100, every=20)
-            extra["other_configs"] = time_other_configs(pkg, torch, stream)
-            extra["downsampled_deshade"] = time_downsampled(pkg, torch, stream)
-            extra["masked_deshade"] = time_masked(pkg, torch, stream)
+            want = set(args.extras.split(",")) if args.extras else set(EXTRAS)
+            unknown = want - set(EXTRAS)
+            if unknown:
+                raise SystemExit(f"unknown --extras {sorted(unknown)}; known: {EXTRAS}")
+            if "iteration_variants" in want:
+                var = {}
+                for kernel, prec in (("two_pass", 0), ("fused", 0), ("two_pass", 2),
+                                     ("fused", 2), ("fused", 1)):
+                    t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 40, stream)
+                    var[f"{kernel}_{PREC_NAMES[prec]}"] = {
+                        "ms_per_iteration": t, "voxel_iters_per_s": V / (t * 1e-3),
+                        "algorithmic_gbs": ALGO_BYTES[prec] * V / (t * 1e-3) / 1e9}
+                extra["iteration_variants"] = var
+            if "dct_poisson_256cube" in want:
+                extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
+            if "adjoint" in want:
+                extra["adjoint"] = time_adjoint(pkg, torch, stream)
+            if "adjoint_256x256x192" in want:
+                extra["adjoint_256x256x192"] = time_adjoint(pkg, torch, stream, (192, 256, 256),
+                                                            K=100, every=20)
+            if "other_configs" in want:
+                extra["other_configs"] = time_other_configs(pkg, torch, stream)
+            if "downsampled_deshade" in want:
+                extra["downsampled_deshade"] = time_downsampled(pkg, torch, stream)
+            if "masked_deshade" in want:
+                extra["masked_deshade"] = time_masked(pkg, torch, stream)
         cpu = None
         if not args.no_cpu_baseline:
             rate, cores, dt = cpu_reference(args, f_host, args.cpu_sample_iterations)
@@ -637,6 +651,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--extras", default="",
+                    help="comma-separated subset of the extra measurements (default: all of "
+                         + ", ".join(EXTRAS) + ")")
     ap.add_argument("--accuracy", action="store_true",
                     help="error of every precision form against the FP64 oracle instead")
     args = ap.parse_args()
