@@ -10,7 +10,7 @@ deshade of the volume.  Metric: voxel-iterations per second.
   e2e    the reference-facing call tgvdct_process_tgv2_l1 with host buffers
          (host->device copy of f and device->host copies of u, l, r inside)
   roofline  the TGV iteration kernels, timed live with CUDA events on the stream
-         they run on; algorithmic bytes per voxel-iteration as in the design doc
+         they run on; algorithmic bytes per voxel-iteration from ALGO_BYTES
 
 ``--impl reference`` times the reference algorithm's CPU restatement (the oracle
 port; the reference itself has no CPU path) on the host cores instead.

@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE — Python bindings of the CPU oracle.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may use
-this package, and only as the checker.  ``liboracle.so`` is the C++ restatement of
+this package, and only to check the CUDA path.  ``liboracle.so`` is the C++ restatement of
 the reference's TGV-DCT kernel sequence (``tgv_oracle.hpp``); ``libref_cpu.so``
 (optional, ``oracle/_ref``) is the reference's own CUDA source compiled for the CPU
 by ``ref_cpu/build_ref_cpu.py`` where the reference tree is available.

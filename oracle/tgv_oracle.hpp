@@ -1,6 +1,6 @@
 // TEST INFRASTRUCTURE — the CPU oracle for the TGV-DCT deshade path.
 //
-// This header is the checker, not the product: only tests/, __graft_entry__.smoke()
+// This header checks the product and is not part of it: only tests/, __graft_entry__.smoke()
 // and bench.py's CPU-baseline leg may call it.  It restates, step by step, the
 // reference's CUDA kernel sequence of josefkoller/ambient_image_processor as plain
 // C++ loops (OpenMP over voxels), templated on the pixel type:

@@ -3,8 +3,8 @@
 Each fixture holds seeded inputs and the outputs of the reference's CUDA sources
 (source/modules/tgv_deshade, tgv_cuda, cuda_image_operations) compiled for the
 CPU by oracle/ref_cpu/build_ref_cpu.py and run in the build container, where the
-reference tree is available.  The GPU machine never runs this script; tests there
-read the committed .npz files.
+reference tree is available.  A machine without that tree never runs this script;
+tests there read the committed .npz files.
 
     python oracle/ref_cpu/build_ref_cpu.py && python tests/golden/make_golden.py
 """
