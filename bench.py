@@ -193,9 +193,8 @@ def run_reference_arm(args):
 
 # ---------------------------------------------------------------------------------
 # DRAM bytes (read + write) of one launch of the fused TMA kernel on this workload,
-# FP32 state, from the ncu capture summarised in
-# profiles/tgv_fused_tma_kernel_deshade_256x256x192.md (dram__bytes_read.sum +
-# dram__bytes_write.sum).
+# FP32 state: dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full
+# capture of that launch (its summary is under profiles/).
 TRAFFIC_FUSED_FP32_256x256x192 = 914891776 + 801782528
 
 

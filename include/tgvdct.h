@@ -42,7 +42,7 @@ typedef enum tgvdct_status {
     TGVDCT_ERR_OOM = 2,         /* device or host allocation failed */
     TGVDCT_ERR_CUDA = 3,        /* a CUDA runtime call or kernel launch failed */
     TGVDCT_ERR_NO_DEVICE = 4,   /* no CUDA device, or not an sm_103 device */
-    TGVDCT_ERR_UNSUPPORTED = 5, /* a mode this build does not provide */
+    TGVDCT_ERR_UNSUPPORTED = 5, /* a mode this library does not provide */
     TGVDCT_STOPPED = 6,         /* the loop ended early: the iteration callback or
                                    tgvdct_request_stop asked to stop, or the energy
                                    tolerance was met; outputs hold the state after
@@ -483,7 +483,7 @@ tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* ctx, float* u_dev, float* v
                                      tgvdct_iteration_callback callback, void* user,
                                      void* stream);
 
-/* ---- bounds checking (compute-sanitizer is not available to this build) -------- */
+/* ---- bounds checking (a device-side stand-in for compute-sanitizer) -------------- */
 /* In libtgvdct_checked.so (built with -DTGV_CHECK_BOUNDS) the iteration, adjoint and
    resize kernels check the indices they use and record the first bad one instead of
    making the access.  This call waits for the device, then returns that record

@@ -1,7 +1,7 @@
 """The bounds-checking build (libtgvdct_checked.so: every instrumented kernel checks
 the indices it is about to use and records the first bad one instead of making the
-access).  compute-sanitizer is not available on these GPUs; this build plus small and
-odd shapes stands in for it.  Each path must record nothing and give exactly the
+access).  compute-sanitizer is not available on these GPUs; the checked library plus
+small and odd shapes stands in for it.  Each path must record nothing and give exactly the
 normal library's results."""
 import ctypes
 
