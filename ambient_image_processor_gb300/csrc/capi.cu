@@ -38,6 +38,7 @@ struct tgvdct_context {
     // derived from it (voxels with mask >= 1 are iterated)
     float* domain_mask = nullptr;
     uint8_t* domain = nullptr;
+    uint32_t* tile_flags = nullptr;  // per-block plane ranges of the fused TMA kernel
     // CUDA graph of kGraphChunk iterations (an even number, so the ping-pong parity
     // of the state is unchanged after a replay), captured on a private stream and
     // replayed on the caller's; rebuilt when the step or the state changes
@@ -411,6 +412,7 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->cb_dev) cudaFree(c->cb_dev);
     if (c->domain_mask) cudaFree(c->domain_mask);
     if (c->domain) cudaFree(c->domain);
+    if (c->tile_flags) cudaFree(c->tile_flags);
     if (c->host_cb) cudaFreeHost(c->host_cb);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->bwd_graph) cudaGraphExecDestroy(c->bwd_graph);
@@ -455,17 +457,24 @@ void set_domain(tgvdct_context* c, const float* mask_dev, cudaStream_t s) {
         TGV_CUDA(cudaStreamSynchronize(s));
         if (c->domain_mask) TGV_CUDA(cudaFree(c->domain_mask));
         if (c->domain) TGV_CUDA(cudaFree(c->domain));
+        if (c->tile_flags) TGV_CUDA(cudaFree(c->tile_flags));
         c->domain_mask = nullptr;
         c->domain = nullptr;
+        c->tile_flags = nullptr;
         c->st.domain = nullptr;
+        c->st.tile_active = nullptr;
         return;
     }
     if (!c->domain) {
         if (cudaMalloc(&c->domain_mask, n * 4) != cudaSuccess ||
-            cudaMalloc(&c->domain, n) != cudaSuccess) {
+            cudaMalloc(&c->domain, n) != cudaSuccess ||
+            cudaMalloc(&c->tile_flags, tgv_tile_flags_bytes(c->st)) != cudaSuccess) {
             cudaGetLastError();
             if (c->domain_mask) cudaFree(c->domain_mask);
+            if (c->domain) cudaFree(c->domain);
             c->domain_mask = nullptr;
+            c->domain = nullptr;
+            c->tile_flags = nullptr;
             set_error("device allocation of the domain mask failed");
             throw Error{TGVDCT_ERR_OOM};
         }
@@ -473,6 +482,7 @@ void set_domain(tgvdct_context* c, const float* mask_dev, cudaStream_t s) {
     TGV_CUDA(cudaMemcpyAsync(c->domain_mask, mask_dev, n * 4, cudaMemcpyDeviceToDevice, s));
     build_domain(c->domain_mask, n, c->domain, s);
     c->st.domain = c->domain;
+    tgv_build_tile_flags(c->st, c->tile_flags, s);
 }
 
 struct CtxGuard {
@@ -877,7 +887,12 @@ tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p) {
                         kernel_of(*p) == kernel_of(ctx->prm),
                     "set_params cannot change geometry, state precision or iteration kernel");
         ctx->prm = *p;
-        ctx->st.zchunk = auto_zchunk(*p);
+        const int zchunk = auto_zchunk(*p);
+        if (zchunk != ctx->st.zchunk) {
+            ctx->st.zchunk = zchunk;
+            // the per-block domain flags follow the fused kernel's grid
+            if (ctx->st.domain) tgv_build_tile_flags(ctx->st, ctx->tile_flags, 0);
+        }
         return TGVDCT_OK;
     });
 }

@@ -125,6 +125,12 @@ struct TgvState {
     // updated and keep u = ubar = f, p = v = vbar = q = 0 (both sets of the fused
     // kernels hold those values).  Null: every voxel is updated.
     const uint8_t* domain = nullptr;
+    // Per-block plane ranges of the fused TMA kernel's grid for that domain (built for
+    // the z-chunk tile_zchunk): (first << 16) | end of the planes in which some of the
+    // block's own voxels are in the domain, 0 when there are none.  The block works on
+    // those planes only; the others are frozen.  Null: every block runs its chunk.
+    const uint32_t* tile_active = nullptr;
+    int tile_zchunk = 0;
     const TgvStencilFields& now() const { return set[cur]; }
 };
 
@@ -141,6 +147,10 @@ void tgv_state_bind(TgvState& s, char* base);
 void tgv_state_init(TgvState& s, cudaStream_t st);
 // domain[i] = mask[i] >= 1 (the masked processor's test, TGVDeshadeMaskedProcessor.cpp:347).
 void build_domain(const float* mask, size_t n, uint8_t* domain, cudaStream_t st);
+// Bytes of the fused kernel's per-block plane ranges (enough for any z-chunk).
+size_t tgv_tile_flags_bytes(const TgvState& s);
+// Fills `flags` from s.domain for the current z-chunk and points s.tile_active at it.
+void tgv_build_tile_flags(TgvState& s, uint32_t* flags, cudaStream_t st);
 // Snapshot of the whole loop state (f, u, v, and the current stencil set ubar, vbar,
 // p, q) into or out of one contiguous device buffer of tgv_snapshot_bytes.
 size_t tgv_snapshot_bytes(const TgvState& s);

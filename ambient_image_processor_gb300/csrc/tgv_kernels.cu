@@ -714,6 +714,8 @@ struct Args {
     int skip_bz;
     int* err;
     const uint8_t* dom;  // masked deshade domain (null: every voxel)
+    // per-block plane ranges of this grid for that domain (null: whole chunks)
+    const uint32_t* tile_active;
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -830,6 +832,20 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     float* sQ = sP + 2 * 3 * NE;                             // [3][6][NE]
     __shared__ uint64_t full[NS];
 
+    int zr0 = (int)blockIdx.z * a.zchunk, zr1 = min(a.D, zr0 + a.zchunk);
+    if constexpr (MASKED) {
+        // Only the planes in which some of this block's own voxels are in the domain
+        // have anything to update; none: the block leaves.  The other planes are frozen,
+        // and both stencil sets hold the values the neighbours read there.  One entry
+        // per block, so the whole block takes the same branch, before any barrier.
+        if (a.tile_active) {
+            const uint32_t r = a.tile_active[((size_t)blockIdx.z * gridDim.y + blockIdx.y) *
+                                                 gridDim.x + blockIdx.x];
+            if (r == 0) return;
+            zr0 = (int)(r >> 16);
+            zr1 = (int)(r & 0xffffu);
+        }
+    }
     // a pipeline wait of an earlier block or launch timed out: do nothing more
     // (one read, shared by the whole block, so every thread takes the same branch)
     if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
@@ -860,8 +876,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     interior = interior && in_dom;
     const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
     const int D = a.D;
-    const int z0 = (int)blockIdx.z * a.zchunk;
-    const int z1 = min(D, z0 + a.zchunk);
+    const int z0 = zr0, z1 = zr1;      // this block's planes
     const int pbase = max(z0 - 1, 0);  // first plane this block loads; slots count from it
     const int plast = min(D - 1, z1);  // last plane this block reads
     const size_t col = in_dom ? (size_t)y * a.W + x : 0;
@@ -1416,6 +1431,9 @@ void launch_tma(const tma::Args<typename Dual<PREC>::T>& a, cudaStream_t st) {
     TGV_CHECK_LAUNCH();
 }
 
+// planes per block of the fused TMA kernel's grid
+int tma_zchunk(const TgvState& s) { return s.three ? (s.zchunk > 0 ? s.zchunk : s.D) : 1; }
+
 // alpha^2 (1 - 2^-19), or -1 (never skip) where alpha^2 would leave the normal range
 float projection_skip_bound(float alpha) {
     const double a2 = (double)alpha * alpha;
@@ -1426,7 +1444,7 @@ float projection_skip_bound(float alpha) {
 template <int PREC, class T>
 void launch_tma_step(tma::Args<T> a, const TgvState& s, const TgvStep& k, int* err,
                      cudaStream_t st) {
-    a.zchunk = s.three ? (s.zchunk > 0 ? s.zchunk : s.D) : 1;
+    a.zchunk = tma_zchunk(s);
     a.tau = k.tau;
     a.sigma = k.sigma;
     a.theta = k.theta;
@@ -1442,6 +1460,8 @@ void launch_tma_step(tma::Args<T> a, const TgvState& s, const TgvStep& k, int* e
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
     a.err = err;
     a.dom = s.domain;
+    a.tile_active =
+        (s.domain && s.tile_active && s.tile_zchunk == a.zchunk) ? s.tile_active : nullptr;
     if (s.three) {
         if (k.data_term == TGVDCT_DATA_L1) launch_tma<PREC, true, TGVDCT_DATA_L1>(a, st);
         else launch_tma<PREC, true, TGVDCT_DATA_L2>(a, st);
@@ -1586,6 +1606,57 @@ void build_domain(const float* mask, size_t n, uint8_t* domain, cudaStream_t st)
     const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
     domain_kernel<<<blocks, 256, 0, st>>>(mask, n, domain);
     TGV_CHECK_LAUNCH();
+}
+
+namespace {
+// flags[(cz * gridDim.y + by) * gridDim.x + bx] for the fused TMA kernel's block
+// (bx, by, cz) -- columns [TX bx, TX bx + TX) x [TY by, TY by + TY), planes
+// [cz zchunk, (cz + 1) zchunk) -- is (first << 16) | (last + 1) over the planes in
+// which one of those columns is in the domain, or 0.  One thread per column.
+__global__ void tile_flags_kernel(const uint8_t* domain, int W, int H, int D, int zchunk,
+                                  uint32_t* flags) {
+    __shared__ int lo, hi;
+    if (threadIdx.x == 0) {
+        lo = D;
+        hi = -1;
+    }
+    __syncthreads();
+    const int x = blockIdx.x * tma::TX + (int)(threadIdx.x % tma::TX);
+    const int y = blockIdx.y * tma::TY + (int)(threadIdx.x / tma::TX);
+    if (x < W && y < H) {
+        const int z0 = (int)blockIdx.z * zchunk, z1 = min(D, z0 + zchunk);
+        int first = D, last = -1;
+        for (int z = z0; z < z1; ++z)
+            if (domain[((size_t)z * H + y) * W + x]) {
+                first = min(first, z);
+                last = z;
+            }
+        if (last >= 0) {
+            atomicMin(&lo, first);
+            atomicMax(&hi, last);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        flags[((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] =
+            hi >= 0 ? ((uint32_t)lo << 16) | (uint32_t)(hi + 1) : 0u;
+}
+}  // namespace
+
+size_t tgv_tile_flags_bytes(const TgvState& s) {
+    return (size_t)ceil_div(s.W, tma::TX) * ceil_div(s.H, tma::TY) * (size_t)s.D *
+           sizeof(uint32_t);
+}
+
+void tgv_build_tile_flags(TgvState& s, uint32_t* flags, cudaStream_t st) {
+    s.tile_active = nullptr;
+    if (!s.domain || !flags) return;
+    const int ez = tma_zchunk(s);
+    const dim3 grid(ceil_div(s.W, tma::TX), ceil_div(s.H, tma::TY), ceil_div(s.D, ez));
+    tile_flags_kernel<<<grid, tma::TX * tma::TY, 0, st>>>(s.domain, s.W, s.H, s.D, ez, flags);
+    TGV_CHECK_LAUNCH();
+    s.tile_active = flags;
+    s.tile_zchunk = ez;
 }
 
 bool tgv_uses_tma(const TgvState& s) { return tma_shape_ok(s); }

@@ -150,3 +150,40 @@ def test_masked_callback_gets_masked_deshade(gpu_lib):
     assert np.array_equal(u, fu) and np.array_equal(l, fl) and np.array_equal(r, fr)
     out = g["mask"] == 0
     assert not np.any(r[out]) and not np.any(l[out])
+
+
+def test_blocks_outside_the_domain_are_skipped_exactly(gpu_lib):
+    """A domain in one sub-box: most blocks of the fused kernel have no voxel in it and
+    leave at once (per-block flags).  The result is the two-pass kernels' bits and the
+    oracle's, also after set_params changes the z-chunk (the flags are rebuilt)."""
+    import torch
+    shape = (20, 40, 96)
+    d, h, w = shape
+    f = np.log(tissue_phantom_3d(*shape, seed=29)).astype(np.float32)
+    m = np.zeros(shape, np.float32)
+    m[3:9, 10:20, 40:70] = 1.0  # 12 of the 75 blocks at z-chunk 4 touch it
+    ft, mt = torch.from_numpy(f).cuda(), torch.from_numpy(m).cuda()
+
+    def run(kernel, z_chunk, z_chunk_after=None):
+        prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=40,
+                                 iteration_kernel=kernel, z_chunk=z_chunk)
+        u, vx, vy, vz = (torch.empty_like(ft) for _ in range(4))
+        with pkg.Context(prm) as ctx:
+            ctx.set_domain_mask_dev(mt.data_ptr())
+            if z_chunk_after is not None:
+                prm.z_chunk = z_chunk_after
+                ctx.set_params(prm)
+            ctx.run_dev(ft.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr())
+            torch.cuda.synchronize()
+            ctx.check_device_error()
+        return [t.cpu().numpy() for t in (u, vx, vy, vz)]
+
+    ref = run(pkg.KERNEL_TWO_PASS, 0)
+    for got in (run(pkg.KERNEL_FUSED, 4), run(pkg.KERNEL_FUSED, 4, z_chunk_after=7),
+                run(pkg.KERNEL_FUSED, 0)):
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+    ou, ovx, ovy, ovz = oracle.tgv2_deshade_masked(f, m, 1.0, 2.0, 1.0, 40, dtype=np.float32)
+    assert rel_l2(ref[0], ou) < TOL and rel_l2(ref[1], ovx) < TOL
+    out = m < 1
+    assert np.array_equal(ref[0][out], f[out])
