@@ -154,6 +154,25 @@ int auto_zchunk(const tgvdct_params& p) {
     return best_z;
 }
 
+// Planes per block when a domain mask is set.  The blocks' plane ranges are trimmed to
+// the domain and so differ in length; a grid of at most one wave keeps every block
+// resident at once and the longest one sets the time, so it takes half the chunk.  At
+// 128 x 128 x 96 with an ellipsoid domain: 55.6 -> 40.4 us per iteration (24 -> 12
+// planes); at 256 x 256 x 192 the unmasked choice stays the fastest.
+int masked_zchunk(const tgvdct_params& p) {
+    const int z = auto_zchunk(p);
+    if (p.z_chunk > 0) return z;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    const long long blocks = (long long)((p.width + 31) / 32) * ((p.height + 7) / 8) *
+                             (((long long)p.depth + z - 1) / z);
+    return blocks <= 2LL * sms ? std::max(1, (z + 1) / 2) : z;
+}
+
 void check_device() {
     int dev = 0, n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
@@ -463,6 +482,7 @@ void set_domain(tgvdct_context* c, const float* mask_dev, cudaStream_t s) {
         c->tile_flags = nullptr;
         c->st.domain = nullptr;
         c->st.tile_active = nullptr;
+        c->st.zchunk = auto_zchunk(c->prm);
         return;
     }
     if (!c->domain) {
@@ -482,6 +502,7 @@ void set_domain(tgvdct_context* c, const float* mask_dev, cudaStream_t s) {
     TGV_CUDA(cudaMemcpyAsync(c->domain_mask, mask_dev, n * 4, cudaMemcpyDeviceToDevice, s));
     build_domain(c->domain_mask, n, c->domain, s);
     c->st.domain = c->domain;
+    c->st.zchunk = masked_zchunk(c->prm);
     tgv_build_tile_flags(c->st, c->tile_flags, s);
 }
 
@@ -887,7 +908,7 @@ tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p) {
                         kernel_of(*p) == kernel_of(ctx->prm),
                     "set_params cannot change geometry, state precision or iteration kernel");
         ctx->prm = *p;
-        const int zchunk = auto_zchunk(*p);
+        const int zchunk = ctx->st.domain ? masked_zchunk(*p) : auto_zchunk(*p);
         if (zchunk != ctx->st.zchunk) {
             ctx->st.zchunk = zchunk;
             // the per-block domain flags follow the fused kernel's grid
