@@ -507,10 +507,7 @@ def run_ours(args):
     if rank == 0:
         extra = {}
         if not args.no_variants:
-            want = set(args.extras.split(",")) if args.extras else set(EXTRAS)
-            unknown = want - set(EXTRAS)
-            if unknown:
-                raise SystemExit(f"unknown --extras {sorted(unknown)}; known: {EXTRAS}")
+            want = set(filter(None, args.extras.split(","))) or set(EXTRAS)
             if "iteration_variants" in want:
                 var = {}
                 for kernel, prec in (("two_pass", 0), ("fused", 0), ("two_pass", 2),
@@ -656,6 +653,9 @@ def main():
     ap.add_argument("--accuracy", action="store_true",
                     help="error of every precision form against the FP64 oracle instead")
     args = ap.parse_args()
+    unknown = sorted(set(filter(None, args.extras.split(","))) - set(EXTRAS))
+    if unknown:  # before any device work
+        ap.error(f"unknown --extras {unknown}; known: {', '.join(EXTRAS)}")
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.accuracy:

@@ -65,3 +65,13 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch):
     line = json.loads(buf.getvalue())
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_unknown_extras_are_refused_before_device_work(monkeypatch, capsys):
+    """An unknown --extras name stops the bench at argument parsing, before it touches
+    a device (this runs on the CPU)."""
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--extras", "adjoint,bogus"])
+    with pytest.raises(SystemExit) as e:
+        bench.main()
+    assert e.value.code == 2
+    assert "bogus" in capsys.readouterr().err
