@@ -308,12 +308,15 @@ tgvdct_status tgvdct_check_device_error(tgvdct_context* ctx, void* stream);
    they run (their memory manager owns the GPU, their footprint is fixed in
    advance, or a cudaMalloc/cudaFree would synchronise a latency-critical
    pipeline): it calls no cudaMalloc, cudaFree or other allocating routine.  Its
-   scratch is one static device array of the library (about 18 MB, held by every
+   scratch is one static device array of the library (about 19 MB, held by every
    GPU that loads the library until the process exits), which limits the volume
    to TGVDCT_NOALLOC_MAX_VOXELS voxels with every side <= TGVDCT_NOALLOC_MAX_SIDE;
-   larger volumes are rejected with TGVDCT_ERR_BAD_ARG.  The first call on each
-   device looks up the array's device address (make that first call before any
-   stream capture).  All calls share the one array: calls that overlap on the
+   larger volumes are rejected with TGVDCT_ERR_BAD_ARG.  The first call in each
+   device context does set-up: it looks up the array's device address and fills
+   the array's exact fixed-point cosine tables, with one synchronous read on the
+   legacy default stream (make that first call before any stream capture).  A
+   context with a new id (after cudaDeviceReset, for one) gets the set-up again.
+   All calls share the one array: calls that overlap on the
    GPU (different streams, no ordering between them) race and corrupt each
    other's results, so order them, e.g. on one stream.  The caller passes v on
    the device (v_z_dev may be NULL when depth == 1) and the output l_dev.  Only

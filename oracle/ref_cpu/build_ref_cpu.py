@@ -26,7 +26,9 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
-DEFAULT_REFERENCE = "/root/reference"
+# the reference checkout: TGVDCT_REFERENCE_ROOT, else "reference" beside the repository
+DEFAULT_REFERENCE = os.environ.get(
+    "TGVDCT_REFERENCE_ROOT", os.path.join(os.path.dirname(os.path.dirname(ORACLE)), "reference"))
 
 MODULE_DIRS = ("tgv_cuda", "tgv_deshade", "tgv_deshade_masked", "cuda_image_operations")
 # translation units that provide the launchers ref_harness.cpp calls

@@ -68,3 +68,67 @@ def test_downsampled_deshade_at_factor_one_is_the_plain_processor():
     assert np.array_equal(l, ol * mask)
     with pytest.raises(ValueError):
         oracle.process_tgvk_l1_downsampled(f, 0.5, 1.0, 3, [1.0, 2.0, 3.0], 5)
+
+
+# ---- pin against an independent implementation of the same cubic B-spline -------
+# scipy.ndimage implements Unser's recursive prefilter (one pole z = sqrt(3) - 2) and
+# the cubic B-spline evaluation with a whole-sample-symmetric ("mirror") extension,
+# the boundary ITK's BSplineDecompositionImageFilter and BSplineInterpolateImageFunction
+# use.  The two differ only in summation order and in the causal start (ITK truncates
+# the mirror sum after ceil(log 1e-10 / log |z|) = 18 terms on longer lines; scipy sums
+# it in full), about 1e-11 of the line's scale in FP64.  The oracle then rounds once
+# to float32.  Tolerance: 2^-23 of the value (that rounding, twice over) plus 1e-9.
+
+def _scipy_resize(x, shape):
+    """ResizeProcessor's sample geometry (ResizeProcessor.cpp:55-90: size factor
+    out_grid / n in float, origin 0, two extra samples per axis when any axis grows,
+    the first `shape` samples kept) evaluated with scipy.ndimage."""
+    ndimage = pytest.importorskip("scipy.ndimage")
+    x64 = np.asarray(x, np.float64)
+    if x64.ndim == 2:
+        x64 = x64[None]
+    d, h, w = x64.shape
+    D, H, W = shape
+    up = W > w or H > h or D > d
+    axes = []
+    for n, out in ((d, D), (h, H), (w, W)):
+        grid = out + 2 if up else out
+        size_factor = np.float32(grid) / np.float32(n)  # float division, as the reference
+        spacing = 1.0 / np.float64(size_factor)
+        axes.append(np.arange(out, dtype=np.float64) * spacing)
+    coords = np.stack(np.meshgrid(*axes, indexing="ij"))
+    # a single-sample axis stays at its one sample (ITK's mirror index is 0 there)
+    keep = [n > 1 for n in (d, h, w)]
+    x_in = x64.reshape([n for n, k in zip((d, h, w), keep) if k])
+    c = coords[[i for i, k in enumerate(keep) if k]]
+    y = ndimage.map_coordinates(x_in, c, order=3, mode="mirror", prefilter=True)
+    return y.reshape(D, H, W)
+
+
+@pytest.mark.parametrize("src,dst", [
+    ((16, 24, 32), (8, 12, 16)),      # factor 0.5
+    ((20, 30, 33), (12, 18, 20)),     # factor 0.6, odd extents
+    ((9, 11, 40), (19, 23, 85)),      # upsampling (two extra samples, then cropped)
+    ((12, 12, 12), (29, 29, 29)),     # upsampling by 2.4
+    ((2, 3, 4), (1, 2, 2)),           # lines of 2-4 samples (closed mirror start)
+    ((3, 5, 17), (7, 11, 41)),        # short lines upsampled
+    ((1, 19, 37), (1, 10, 19)),       # a single plane
+])
+def test_resize_matches_scipy_cubic_bspline(src, dst):
+    x = np.random.default_rng(sum(src) + sum(dst)).standard_normal(src).astype(np.float32)
+    y = oracle.resize_bspline3(x, dst).reshape(dst)
+    s = _scipy_resize(x, dst)
+    assert np.all(np.abs(y - s) <= 2.0 ** -23 * np.abs(s) + 1e-9), float(np.abs(y - s).max())
+
+
+def test_resize_matches_scipy_at_the_down_sampled_deshade_geometry():
+    """The down-sampled deshade's round trip at factor 0.5 on the 256x256x192
+    workload's proportions, scaled to 64x64x48: down to 32x32x24, then back up."""
+    x = np.random.default_rng(9).standard_normal((48, 64, 64)).astype(np.float32)
+    down_shape = oracle.resize_factor_shape(x.shape, 0.5)
+    y = oracle.resize_bspline3(x, down_shape)
+    s = _scipy_resize(x, down_shape)
+    assert np.all(np.abs(y - s) <= 2.0 ** -23 * np.abs(s) + 1e-9)
+    back = oracle.resize_bspline3(y, x.shape)
+    sb = _scipy_resize(y, x.shape)
+    assert np.all(np.abs(back - sb) <= 2.0 ** -23 * np.abs(sb) + 1e-9)

@@ -20,13 +20,14 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 TOL_DCT = 1e-5  # as in test_parity_gpu.py
+NOALLOC_MAX_VOXELS = 1 << 21  # TGVDCT_NOALLOC_MAX_VOXELS in include/tgvdct.h
 
 
-def _noalloc(vx, vy, vz, shape, out, stream=None):
+def _noalloc(vx, vy, vz, shape, out, stream=None, eigen=None):
     d, h, w = shape
     return pkg.lib().tgvdct_integrate_poisson_noalloc_dev(
         vx.data_ptr(), vy.data_ptr(), vz.data_ptr() if vz is not None else None, w, h, d,
-        pkg.DCT_FP32, pkg.EIGEN_REFERENCE, out.data_ptr(), stream)
+        pkg.DCT_FP32, pkg.EIGEN_REFERENCE if eigen is None else eigen, out.data_ptr(), stream)
 
 
 def test_two_calls_in_a_row_match_the_allocating_entry_point(gpu_lib):
@@ -72,3 +73,45 @@ def test_rejects_volumes_beyond_the_static_scratch(gpu_lib):
                                                       None)
         assert st == pkg.ERR_BAD_ARG
         assert b"TGVDCT_NOALLOC_MAX" in lib.tgvdct_last_error()
+
+
+@pytest.mark.parametrize("shape", [(32, 256, 256), (256, 256, 32)])
+@pytest.mark.parametrize("eigen", ["reference", "accurate"])
+def test_largest_volumes_with_a_256_side(gpu_lib, shape, eigen):
+    """At TGVDCT_NOALLOC_MAX_VOXELS with a side of 256 the volumes fill the static
+    scratch and the cosine tables use their full rows."""
+    import torch
+
+    mode = pkg.EIGEN_REFERENCE if eigen == "reference" else pkg.EIGEN_ACCURATE
+    assert int(np.prod(shape)) == NOALLOC_MAX_VOXELS
+    rng = np.random.default_rng(11)
+    v = [rng.standard_normal(shape).astype(np.float32) for _ in range(3)]
+    ref = pkg.TGVDeshadeProcessor.integrate_image_gradients_poisson_cosine_transform(
+        *v, poisson_eigen=mode)
+    dev = [torch.from_numpy(a).cuda() for a in v]
+    outs = [torch.empty(shape, dtype=torch.float32, device="cuda") for _ in range(2)]
+    for out in outs:
+        assert _noalloc(*dev, shape, out, eigen=mode) == pkg.OK
+    torch.cuda.synchronize()
+    for out in outs:
+        assert rel_l2(out.cpu().numpy(), ref) < TOL_DCT
+
+
+def test_a_call_leaves_free_device_memory_unchanged(gpu_lib):
+    """After a first call (which loads the library's device code and does the
+    set-up), a call changes the device's free memory by nothing."""
+    import torch
+
+    shape = (64, 64, 64)
+    rng = np.random.default_rng(5)
+    dev = [torch.from_numpy(rng.standard_normal(shape).astype(np.float32)).cuda()
+           for _ in range(3)]
+    out = torch.empty(shape, dtype=torch.float32, device="cuda")
+    assert _noalloc(*dev, shape, out) == pkg.OK
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for eigen in (pkg.EIGEN_REFERENCE, pkg.EIGEN_ACCURATE):
+        assert _noalloc(*dev, shape, out, eigen=eigen) == pkg.OK
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
