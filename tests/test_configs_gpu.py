@@ -1,0 +1,191 @@
+"""Parity at the benchmark configurations themselves, not only at small shapes.
+
+Each configuration runs through the C ABI on the GPU and is compared with the CPU
+oracle on the same seeded input: with the FP32 oracle (the reference's float
+arithmetic, pinned bit-exactly to the reference's own kernels by
+test_oracle_golden.py) and with the FP64 oracle (the error of each precision form).
+
+  C1  2-D 512x512 TGV2-L1 denoise, 1000 iterations, tau = sigma = 1/sqrt(12)
+  C2  3-D 128^3 deshade, log domain, 2000 iterations, then the DCT Poisson integration
+  C3  the 256^3 DCT Poisson solve alone in FP32, TF32 and BF16x3
+  C5  the 256x256x192 deshade at its full shape, 300 of its 1500 iterations (the
+      bench line carries the full-length FP64 errors), in every precision form
+
+Tolerances are relative L2 norms, written beside each comparison.  Against the FP32
+oracle the only differences left are an ulp in CUDA's norm3df / sqrtf / cospif and
+the FP32 DCT contraction order; the nonsmooth prox and projection steps let an ulp
+grow over thousands of iterations, so the loop tolerances grow with the count.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import ambient_image_processor_gb300 as pkg
+import oracle
+from ambient_image_processor_gb300.phantoms import (cosine_modes_rhs, rectangles_ellipses_2d,
+                                                    tissue_phantom_3d)
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _threads():
+    import os
+    return oracle.set_threads(os.cpu_count() or 1)
+
+
+def _report(name, **errors):
+    print("MEASURED", name, " ".join(f"{k}={v:.3e}" for k, v in errors.items()))
+
+
+def _process_dev(f, iterations, *, state=pkg.STATE_FP32, dct=pkg.DCT_FP32,
+                 eigen=pkg.EIGEN_REFERENCE, kernel=pkg.KERNEL_AUTO):
+    """The whole deshade (loop, Poisson integration, r = u - l, no clamp) of a device
+    tensor through tgvdct_process_dev; returns host (u, l, r)."""
+    import torch
+    d, h, w = f.shape
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=iterations,
+                             state_precision=state, dct_mode=dct, poisson_eigen=eigen,
+                             iteration_kernel=kernel)
+    u, l, r = (torch.empty_like(f) for _ in range(3))
+    with pkg.Context(prm) as ctx:
+        ctx.process_dev(f.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
+                        set_negative_values_to_zero=False)
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+    return u.cpu().numpy(), l.cpu().numpy(), r.cpu().numpy()
+
+
+# ---- C1 ------------------------------------------------------------------------
+def test_c1_denoise_2d_512_1000_iterations(gpu_lib):
+    import torch
+    _threads()
+    f = rectangles_ellipses_2d(512, 512, seed=1)
+    step = 1.0 / math.sqrt(12.0)
+    prm = pkg.default_params(width=512, height=512, depth=1, iteration_count=1000,
+                             geometry=pkg.GEOMETRY_2D)
+    prm.tau = prm.sigma = step
+    ft = torch.from_numpy(f).cuda()
+    u, vx, vy = (torch.empty_like(ft) for _ in range(3))
+    with pkg.Context(prm) as ctx:
+        ctx.run_dev(ft.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), None)
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+    u = u.cpu().numpy()
+    o32, *_ = oracle.tgv2_deshade(f, 1.0, 2.0, 1.0, 1000, tau=step, sigma=step, two_d=True,
+                                  dtype=np.float32)
+    o64, *_ = oracle.tgv2_deshade(f.astype(np.float64), 1.0, 2.0, 1.0, 1000, tau=step,
+                                  sigma=step, two_d=True, dtype=np.float64)
+    e32, e64, e_oracle = rel_l2(u, o32), rel_l2(u, o64), rel_l2(o32, o64)
+    _report("c1", vs_f32=e32, vs_f64=e64, oracle_f32_vs_f64=e_oracle)
+    assert e32 < 1e-5   # the reference's float arithmetic
+    assert e64 < 1e-5   # FP32 against FP64
+
+
+# ---- C2 ------------------------------------------------------------------------
+def test_c2_deshade_128cube_2000_iterations(gpu_lib):
+    import torch
+    _threads()
+    flog = np.log(tissue_phantom_3d(128, 128, 128, seed=2)).astype(np.float32)
+    u, l, r = _process_dev(torch.from_numpy(flog).cuda(), 2000)
+    o32 = oracle.process_tgv2_l1(flog, 1.0, 2.0, 1.0, 2000, set_negative_values_to_zero=False,
+                                 dtype=np.float32)
+    o64 = oracle.process_tgv2_l1(flog.astype(np.float64), 1.0, 2.0, 1.0, 2000,
+                                 set_negative_values_to_zero=False, dtype=np.float64)
+    errs = {}
+    for name, got, a, b in zip("ulr", (u, l, r), o32, o64):
+        errs[name + "_vs_f32"] = rel_l2(got, a)
+        errs[name + "_vs_f64"] = rel_l2(got, b)
+    _report("c2", **errs)
+    # against the reference's float arithmetic (the same eigenvalue formula)
+    assert errs["u_vs_f32"] < 1e-5 and errs["r_vs_f32"] < 1e-5
+    assert errs["l_vs_f32"] < 1e-4
+    # against FP64: the reference eigenvalues' float cosines dominate l's error
+    assert errs["u_vs_f64"] < 1e-5 and errs["r_vs_f64"] < 1e-4 and errs["l_vs_f64"] < 1e-4
+
+
+# ---- C3 ------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def c3_oracle():
+    _threads()
+    rhs = cosine_modes_rhs(256, 256, 256, seed=3)
+    x = rhs.astype(np.float64)
+    l64 = oracle.inverse_cosine_transform(oracle.solve_poisson(oracle.cosine_transform(x)))
+    l32 = oracle.inverse_cosine_transform(oracle.solve_poisson(oracle.cosine_transform(rhs)))
+    return rhs, l32, l64
+
+
+@pytest.mark.parametrize("mode,eigen,tol64", [
+    ("fp32", "reference", 1e-4),
+    ("fp32", "accurate", 1e-5),
+    ("bf16x3", "accurate", 3e-5),
+    ("tf32", "accurate", 5e-3),
+])
+def test_c3_poisson_256cube(gpu_lib, c3_oracle, mode, eigen, tol64):
+    import torch
+    rhs, l32, l64 = c3_oracle
+    dct = {"fp32": pkg.DCT_FP32, "tf32": pkg.DCT_TF32, "bf16x3": pkg.DCT_BF16X3}[mode]
+    eig = pkg.EIGEN_REFERENCE if eigen == "reference" else pkg.EIGEN_ACCURATE
+    prm = pkg.default_params(width=256, height=256, depth=256, dct_mode=dct, poisson_eigen=eig)
+    rt = torch.from_numpy(rhs).cuda()
+    out = torch.empty_like(rt)
+    with pkg.Context(prm) as ctx:
+        ctx.poisson_solve_dev(rt.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+    got = out.cpu().numpy()
+    e64 = rel_l2(got, l64)
+    e32 = rel_l2(got, l32)
+    _report(f"c3_{mode}_{eigen}", vs_f64=e64, vs_f32_oracle=e32)
+    assert e64 < tol64
+    if (mode, eigen) == ("fp32", "reference"):
+        assert e32 < 1e-5  # the reference's float solve
+
+
+# ---- C5 ------------------------------------------------------------------------
+C5_ITERATIONS = 300
+
+
+@pytest.fixture(scope="module")
+def c5_case():
+    _threads()
+    flog = np.log(tissue_phantom_3d(192, 256, 256, seed=2)).astype(np.float32)
+    o32 = oracle.process_tgv2_l1(flog, 1.0, 2.0, 1.0, C5_ITERATIONS,
+                                 set_negative_values_to_zero=False, dtype=np.float32)
+    o64 = oracle.process_tgv2_l1(flog.astype(np.float64), 1.0, 2.0, 1.0, C5_ITERATIONS,
+                                 set_negative_values_to_zero=False, dtype=np.float64)
+    return flog, o32, o64
+
+
+# (state, dct, eigen) -> relative L2 bounds of (u, l, r) against FP64 at 300 iterations
+C5_FORMS = {
+    ("fp32", "fp32", "reference"): (1e-6, 2e-5, 2e-5),
+    ("fp32", "fp32", "accurate"): (1e-6, 2e-6, 2e-6),
+    ("fp32", "bf16x3", "accurate"): (1e-6, 5e-6, 5e-6),
+    ("fp32", "tf32", "accurate"): (1e-6, 1e-4, 1e-4),
+    ("fx16", "fp32", "accurate"): (3e-4, 1e-3, 3e-4),
+    ("bf16", "fp32", "accurate"): (1e-2, 1e-1, 1e-1),
+}
+
+
+@pytest.mark.parametrize("form", list(C5_FORMS), ids=lambda f: "-".join(f))
+def test_c5_deshade_256x256x192_full_shape(gpu_lib, c5_case, form):
+    import torch
+    flog, o32, o64 = c5_case
+    state, dct, eigen = form
+    got = _process_dev(torch.from_numpy(flog).cuda(), C5_ITERATIONS,
+                       state={"fp32": pkg.STATE_FP32, "bf16": pkg.STATE_BF16_DUAL,
+                              "fx16": pkg.STATE_FX16_DUAL}[state],
+                       dct={"fp32": pkg.DCT_FP32, "tf32": pkg.DCT_TF32,
+                            "bf16x3": pkg.DCT_BF16X3}[dct],
+                       eigen=pkg.EIGEN_REFERENCE if eigen == "reference" else pkg.EIGEN_ACCURATE)
+    errs = {n + "_vs_f64": rel_l2(g, b) for n, g, b in zip("ulr", got, o64)}
+    if form == ("fp32", "fp32", "reference"):
+        errs.update({n + "_vs_f32": rel_l2(g, a) for n, g, a in zip("ulr", got, o32)})
+    _report("c5_" + "_".join(form), **errs)
+    for n, tol in zip("ulr", C5_FORMS[form]):
+        assert errs[n + "_vs_f64"] < tol, (n, errs)
+    if form == ("fp32", "fp32", "reference"):
+        # the reference's float arithmetic at the full shape
+        assert errs["u_vs_f32"] < 1e-5 and errs["l_vs_f32"] < 1e-5 and errs["r_vs_f32"] < 1e-5
