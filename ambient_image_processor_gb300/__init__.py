@@ -128,6 +128,16 @@ _SIGS = {
     "tgvdct_state_save_dev": [_vp, _vp, _vp],
     "tgvdct_state_load_dev": [_vp, _vp, _vp],
     "tgvdct_tgv2_resume_dev": [_vp, _vp, _vp, _vp, _vp, CALLBACK, _vp, _vp],
+    "tgvdct_state_init_dev": [_vp, _vp, _vp],
+    "tgvdct_tgv2_step_dev": [_vp, _u32, _vp],
+    "tgvdct_state_planes_bytes": [_vp, _u32, _u32],
+    "tgvdct_state_read_dev": [_vp, _u32, _u32, _u32, _vp, _vp],
+    "tgvdct_state_write_dev": [_vp, _u32, _u32, _u32, _vp, _vp],
+    "tgvdct_slab_poisson_xy_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "tgvdct_slab_poisson_inverse_yx_dev": [_vp, _vp, _vp, _u32, _u32, _vp],
+    "tgvdct_pencil_create": [_u32, _u32, _u32, ctypes.c_uint64, ctypes.POINTER(_vp)],
+    "tgvdct_pencil_destroy": [_vp],
+    "tgvdct_pencil_poisson_z_dev": [_vp, _vp, _vp, ctypes.c_uint64, _i32, _vp],
     "tgvdct_resize_bspline3": [_f32p, _u32, _u32, _u32, _f32p, _u32, _u32, _u32],
     "tgvdct_resize_bspline3_dev": [_vp, _u32, _u32, _u32, _vp, _u32, _u32, _u32, _vp],
     "tgvdct_resize_factor_extent": [_u32, _flt],
@@ -142,7 +152,8 @@ _RESTYPES = {"tgvdct_params_init": None, "tgvdct_workspace_bytes": ctypes.c_size
              "tgvdct_iterations_run": ctypes.c_uint32, "tgvdct_version": ctypes.c_char_p,
              "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p,
              "tgvdct_resize_factor_extent": ctypes.c_uint32,
-             "tgvdct_state_bytes": ctypes.c_size_t}
+             "tgvdct_state_bytes": ctypes.c_size_t,
+             "tgvdct_state_planes_bytes": ctypes.c_size_t}
 
 # symbols of include/tgvdct.h (checked by the CPU test suite)
 EXPORTED = sorted(set(_SIGS) | {"tgvdct_version", "tgvdct_last_error", "tgvdct_status_string"})

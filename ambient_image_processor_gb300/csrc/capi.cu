@@ -998,6 +998,205 @@ tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* c, float* u_dev, float* v_x
     });
 }
 
+// ---- z-slab decomposition: state access by planes, single steps, Poisson pieces ----
+}  // extern "C"
+namespace {
+
+// The state field a field-mask bit names (current stencil set for ubar, vbar, p, q),
+// with its element size; null when the state has no such field (v_z in 2-D).
+void* state_field(const TgvState& s, int bit, size_t* elem) {
+    const TgvStencilFields& F = s.now();
+    *elem = 4;
+    switch (bit) {
+        case 0: return s.f;
+        case 1: return s.u;
+        case 2: case 3: case 4: return s.v[bit - 2];
+        case 5: return F.ubar;
+        case 6: case 7: case 8: return F.vbar[bit - 6];
+        default: break;
+    }
+    *elem = s.precision == TGVDCT_STATE_FP32 ? 4 : 2;
+    if (bit >= 9 && bit <= 11) return F.p[bit - 9];
+    if (bit >= 12 && bit <= 17) return F.q[bit - 12];
+    return nullptr;
+}
+
+// Runs fn(field pointer, bytes of one plane) over the fields of `mask` in bit order.
+template <class Fn>
+void for_each_masked_field(const TgvState& s, uint32_t mask, Fn&& fn) {
+    TGV_REQUIRE((mask & ~TGVDCT_FIELD_ALL) == 0, "unknown bits in the field mask");
+    const size_t plane = (size_t)s.W * s.H;
+    for (int bit = 0; bit < 18; ++bit) {
+        if (!(mask & (1u << bit))) continue;
+        size_t e = 0;
+        void* f = state_field(s, bit, &e);
+        TGV_REQUIRE(f != nullptr, "the field mask names a field this state does not have");
+        fn((char*)f, plane * e);
+    }
+}
+
+}  // namespace
+extern "C" {
+
+tgvdct_status tgvdct_state_init_dev(tgvdct_context* c, const float* f_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(f_dev != nullptr, "null device buffer");
+        cudaStream_t s = (cudaStream_t)stream;
+        TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, voxels(c->prm) * 4, cudaMemcpyDeviceToDevice, s));
+        tgv_state_init(c->st, s);
+        c->iterations_run = 0;
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_tgv2_step_dev(tgvdct_context* c, uint32_t iterations, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        const TgvStep k = step_of(c->prm);
+        for (uint32_t i = 0; i < iterations; ++i) tgv_iterate(c->st, k, (cudaStream_t)stream);
+        c->iterations_run = iterations;
+        return TGVDCT_OK;
+    });
+}
+
+size_t tgvdct_state_planes_bytes(const tgvdct_context* c, uint32_t field_mask,
+                                 uint32_t plane_count) {
+    if (!c) return 0;
+    size_t b = 0;
+    try {
+        for_each_masked_field(c->st, field_mask,
+                              [&](char*, size_t plane_bytes) { b += plane_bytes * plane_count; });
+    } catch (const Error&) {
+        return 0;
+    }
+    return b;
+}
+
+tgvdct_status tgvdct_state_read_dev(tgvdct_context* c, uint32_t field_mask, uint32_t plane_begin,
+                                    uint32_t plane_count, void* dst_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(dst_dev != nullptr, "null device buffer");
+        TGV_REQUIRE((uint64_t)plane_begin + plane_count <= c->prm.depth, "planes out of range");
+        char* d = (char*)dst_dev;
+        for_each_masked_field(c->st, field_mask, [&](char* f, size_t plane_bytes) {
+            const size_t n = plane_bytes * plane_count;
+            TGV_CUDA(cudaMemcpyAsync(d, f + plane_bytes * plane_begin, n,
+                                     cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+            d += n;
+        });
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_state_write_dev(tgvdct_context* c, uint32_t field_mask,
+                                     uint32_t plane_begin, uint32_t plane_count,
+                                     const void* src_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(src_dev != nullptr, "null device buffer");
+        TGV_REQUIRE((uint64_t)plane_begin + plane_count <= c->prm.depth, "planes out of range");
+        const char* d = (const char*)src_dev;
+        for_each_masked_field(c->st, field_mask, [&](char* f, size_t plane_bytes) {
+            const size_t n = plane_bytes * plane_count;
+            TGV_CUDA(cudaMemcpyAsync(f + plane_bytes * plane_begin, d, n,
+                                     cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+            d += n;
+        });
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_slab_poisson_xy_dev(tgvdct_context* c, const float* v_x_dev,
+                                         const float* v_y_dev, const float* v_z_dev,
+                                         float* out_dev, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(v_x_dev && v_y_dev && v_z_dev && out_dev, "null device buffer");
+        TGV_REQUIRE(c->prm.depth > 1 && c->st.three, "a slab is a 3-D volume of depth > 1");
+        if (c->prm.dct_mode != TGVDCT_DCT_FP32) {
+            set_error("the slab Poisson passes run the FP32 contractions only");
+            return TGVDCT_ERR_UNSUPPORTED;
+        }
+        slab_poisson_xy(plan_of(c), v_x_dev, v_y_dev, v_z_dev, out_dev, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_slab_poisson_inverse_yx_dev(tgvdct_context* c, const float* in_dev,
+                                                 float* out_dev, uint32_t plane_count,
+                                                 uint32_t total_depth, void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        TGV_REQUIRE(in_dev && out_dev, "null device buffer");
+        TGV_REQUIRE(plane_count >= 1 && plane_count <= c->prm.depth, "plane_count out of range");
+        TGV_REQUIRE(total_depth >= plane_count, "total_depth below plane_count");
+        if (c->prm.dct_mode != TGVDCT_DCT_FP32) {
+            set_error("the slab Poisson passes run the FP32 contractions only");
+            return TGVDCT_ERR_UNSUPPORTED;
+        }
+        // the single-volume scale 1 / (8 W H D) of the whole volume
+        const float scale =
+            (float)(1.0 / ((double)c->prm.width * c->prm.height * total_depth * 8.0));
+        slab_poisson_inverse_yx(plan_of(c), in_dev, out_dev, (int)plane_count, scale,
+                                (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
+struct tgvdct_pencil {
+    DctPlan* plan = nullptr;
+    uint64_t columns = 0;
+};
+
+tgvdct_status tgvdct_pencil_create(uint32_t width, uint32_t height, uint32_t depth,
+                                   uint64_t columns, tgvdct_pencil** out) {
+    return guarded([&] {
+        TGV_REQUIRE(out != nullptr, "null output pointer");
+        *out = nullptr;
+        TGV_REQUIRE(width >= 1 && height >= 1 && depth >= 2, "a pencil needs depth >= 2");
+        TGV_REQUIRE(columns >= 1 && columns <= (uint64_t)width * height,
+                    "columns must be in 1 .. width * height");
+        TGV_REQUIRE((uint64_t)depth * columns < ((uint64_t)1 << 31), "pencil too large");
+        auto* p = new tgvdct_pencil();
+        try {
+            p->plan = dct_plan_create((int)width, (int)height, (int)depth,
+                                      (size_t)depth * columns);
+        } catch (...) {
+            delete p;
+            throw;
+        }
+        p->columns = columns;
+        *out = p;
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_pencil_destroy(tgvdct_pencil* p) {
+    if (!p) return TGVDCT_OK;
+    dct_plan_destroy(p->plan);
+    delete p;
+    return TGVDCT_OK;
+}
+
+tgvdct_status tgvdct_pencil_poisson_z_dev(tgvdct_pencil* p, const float* in_dev, float* out_dev,
+                                          uint64_t column_begin, int32_t poisson_eigen,
+                                          void* stream) {
+    return guarded([&] {
+        TGV_REQUIRE(p != nullptr, "null pencil");
+        TGV_REQUIRE(in_dev && out_dev, "null device buffer");
+        TGV_REQUIRE(column_begin + p->columns <= (uint64_t)p->plan->W * p->plan->H,
+                    "the pencil's columns run past the plane");
+        TGV_REQUIRE(poisson_eigen == TGVDCT_EIGEN_REFERENCE ||
+                        poisson_eigen == TGVDCT_EIGEN_ACCURATE,
+                    "unknown Poisson eigenvalue mode");
+        pencil_poisson_z(p->plan, in_dev, out_dev, (long long)p->columns, (long long)column_begin,
+                         poisson_eigen, (cudaStream_t)stream);
+        return TGVDCT_OK;
+    });
+}
+
 tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const float* f_dev,
                                                    float* u_dev, float* v_x_dev,
                                                    float* v_y_dev, float* v_z_dev,

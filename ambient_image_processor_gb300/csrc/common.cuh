@@ -261,9 +261,21 @@ void pass_tc(DctPlan* p, int axis, bool inverse, const float* in, float* out, in
 bool dct_pipe_supported(const DctPlan* p);
 bool pass_pipe(DctPlan* p, int axis, bool inverse, const float* in, float* out, int epi,
                float scale, int dct_mode, cudaStream_t st);
-DctPlan* dct_plan_create(int W, int H, int D);
+// tmp_voxels: size of each of the two scratch volumes (0: W * H * D)
+DctPlan* dct_plan_create(int W, int H, int D, size_t tmp_voxels = 0);
 void dct_plan_destroy(DctPlan* p);
-size_t dct_plan_bytes(int W, int H, int D);
+size_t dct_plan_bytes(int W, int H, int D, size_t tmp_voxels = 0);
+// z-slab decomposition of poisson_integrate (FP32): the divergence and the forward x, y
+// passes over a slab's planes; the forward and inverse z passes (with the division) on
+// a pencil of `columns` columns starting at column col_off of the W*H plane (a plan of
+// the whole volume's shape whose scratch holds D * columns); the inverse y, x passes
+// (x scaled) over `planes` planes.
+void slab_poisson_xy(DctPlan* p, const float* vx, const float* vy, const float* vz, float* out,
+                     cudaStream_t st);
+void pencil_poisson_z(DctPlan* p, const float* in, float* out, long long columns,
+                      long long col_off, int eigen_mode, cudaStream_t st);
+void slab_poisson_inverse_yx(DctPlan* p, const float* in, float* out, int planes, float scale,
+                             cudaStream_t st);
 
 // l = DCT-III( DCT-II(div v) / eigenvalue ) with the reference's scale factors.
 void poisson_integrate(DctPlan* plan, const float* vx, const float* vy, const float* vz,

@@ -76,6 +76,7 @@ struct GemmArgs {
     // epilogue
     float scale;
     int pz_layout;  // 1: outputs indexed (i = ky, j = kx); 2: (i = kz, j = ky*W + kx)
+    long long col_off;  // layout 2 on a pencil: the global index of output column j = 0
     const long long* fx0;  // DctPlan::cosk_fx (null: the FP64 form)
     const long long* fx1;
     const long long* fx2;
@@ -167,7 +168,12 @@ __global__ void __launch_bounds__(NT) gemm_kernel(GemmArgs g) {
             } else if constexpr (EPI == EPI_POISSON_REF || EPI == EPI_POISSON_ACC) {
                 int kx, ky, kz;
                 if (g.pz_layout == 1) { kx = gj; ky = gi; kz = 0; }
-                else { kx = gj % g.W; ky = gj / g.W; kz = gi; }
+                else {
+                    const long long gc = gj + g.col_off;
+                    kx = (int)(gc % g.W);
+                    ky = (int)(gc / g.W);
+                    kz = gi;
+                }
                 v = v * 8.f;  // the forward transform's last-pass factor
                 if (kx == 0 && ky == 0 && kz == 0) {
                     v = 0.f;
@@ -209,10 +215,11 @@ GemmArgs base_args(const DctPlan* p) {
 }
 
 // One separable pass along `axis` with matrix Mat (N x N row-major).
+// planes > 0: the x and y passes run over that many planes instead of the plan's depth.
 void pass(const DctPlan* p, int axis, const float* Mat, const float* in, float* out, int epi,
           float scale, int aload, const float* vx, const float* vy, const float* vz,
-          cudaStream_t st) {
-    const long long W = p->W, H = p->H, D = p->D, WH = W * H;
+          cudaStream_t st, int planes = 0) {
+    const long long W = p->W, H = p->H, D = planes > 0 ? planes : p->D, WH = W * H;
     GemmArgs g = base_args(p);
     g.scale = scale;
     g.vx = vx;
@@ -393,22 +400,24 @@ unsigned ew_grid(size_t n) {
 
 }  // namespace
 
-size_t dct_plan_bytes(int W, int H, int D) {
+size_t dct_plan_bytes(int W, int H, int D, size_t tmp_voxels) {
     size_t b = 0;
     const int N[3] = {W, H, D};
     for (int a = 0; a < 3; ++a)
         b += 2 * a256((size_t)N[a] * N[a] * 4) + 2 * a256((size_t)N[a] * 4) +
              a256((size_t)N[a] * 8);
-    b += 2 * a256((size_t)W * H * D * 4) + 256;
+    if (tmp_voxels == 0) tmp_voxels = (size_t)W * H * D;
+    b += 2 * a256(tmp_voxels * 4) + 256;
     return b;
 }
 
-DctPlan* dct_plan_create(int W, int H, int D) {
+DctPlan* dct_plan_create(int W, int H, int D, size_t tmp_voxels) {
     DctPlan* p = new DctPlan();
     p->W = W;
     p->H = H;
     p->D = D;
-    const size_t bytes = dct_plan_bytes(W, H, D);
+    if (tmp_voxels == 0) tmp_voxels = (size_t)W * H * D;
+    const size_t bytes = dct_plan_bytes(W, H, D, tmp_voxels);
     cudaError_t e = cudaMalloc(&p->block, bytes);
     if (e != cudaSuccess) {
         delete p;
@@ -452,9 +461,9 @@ DctPlan* dct_plan_create(int W, int H, int D) {
         }
     }
     p->tmp[0] = (float*)c;
-    c += a256((size_t)W * H * D * 4);
+    c += a256(tmp_voxels * 4);
     p->tmp[1] = (float*)c;
-    c += a256((size_t)W * H * D * 4);
+    c += a256(tmp_voxels * 4);
     int* inexact = (int*)c;
     cudaError_t se = cudaMemset(inexact, 0, sizeof(int));
     const bool small = W <= 256 && H <= 256 && D <= 256;
@@ -563,11 +572,13 @@ void poisson_solve(DctPlan* p, const float* rhs, float* l, int dct_mode, int eig
         any_pass(p, 0, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 1, true, t0, l, EPI_SCALE, s, dct_mode, st);
     } else {
+        // forward x, y, z (+ division); inverse z, y, x: the z contractions are adjacent,
+        // so a z-slab decomposition needs one transposition to z pencils and one back
         any_pass(p, 1, false, t0, t1, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 2, false, t1, t0, epi, 1.f, dct_mode, st);
-        any_pass(p, 0, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 1, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
-        any_pass(p, 2, true, t0, l, EPI_SCALE, s, dct_mode, st);
+        any_pass(p, 0, true, t0, l, EPI_SCALE, s, dct_mode, st);
     }
 }
 
@@ -594,11 +605,64 @@ void poisson_integrate(DctPlan* p, const float* vx, const float* vy, const float
         any_pass(p, 0, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 1, true, t0, l, EPI_SCALE, s, dct_mode, st);
     } else {
+        // forward x, y, z (+ division); inverse z, y, x: the z contractions are adjacent,
+        // so a z-slab decomposition needs one transposition to z pencils and one back
         any_pass(p, 1, false, t0, t1, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 2, false, t1, t0, epi, 1.f, dct_mode, st);
-        any_pass(p, 0, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
+        any_pass(p, 2, true, t0, t1, EPI_NONE, 1.f, dct_mode, st);
         any_pass(p, 1, true, t1, t0, EPI_NONE, 1.f, dct_mode, st);
-        any_pass(p, 2, true, t0, l, EPI_SCALE, s, dct_mode, st);
+        any_pass(p, 0, true, t0, l, EPI_SCALE, s, dct_mode, st);
+    }
+}
+
+// ---- z-slab decomposition of the Poisson integration (FP32 contractions) ---------
+// The single-volume order is: divergence fused into the forward x pass, forward y,
+// forward z with the division, inverse z, inverse y, inverse x (scaled).  A rank
+// that holds z-planes runs the x and y passes on its planes, the z passes run on z
+// pencils (all planes of a span of columns), and the inverse y and x passes run on
+// the rank's planes again.  Each output value is the same dot product, accumulated
+// in the same order, as in the single-volume solve, so the results agree bit for bit.
+
+void slab_poisson_xy(DctPlan* p, const float* vx, const float* vy, const float* vz, float* out,
+                     cudaStream_t st) {
+    pass(p, 0, p->fwd[0], nullptr, p->tmp[0], EPI_NONE, 1.f, A_DIVERGENCE, vx, vy, vz, st);
+    pass(p, 1, p->fwd[1], p->tmp[0], out, EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st);
+}
+
+void slab_poisson_inverse_yx(DctPlan* p, const float* in, float* out, int planes, float scale,
+                             cudaStream_t st) {
+    pass(p, 1, p->inv[1], in, p->tmp[0], EPI_NONE, 1.f, A_PLAIN, 0, 0, 0, st, planes);
+    pass(p, 0, p->inv[0], p->tmp[0], out, EPI_SCALE, scale, A_PLAIN, 0, 0, 0, st, planes);
+}
+
+// in, out: D x columns (z-major), the columns [col_off, col_off + columns) of the
+// W*H plane; forward z (x 8, the division by the Laplacian eigenvalues, DC = 0),
+// then inverse z.  Uses tmp[0] (D x columns).
+void pencil_poisson_z(DctPlan* p, const float* in, float* out, long long columns,
+                      long long col_off, int eigen_mode, cudaStream_t st) {
+    const int epi = eigen_mode == TGVDCT_EIGEN_ACCURATE ? EPI_POISSON_ACC : EPI_POISSON_REF;
+    for (int step = 0; step < 2; ++step) {
+        GemmArgs g = base_args(p);
+        g.M = p->D;
+        g.N = (int)columns;
+        g.K = p->D;
+        g.A = step == 0 ? p->fwd[2] : p->inv[2];
+        g.sAi = p->D;
+        g.sAk = 1;
+        g.B = step == 0 ? in : p->tmp[0];
+        g.sBk = columns;
+        g.sBj = 1;
+        g.C = step == 0 ? p->tmp[0] : out;
+        g.sCi = columns;
+        g.sCj = 1;
+        g.pz_layout = 2;
+        g.col_off = col_off;
+        g.fx0 = p->cosk_fx[0];
+        g.fx1 = p->cosk_fx[1];
+        g.fx2 = p->cosk_fx[2];
+        if (step == 1) launch_gemm<A_PLAIN, EPI_NONE>(g, 1, st);
+        else if (epi == EPI_POISSON_ACC) launch_gemm<A_PLAIN, EPI_POISSON_ACC>(g, 1, st);
+        else launch_gemm<A_PLAIN, EPI_POISSON_REF>(g, 1, st);
     }
 }
 

@@ -486,6 +486,76 @@ tgvdct_status tgvdct_tgv2_resume_dev(tgvdct_context* ctx, float* u_dev, float* v
                                      tgvdct_iteration_callback callback, void* user,
                                      void* stream);
 
+/* ---- z-slab decomposition (building blocks; no counterpart in the reference) ----
+   The reference runs one volume on one device (tgv_cuda/tgv_common.cu:249-253).  To
+   spread a volume over several GPUs along z, each rank holds a context for its slab of
+   planes plus one halo plane on each side that has a neighbour; the host moves halo
+   planes and pencils between ranks with its own transport (NCCL, MPI, ...).  After
+   every iteration a rank copies its first own plane's ubar and vbar into the rank
+   below (that rank's top halo) and its last own plane's into the rank above (its
+   bottom halo).  p and q at the halo planes need no exchange: p takes forward
+   differences of ubar and q backward differences of vbar, so the bottom halo's p and
+   the top halo's q are computed exactly from the halo and the own plane next to it.
+   Every own plane then advances exactly as in the single volume.
+   ambient_image_processor_gb300/slab.py is the host side over torch.distributed. */
+/* Field-mask bits of the loop state (ubar, vbar, p, q: the current stencil set). */
+#define TGVDCT_FIELD_F (1u << 0)
+#define TGVDCT_FIELD_U (1u << 1)
+#define TGVDCT_FIELD_V (7u << 2)     /* v_x, v_y, v_z */
+#define TGVDCT_FIELD_UBAR (1u << 5)
+#define TGVDCT_FIELD_VBAR (7u << 6)  /* vbar_x, vbar_y, vbar_z */
+#define TGVDCT_FIELD_P (7u << 9)     /* p_x, p_y, p_z */
+#define TGVDCT_FIELD_Q (63u << 12)   /* q_xx, q_yy, q_zz, q_xy, q_xz, q_yz */
+#define TGVDCT_FIELD_ALL ((1u << 18) - 1u)
+/* what a rank's halo planes receive from its neighbours after every iteration */
+#define TGVDCT_HALO_FIELDS (TGVDCT_FIELD_UBAR | TGVDCT_FIELD_VBAR)
+/* The loop's starting state from f (u = ubar = f, p = q = v = vbar = 0), no iteration. */
+tgvdct_status tgvdct_state_init_dev(tgvdct_context* ctx, const float* f_dev, void* stream);
+/* Advances the state by `iterations` iterations (no callbacks, no output copies). */
+tgvdct_status tgvdct_tgv2_step_dev(tgvdct_context* ctx, uint32_t iterations, void* stream);
+/* Bytes that tgvdct_state_read_dev / _write_dev move for these fields and planes
+   (p, q in the context's dual element size); 0 for a bad mask. */
+size_t tgvdct_state_planes_bytes(const tgvdct_context* ctx, uint32_t field_mask,
+                                 uint32_t plane_count);
+/* Copies planes [plane_begin, plane_begin + plane_count) of each field of the mask, in
+   bit order, field after field, out of (read) or into (write) one device buffer.
+   Stream-ordered. */
+tgvdct_status tgvdct_state_read_dev(tgvdct_context* ctx, uint32_t field_mask,
+                                    uint32_t plane_begin, uint32_t plane_count, void* dst_dev,
+                                    void* stream);
+tgvdct_status tgvdct_state_write_dev(tgvdct_context* ctx, uint32_t field_mask,
+                                     uint32_t plane_begin, uint32_t plane_count,
+                                     const void* src_dev, void* stream);
+/* The Poisson integration of tgvdct_poisson_integrate_dev split for z-slabs (FP32
+   contractions, dct_mode TGVDCT_DCT_FP32).  Its single-volume order is: divergence
+   fused into the forward x pass, forward y, forward z with the eigenvalue division,
+   inverse z, inverse y, inverse x (scaled).  A rank runs
+     1. tgvdct_slab_poisson_xy_dev on its context's planes (v with the bottom halo
+        plane's v_z from the rank below): divergence, forward x, forward y;
+     2. sends each rank its columns of its own planes and receives its pencil: all D
+        planes of the columns [column_begin, column_begin + columns) of the W*H plane;
+     3. tgvdct_pencil_poisson_z_dev: forward z, division, inverse z on the pencil;
+     4. sends the pencil back by planes and receives its own planes;
+     5. tgvdct_slab_poisson_inverse_yx_dev over its own planes: inverse y, inverse x
+        scaled by 1 / (8 W H total_depth).
+   Every value is the same dot product, summed in the same order, as in the single
+   volume: the slab result equals tgvdct_poisson_integrate_dev's bit for bit. */
+tgvdct_status tgvdct_slab_poisson_xy_dev(tgvdct_context* ctx, const float* v_x_dev,
+                                         const float* v_y_dev, const float* v_z_dev,
+                                         float* out_dev, void* stream);
+tgvdct_status tgvdct_slab_poisson_inverse_yx_dev(tgvdct_context* ctx, const float* in_dev,
+                                                 float* out_dev, uint32_t plane_count,
+                                                 uint32_t total_depth, void* stream);
+typedef struct tgvdct_pencil tgvdct_pencil;
+/* A pencil of the width x height x depth volume: `columns` columns, all depth planes
+   (z-major, columns contiguous), with the z cosine tables and D * columns of scratch. */
+tgvdct_status tgvdct_pencil_create(uint32_t width, uint32_t height, uint32_t depth,
+                                   uint64_t columns, tgvdct_pencil** out);
+tgvdct_status tgvdct_pencil_destroy(tgvdct_pencil* pencil);
+tgvdct_status tgvdct_pencil_poisson_z_dev(tgvdct_pencil* pencil, const float* in_dev,
+                                          float* out_dev, uint64_t column_begin,
+                                          int32_t poisson_eigen, void* stream);
+
 /* ---- bounds checking (a device-side stand-in for compute-sanitizer) -------------- */
 /* In libtgvdct_checked.so (built with -DTGV_CHECK_BOUNDS) the iteration, adjoint and
    resize kernels check the indices they use and record the first bad one instead of

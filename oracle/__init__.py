@@ -65,6 +65,10 @@ def lib() -> ctypes.CDLL:
             fn.argtypes = [p, p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int,
                            ctypes.c_int, p, p, p, p]
             fn.restype = _u
+        for suf in ("f32", "f64"):
+            fn = getattr(L, f"oracle_tgv2_step_{suf}")
+            fn.argtypes = [ctypes.c_void_p, _u, _u, _u, _d, _d, _d, _u, _d, _d, _d, ctypes.c_int,
+                           ctypes.c_int]
         L.oracle_resize_bspline3_f32.argtypes = [_f32p, _u, _u, _u, _f32p, _u, _u, _u]
         L.oracle_resize_factor_extent.argtypes = [_u, ctypes.c_float]
         L.oracle_resize_factor_extent.restype = _u
@@ -109,6 +113,39 @@ def tgv2_deshade(f, lambda_=1.0, alpha0=2.0, alpha1=1.0, iterations=100, *, tau=
         f, w, h, d, lambda_, alpha0, alpha1, iterations, tau, sigma, theta, dt, int(two_d),
         u, vx, vy, vz)
     return u, vx, vy, vz
+
+
+# the persistent fields of one loop state, in the order oracle_tgv2_step_* takes them
+STATE_FIELDS = ("f", "u", "u_bar", "p_x", "p_y", "p_z", "v_x", "v_y", "v_z", "vbar_x", "vbar_y",
+                "vbar_z", "q_xx", "q_yy", "q_zz", "q_xy", "q_xz", "q_yz")
+
+
+def tgv2_initial_state(f):
+    """The loop's starting state: u = u_bar = f, every other field 0 (a dict of arrays
+    keyed by STATE_FIELDS, shaped like f)."""
+    f = np.ascontiguousarray(f)
+    st = {k: np.zeros_like(f) for k in STATE_FIELDS}
+    st["f"][...] = f
+    st["u"][...] = f
+    st["u_bar"][...] = f
+    return st
+
+
+def tgv2_step(state, iterations=1, lambda_=1.0, alpha0=2.0, alpha1=1.0, *, tau=0.0, sigma=0.0,
+              theta=1.0, data_term="l1", two_d=False):
+    """Advances a loop state (a dict from tgv2_initial_state, updated in place) by
+    `iterations` iterations of the restated loop: the arithmetic of tgv2_deshade."""
+    arrs = [state[k] for k in STATE_FIELDS]
+    dtype = arrs[0].dtype
+    for a in arrs:
+        if a.dtype != dtype or not a.flags.c_contiguous or a.shape != arrs[0].shape:
+            raise ValueError("state fields must be C-contiguous arrays of one shape and dtype")
+    w, h, d = _shape3(arrs[0])
+    ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    dt = 0 if data_term in ("l1", 0) else 1
+    getattr(lib(), f"oracle_tgv2_step_{_dt(dtype)}")(
+        ptrs, w, h, d, lambda_, alpha0, alpha1, iterations, tau, sigma, theta, dt, int(two_d))
+    return state
 
 
 def divergence(vx, vy, vz):

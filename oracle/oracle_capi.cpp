@@ -1,5 +1,6 @@
 // TEST INFRASTRUCTURE — extern "C" entry points of the CPU oracle (tgv_oracle.hpp),
 // loaded by tests/ and bench.py's CPU-baseline leg through ctypes.  Not product code.
+#include <algorithm>
 #include <vector>
 
 #include "tgv_adjoint.hpp"
@@ -92,6 +93,31 @@ int oracle_set_threads(int n) {
                                                    sigma, theta, data_term, two_d),               \
                                        u, vx, vy, vz, nullptr, dom.data());                       \
     }
+
+// Iterations on an explicit loop state, in place: the 17 persistent fields (f is
+// read only) in the order f, u, u_bar, p_x, p_y, p_z, v_x, v_y, v_z, vbar_x, vbar_y,
+// vbar_z, q_xx, q_yy, q_zz, q_xy, q_xz, q_yz; each w*h*d values.  The same iteration
+// as oracle_tgv2_deshade_*, which starts from u = u_bar = f and zeros.
+#define ORACLE_STEP(T, SUF)                                                                       \
+    void oracle_tgv2_step_##SUF(T* const* fields, unsigned w, unsigned h, unsigned d,            \
+                                double lambda, double alpha0, double alpha1,                      \
+                                unsigned iterations, double tau, double sigma, double theta,      \
+                                int data_term, int two_d) {                                       \
+        const Dims g = dims(w, h, d);                                                             \
+        const index_t n = g.n();                                                                  \
+        oracle::LoopState<T> st(fields[0], n);                                                    \
+        std::vector<T>* v[18] = {&st.f,   &st.u,   &st.u_bar, &st.px,  &st.py,  &st.pz,          \
+                                 &st.vx,  &st.vy,  &st.vz,    &st.vbx, &st.vby, &st.vbz,         \
+                                 &st.qxx, &st.qyy, &st.qzz,   &st.qxy, &st.qxz, &st.qyz};        \
+        for (int k = 1; k < 18; ++k) std::copy(fields[k], fields[k] + n, v[k]->begin());        \
+        const oracle::Params prm = make_params(lambda, alpha0, alpha1, iterations, tau, sigma,    \
+                                               theta, data_term, two_d);                          \
+        for (unsigned it = 0; it < iterations; ++it) oracle::tgv2_iteration(st, g, prm);         \
+        for (int k = 1; k < 18; ++k) std::copy(v[k]->begin(), v[k]->end(), fields[k]);          \
+    }
+ORACLE_STEP(float, f32)
+ORACLE_STEP(double, f64)
+#undef ORACLE_STEP
 
 #define ORACLE_CONVERGENCE(T, SUF)                                                                \
     unsigned oracle_convergence_test_##SUF(const T* f, const T* mask, unsigned w, unsigned h,    \

@@ -129,28 +129,47 @@ using IterCallback = std::function<bool(unsigned, unsigned, const T*, const T*, 
 // TGVDeshadeMaskedProcessor.cpp:337-385).  Voxels with domain[i] == 0 are never
 // updated: they keep u = u_bar = f and p = v = v_bar = q = 0, and the differences
 // taken at updated voxels read those values.
+// The loop state of tgv2_deshade: the persistent fields (f, u, u_bar, p, v, v_bar, q)
+// and the temporaries one iteration uses.
 template <class T>
-unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_out,
-                      T* vy_out, T* vz_out, IterCallback<T> cb = nullptr,
-                      const unsigned char* domain = nullptr) {
+struct LoopState {
+    std::vector<T> f, u, u_prev, u_bar;
+    std::vector<T> gx, gy, gz;                                  // p_x, p_y, p_z temporaries
+    std::vector<T> px, py, pz;                                  // p dual (p_xx, p_yy, p_zz)
+    std::vector<T> vx, vy, vz, vbx, vby, vbz, vpx, vpy, vpz;
+    std::vector<T> qxx, qyy, qzz, qxy, qxz, qyz;                // q dual
+    std::vector<T> exx, eyy, ezz, exy, exz, eyz, tmp;           // temps
+    explicit LoopState(const T* f_in, index_t n)
+        : f(f_in, f_in + n), u(f), u_prev(n), u_bar(f), gx(n), gy(n), gz(n), px(n, 0),
+          py(n, 0), pz(n, 0), vx(n, 0), vy(n, 0), vz(n, 0), vbx(n, 0), vby(n, 0), vbz(n, 0),
+          vpx(n), vpy(n), vpz(n), qxx(n, 0), qyy(n, 0), qzz(n, 0), qxy(n, 0), qxz(n, 0),
+          qyz(n, 0), exx(n), eyy(n), ezz(n), exy(n), exz(n), eyz(n), tmp(n) {}
+};
+
+// One iteration of the loop below, in place on the state.
+template <class T>
+void tgv2_iteration(LoopState<T>& st, Dims g, const Params& prm,
+                    const unsigned char* domain = nullptr) {
     const index_t n = g.n();
     const bool three = !prm.two_d;
     const T tau = T(prm.tau > 0 ? prm.tau : default_step());
     const T sigma = T(prm.sigma > 0 ? prm.sigma : default_step());
     const T theta = T(prm.theta);
     const T lambda = T(prm.lambda), alpha0 = T(prm.alpha0), alpha1 = T(prm.alpha1);
-
-    std::vector<T> f(f_in, f_in + n), u(f), u_prev(n), u_bar(f);
-    std::vector<T> gx(n), gy(n), gz(n);                         // p_x, p_y, p_z temporaries
-    std::vector<T> px(n, 0), py(n, 0), pz(n, 0);                // p dual (p_xx, p_yy, p_zz)
-    std::vector<T> vx(n, 0), vy(n, 0), vz(n, 0);
-    std::vector<T> vbx(n, 0), vby(n, 0), vbz(n, 0);
-    std::vector<T> vpx(n), vpy(n), vpz(n);
-    std::vector<T> qxx(n, 0), qyy(n, 0), qzz(n, 0), qxy(n, 0), qxz(n, 0), qyz(n, 0);  // q dual
-    std::vector<T> exx(n), eyy(n), ezz(n), exy(n), exz(n), eyz(n), tmp(n);            // temps
-
-    unsigned it = 0;
-    for (; it < prm.iterations; ++it) {
+    auto& f = st.f;
+    auto& u = st.u;
+    auto& u_prev = st.u_prev;
+    auto& u_bar = st.u_bar;
+    auto &gx = st.gx, &gy = st.gy, &gz = st.gz;
+    auto &px = st.px, &py = st.py, &pz = st.pz;
+    auto &vx = st.vx, &vy = st.vy, &vz = st.vz;
+    auto &vbx = st.vbx, &vby = st.vby, &vbz = st.vbz;
+    auto &vpx = st.vpx, &vpy = st.vpy, &vpz = st.vpz;
+    auto &qxx = st.qxx, &qyy = st.qyy, &qzz = st.qzz, &qxy = st.qxy, &qxz = st.qxz,
+         &qyz = st.qyz;
+    auto &exx = st.exx, &eyy = st.eyy, &ezz = st.ezz, &exy = st.exy, &exz = st.exz,
+         &eyz = st.eyz, &tmp = st.tmp;
+    {
         // 1. forward differences of u_bar, p update and projection, u_prev = u
         forward_diff(0, u_bar.data(), gx.data(), g);
         forward_diff(1, u_bar.data(), gy.data(), g);
@@ -282,6 +301,22 @@ unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_
                 vbz[i] = T(vz[i] + T(theta * T(vz[i] - vpz[i])));
             }
         }
+    }
+}
+
+template <class T>
+unsigned tgv2_deshade(const T* f_in, Dims g, const Params& prm, T* u_out, T* vx_out,
+                      T* vy_out, T* vz_out, IterCallback<T> cb = nullptr,
+                      const unsigned char* domain = nullptr) {
+    const index_t n = g.n();
+    const bool three = !prm.two_d;
+    LoopState<T> st(f_in, n);
+    auto& u = st.u;
+    auto &vx = st.vx, &vy = st.vy, &vz = st.vz;
+
+    unsigned it = 0;
+    for (; it < prm.iterations; ++it) {
+        tgv2_iteration(st, g, prm, domain);
         // 7. iteration callback (tgv_cuda/tgv2_common.cu:374-408)
         if (cb && prm.paint_interval > 0 && it > 0 && it % prm.paint_interval == 0) {
             if (cb(it, prm.iterations, u.data(), vx.data(), vy.data(), three ? vz.data() : nullptr)) {
