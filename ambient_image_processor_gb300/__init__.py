@@ -111,6 +111,7 @@ _SIGS = {
     "tgvdct_poisson_integrate_dev": [_vp, _vp, _vp, _vp, _vp, _vp],
     "tgvdct_poisson_solve_dev": [_vp, _vp, _vp, _vp],
     "tgvdct_check_device_error": [_vp, _vp],
+    "tgvdct_set_pipeline_wait_limit": [_vp, ctypes.c_uint64],
     "tgvdct_integrate_poisson_noalloc_dev": [_vp, _vp, _vp, _u32, _u32, _u32, _i32, _i32, _vp,
                                              _vp],
     "tgvdct_deshade_epilogue_dev": [_vp, _vp, _vp, ctypes.c_uint64, _i32, _i32, _i32, _vp, _vp],
@@ -743,6 +744,10 @@ class Context:
     def request_stop(self):
         """Ask the loop running on this context (or the next one) to stop; thread-safe."""
         _check(lib().tgvdct_request_stop(self._ctx))
+
+    def set_pipeline_wait_limit(self, limit_ns: int):
+        """Limit of the pipelines' bounded waits (tgvdct_set_pipeline_wait_limit)."""
+        _check(lib().tgvdct_set_pipeline_wait_limit(self._ctx, int(limit_ns)), allow_stop=False)
 
     def check_device_error(self, stream=None):
         _check(lib().tgvdct_check_device_error(self._ctx, stream), allow_stop=False)

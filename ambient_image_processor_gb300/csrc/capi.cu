@@ -219,7 +219,10 @@ tgvdct_status guarded(F&& f) {
 }
 
 DctPlan* plan_of(tgvdct_context* c) {
-    if (!c->plan) c->plan = dct_plan_create((int)c->prm.width, (int)c->prm.height, (int)c->prm.depth);
+    if (!c->plan) {
+        c->plan = dct_plan_create((int)c->prm.width, (int)c->prm.height, (int)c->prm.depth);
+        c->plan->wait_ns = c->st.wait_ns;
+    }
     return c->plan;
 }
 
@@ -1664,6 +1667,24 @@ tgvdct_status tgvdct_poisson_integrate_adjoint_dev(tgvdct_context* c, const floa
         if (grad_v_z_dev && c->prm.depth == 1)
             TGV_CUDA(cudaMemsetAsync(grad_v_z_dev, 0, n * 4, s));
         TGV_CUDA(cudaStreamSynchronize(s));  // the scratch is freed on return
+        return TGVDCT_OK;
+    });
+}
+
+tgvdct_status tgvdct_set_pipeline_wait_limit(tgvdct_context* c, uint64_t limit_ns) {
+    return guarded([&] {
+        TGV_REQUIRE(c != nullptr, "null context");
+        c->st.wait_ns = limit_ns;
+        if (c->plan) c->plan->wait_ns = limit_ns;
+        // the loop and backward graphs hold the old limit in their kernel arguments
+        if (c->graph) {
+            cudaGraphExecDestroy(c->graph);
+            c->graph = nullptr;
+        }
+        if (c->bwd_graph) {
+            cudaGraphExecDestroy(c->bwd_graph);
+            c->bwd_graph = nullptr;
+        }
         return TGVDCT_OK;
     });
 }

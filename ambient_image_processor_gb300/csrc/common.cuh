@@ -121,6 +121,8 @@ struct TgvState {
     // shapes the TMA stride rules exclude)
     std::shared_ptr<void> tma_cache;
     int* err = nullptr;      // device flag raised by a pipeline wait that timed out
+    // limit of the fused TMA kernel's pipeline waits (tgvdct_set_pipeline_wait_limit)
+    uint64_t wait_ns = 200000000ull;
     // Optional domain of the masked deshade: voxels with domain[i] == 0 are never
     // updated and keep u = ubar = f, p = v = vbar = q = 0 (both sets of the fused
     // kernels hold those values).  Null: every voxel is updated.
@@ -237,6 +239,8 @@ struct DctPlan {
     uint16_t* bf_lo[2][3] = {};
     float* tf[2][3] = {};
     int* dev_err = nullptr;                        // set by a tensor-core pass whose wait timed out
+    // limit of the pipelined tensor-core passes' waits (tgvdct_set_pipeline_wait_limit)
+    uint64_t wait_ns = 200000000ull;
     void* tc_block = nullptr;
     // pipelined tensor-core passes (dct_tc2.cu): the matrices as shared-memory stage
     // images, [BF16X3, TF32][fwd, inv][axis], and their number of K stages

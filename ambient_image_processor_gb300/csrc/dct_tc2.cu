@@ -98,6 +98,7 @@ struct PArgs {
     const long long* fx1;
     const long long* fx2;
     int* err;
+    unsigned long long wait_ns;  // limit of the roles' pipeline waits (0: one test)
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -119,15 +120,24 @@ __device__ __forceinline__ bool mtest(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait.  With honour_abort, returns false as soon as another role gave up.
+// Bounded wait.  With honour_abort (the roles' pipeline waits), returns false as soon
+// as another role gave up, and gives up after limit_ns (limit_ns == 0: at the first
+// test that finds the phase open).  Without it (the drain of an error exit), waits up
+// to P_WAIT_NS whatever limit_ns says.
 __device__ bool mwait(uint64_t* bar, uint32_t parity, int* err, volatile int* abort,
-                      bool honour_abort) {
+                      bool honour_abort, uint64_t limit_ns = P_WAIT_NS) {
     if (mtest(bar, parity)) return true;
+    if (!honour_abort) limit_ns = P_WAIT_NS;
+    if (limit_ns == 0) {
+        atomicExch(err, 1);
+        *abort = 1;
+        return false;
+    }
     const uint64_t t0 = gtimer();
     while (true) {
         if (mtest(bar, parity)) return true;
         if (honour_abort && *abort) return false;
-        if (gtimer() - t0 > P_WAIT_NS) {
+        if (gtimer() - t0 > limit_ns) {
             atomicExch(err, 1);
             *abort = 1;
             return false;
@@ -337,7 +347,7 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
                 for (int c = 0; c < nch; ++c, ++gc) {
                     const int s = gc % P_STAGES;
                     if (gc >= P_STAGES &&
-                        !mwait(&empty[s], (uint32_t)((gc / P_STAGES - 1) & 1), g.err, abort, true)) {
+                        !mwait(&empty[s], (uint32_t)((gc / P_STAGES - 1) & 1), g.err, abort, true, g.wait_ns)) {
                         go = false;
                         break;
                     }
@@ -360,7 +370,7 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
         for (long long t = blockIdx.x; t < ntiles && go; t += gridDim.x) {
             for (int c = 0; c < nch; ++c, ++gc) {
                 const int s = gc % P_STAGES;
-                if (!mwait(&full[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true)) {
+                if (!mwait(&full[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true, g.wait_ns)) {
                     go = false;
                     break;
                 }
@@ -410,13 +420,13 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
                 const int b = ti & 1;
                 // the epilogue of tile ti - 2 has read accumulator b
                 if (ti >= 2 &&
-                    !mwait(&acc_empty[b], (uint32_t)((ti / 2 - 1) & 1), g.err, abort, true))
+                    !mwait(&acc_empty[b], (uint32_t)((ti / 2 - 1) & 1), g.err, abort, true, g.wait_ns))
                     break;
                 tc_after();
                 const uint32_t acc_t = tmem + (uint32_t)b * acols;
                 for (int c = 0; c < nch; ++c, ++gc) {
                     const int s = gc % P_STAGES;
-                    if (!mwait(&conv[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true)) {
+                    if (!mwait(&conv[s], (uint32_t)((gc / P_STAGES) & 1), g.err, abort, true, g.wait_ns)) {
                         go = false;
                         break;
                     }
@@ -452,7 +462,7 @@ __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_con
         int ti = 0;
         for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++ti) {
             const int b = ti & 1;
-            if (!mwait(&acc_full[b], (uint32_t)((ti / 2) & 1), g.err, abort, true)) break;
+            if (!mwait(&acc_full[b], (uint32_t)((ti / 2) & 1), g.err, abort, true, g.wait_ns)) break;
             tc_after();
             const long long line = (t % ntl) * P_M + q * 32 + lane;
             const int batch = (int)(t / ntl);
@@ -722,6 +732,7 @@ bool pass_pipe(DctPlan* p, int axis, bool inverse, const float* in, float* out, 
     a.eig1 = p->eig[1];
     a.eig2 = p->eig[2];
     a.err = p->dev_err;
+    a.wait_ns = p->wait_ns;
     a.fx0 = p->cosk_fx[0];
     a.fx1 = p->cosk_fx[1];
     a.fx2 = p->cosk_fx[2];

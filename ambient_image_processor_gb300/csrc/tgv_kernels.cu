@@ -657,7 +657,10 @@ constexpr int TX = 32, TY = 8;
 constexpr int EXW = TX + 2, EYH = TY + 2, NE = EXW * EYH;  // 34 x 10 positions
 constexpr int NTHREADS = 352;                              // 8 interior + 3 halo warps
 constexpr int PRODUCER = 256;                              // first halo thread issues TMA
-constexpr uint64_t WAIT_NS = 200000000ull;  // 200 ms: a plane normally lands in microseconds
+// 200 ms: a plane normally lands in microseconds.  The consumers' waits take their
+// limit from the launch (tgvdct_set_pipeline_wait_limit; this is the default); the
+// drain of a block's own copies on an error exit always waits up to this long.
+constexpr uint64_t WAIT_NS = 200000000ull;
 // u, f and v of plane t + TILE_PREFETCH are prefetched into L2 at step t
 constexpr int TILE_PREFETCH = 3;
 
@@ -713,6 +716,7 @@ struct Args {
     float penc, pdec, qenc, qdec;
     int skip_bz;
     int* err;
+    unsigned long long wait_ns;  // limit of the consumers' pipeline waits (0: one test)
     const uint8_t* dom;  // masked deshade domain (null: every voxel)
     // per-block plane ranges of this grid for that domain (null: whole chunks)
     const uint32_t* tile_active;
@@ -732,14 +736,19 @@ __device__ __forceinline__ bool mtest(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-__device__ bool mwait(uint64_t* bar, uint32_t parity, int* err) {
+// Bounded wait; limit_ns == 0 gives up at the first test that finds the phase open.
+__device__ bool mwait(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns) {
     if (mtest(bar, parity)) return true;
+    if (limit_ns == 0) {
+        atomicExch(err, 1);
+        return false;
+    }
     uint64_t t0, t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
     while (true) {
         if (mtest(bar, parity)) return true;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > WAIT_NS) {
+        if (t - t0 > limit_ns) {
             atomicExch(err, 1);
             return false;
         }
@@ -960,7 +969,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     auto wait_plane = [&](int plane) {
         if (plane < 0 || plane > plast || plane <= waited_upto) return;
         const int j = (plane - pbase) / NS;
-        if (!mwait(&full[(plane - pbase) % NS], j & 1, a.err)) ok = false;
+        if (!mwait(&full[(plane - pbase) % NS], j & 1, a.err, a.wait_ns)) ok = false;
         else waited_upto = plane;
     };
     // p_new over R_p from stage sz (plane z) and sn (plane z+1, or null past the volume):
@@ -1213,7 +1222,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     if (!ok && tid == PRODUCER) {
         for (int pl = max(waited_upto + 1, 0); pl <= min(issued_upto, plast); ++pl) {
             const int j = (pl - pbase) / NS;
-            mwait(&full[(pl - pbase) % NS], j & 1, a.err);
+            mwait(&full[(pl - pbase) % NS], j & 1, a.err, WAIT_NS);
         }
     }
     __syncthreads();
@@ -1459,6 +1468,7 @@ void launch_tma_step(tma::Args<T> a, const TgvState& s, const TgvStep& k, int* e
     a.thr_q = projection_skip_bound(k.alpha0);
     a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
     a.err = err;
+    a.wait_ns = s.wait_ns;
     a.dom = s.domain;
     a.tile_active =
         (s.domain && s.tile_active && s.tile_zchunk == a.zchunk) ? s.tile_active : nullptr;

@@ -298,10 +298,20 @@ tgvdct_status tgvdct_poisson_solve_dev(tgvdct_context* ctx, const float* rhs_dev
 tgvdct_status tgvdct_poisson_integrate_adjoint_dev(tgvdct_context* ctx, const float* grad_l_dev,
                                                    float* grad_v_x_dev, float* grad_v_y_dev,
                                                    float* grad_v_z_dev, void* stream);
-/* Reads and clears the device error flag of the tensor-core DCT passes of a context
-   (set when one of their bounded waits timed out); synchronises the stream.
-   Returns TGVDCT_ERR_CUDA if the flag was set. */
+/* Reads and clears the device error flags of a context: the TGV iteration kernels'
+   and the tensor-core DCT passes' (raised when one of their bounded waits ran out);
+   synchronises the stream.  Returns TGVDCT_ERR_TIMEOUT if a flag was set. */
 tgvdct_status tgvdct_check_device_error(tgvdct_context* ctx, void* stream);
+/* The limit, in nanoseconds, of the bounded waits with which the fused TMA iteration
+   kernel and the pipelined tensor-core DCT passes of this context wait for their
+   staged data: default 200 ms; 0 gives up at the first test that finds the data not
+   yet there.  A wait that runs out raises the context's device error flag; the pass
+   stops, each of its blocks first letting its own copies and tensor-core operations
+   in flight finish (those waits always allow 200 ms), and later launches return at
+   once.  tgvdct_check_device_error (or the next host-buffer call) then returns
+   TGVDCT_ERR_TIMEOUT and clears the flag; the context stays usable.  No counterpart
+   in the reference, whose cudaCheckError prints and exits (cuda_helper.in:11-21). */
+tgvdct_status tgvdct_set_pipeline_wait_limit(tgvdct_context* ctx, uint64_t limit_ns);
 
 /* Allocation-free form of tgvdct_poisson_integrate_dev.  It has no counterpart in
    the reference.  It is for callers that must not allocate device memory while
