@@ -46,6 +46,9 @@ template <>
 struct Dual<TGVDCT_STATE_FP32> {
     using T = float;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float) { return p[i]; }
+    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float) {
+        return __ldcg(p + i);
+    }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) { p[i] = v; }
     // streaming store (evict-first): the next read of the field is an iteration away
     static __device__ __forceinline__ void st_cs(T* p, size_t i, float v, float) {
@@ -58,6 +61,9 @@ struct Dual<TGVDCT_STATE_BF16_DUAL> {
     using T = __nv_bfloat16;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float) {
         return __bfloat162float(p[i]);
+    }
+    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float) {
+        return __bfloat162float(__ushort_as_bfloat16(__ldcg((const unsigned short*)p + i)));
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) {
         p[i] = __float2bfloat16_rn(v);
@@ -79,6 +85,11 @@ struct Dual<TGVDCT_STATE_FX16_DUAL> {
     using T = int16_t;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float dec) {
         const float c = __int_as_float(0x4B400000 + (int)p[i]) - 12582912.f;  // exact
+        return c * dec;
+    }
+    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float dec) {
+        const float c = __int_as_float(0x4B400000 + (int)__ldcg((const short*)p + i)) -
+                        12582912.f;
         return c * dec;
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float enc) {
@@ -132,14 +143,26 @@ struct TgvArgs {
 
 constexpr int BX = 32, BY = 8;
 
-// Dual pass.  THREE: 3-D operators (also for D == 1); otherwise the 2-D launcher.
-template <int PREC, bool THREE>
-__global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<PREC>::T> a) {
+// Loads of the two-pass updates: plain in the per-iteration kernels; through L2 only
+// (ld.global.cg) in the persistent single-plane kernel, whose other blocks write the
+// fields between its passes.
+template <bool CG>
+__device__ __forceinline__ float ldf(const float* p, size_t i) {
+    if constexpr (CG) return __ldcg(p + i);
+    else return p[i];
+}
+template <class S, bool CG>
+__device__ __forceinline__ float ldd(const typename S::T* p, size_t i, float dec) {
+    if constexpr (CG) return S::ld_cg(p, i, dec);
+    else return S::ld(p, i, dec);
+}
+
+// The dual update at voxel (x, y, z), in place.  THREE: 3-D operators (also for
+// D == 1); otherwise the 2-D launcher.
+template <int PREC, bool THREE, bool CG>
+__device__ __forceinline__ void dual_update(const TgvArgs<typename Dual<PREC>::T>& a, int x,
+                                            int y, int z) {
     using S = Dual<PREC>;
-    const int x = blockIdx.x * BX + threadIdx.x;
-    const int y = blockIdx.y * BY + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
     if (!TGV_IN_BOUNDS(i, WH * a.D, 1)) return;
@@ -147,17 +170,17 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     if (a.dom && !a.dom[i]) return;
 
     // p <- proj(p + sigma (F ubar - vbar))          (tgv2_common.cu:118-130)
-    const float ub = a.ubar[i];
-    const float gx = (x + 1 < a.W) ? a.ubar[i + 1] - ub : 0.f;
-    const float gy = (y + 1 < a.H) ? a.ubar[i + W] - ub : 0.f;
-    const float vbx = a.vb0[i], vby = a.vb1[i];
-    float px = __fmaf_rn(a.sigma, gx - vbx, S::ld(a.pin[0], i, a.pdec));
-    float py = __fmaf_rn(a.sigma, gy - vby, S::ld(a.pin[1], i, a.pdec));
+    const float ub = ldf<CG>(a.ubar, i);
+    const float gx = (x + 1 < a.W) ? ldf<CG>(a.ubar, i + 1) - ub : 0.f;
+    const float gy = (y + 1 < a.H) ? ldf<CG>(a.ubar, i + W) - ub : 0.f;
+    const float vbx = ldf<CG>(a.vb0, i), vby = ldf<CG>(a.vb1, i);
+    float px = __fmaf_rn(a.sigma, gx - vbx, ldd<S, CG>(a.pin[0], i, a.pdec));
+    float py = __fmaf_rn(a.sigma, gy - vby, ldd<S, CG>(a.pin[1], i, a.pdec));
     float pz = 0.f, vbz = 0.f, nrm;
     if constexpr (THREE) {
-        const float gz = (z + 1 < a.D) ? a.ubar[i + WH] - ub : 0.f;
-        vbz = a.vb2[i];
-        pz = __fmaf_rn(a.sigma, gz - vbz, S::ld(a.pin[2], i, a.pdec));
+        const float gz = (z + 1 < a.D) ? ldf<CG>(a.ubar, i + WH) - ub : 0.f;
+        vbz = ldf<CG>(a.vb2, i);
+        pz = __fmaf_rn(a.sigma, gz - vbz, ldd<S, CG>(a.pin[2], i, a.pdec));
         nrm = norm3df(px, py, pz);
     } else {
         nrm = sqrtf(px * px + py * py);  // tgv2_common_2d.cu:113
@@ -169,30 +192,30 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
 
     // q <- proj(q + sigma E vbar), E from negated backward differences
     // B w = w[i-e] - w[i], and -w[i] on the first slice   (tgv_common.cu:133-197)
-    const float vbx_x = x > 0 ? a.vb0[i - 1] : 0.f;
-    const float vby_x = x > 0 ? a.vb1[i - 1] : 0.f;
-    const float vbx_y = y > 0 ? a.vb0[i - W] : 0.f;
-    const float vby_y = y > 0 ? a.vb1[i - W] : 0.f;
+    const float vbx_x = x > 0 ? ldf<CG>(a.vb0, i - 1) : 0.f;
+    const float vby_x = x > 0 ? ldf<CG>(a.vb1, i - 1) : 0.f;
+    const float vbx_y = y > 0 ? ldf<CG>(a.vb0, i - W) : 0.f;
+    const float vby_y = y > 0 ? ldf<CG>(a.vb1, i - W) : 0.f;
     const float exx = vbx_x - vbx;
     const float eyy = vby_y - vby;
     const float exy = ((vby_x - vby) + (vbx_y - vbx)) * 0.5f;  // tgv2_common.cu:191-199
-    float qxx = __fmaf_rn(a.sigma, exx, S::ld(a.qin[0], i, a.qdec));
-    float qyy = __fmaf_rn(a.sigma, eyy, S::ld(a.qin[1], i, a.qdec));
-    float qxy = __fmaf_rn(a.sigma, exy, S::ld(a.qin[3], i, a.qdec));
+    float qxx = __fmaf_rn(a.sigma, exx, ldd<S, CG>(a.qin[0], i, a.qdec));
+    float qyy = __fmaf_rn(a.sigma, eyy, ldd<S, CG>(a.qin[1], i, a.qdec));
+    float qxy = __fmaf_rn(a.sigma, exy, ldd<S, CG>(a.qin[3], i, a.qdec));
     float s = qxx * qxx + qyy * qyy + 2.f * qxy * qxy;
     float qzz = 0.f, qxz = 0.f, qyz = 0.f;
     if constexpr (THREE) {
-        const float vbz_x = x > 0 ? a.vb2[i - 1] : 0.f;
-        const float vbz_y = y > 0 ? a.vb2[i - W] : 0.f;
-        const float vbx_z = z > 0 ? a.vb0[i - WH] : 0.f;
-        const float vby_z = z > 0 ? a.vb1[i - WH] : 0.f;
-        const float vbz_z = z > 0 ? a.vb2[i - WH] : 0.f;
+        const float vbz_x = x > 0 ? ldf<CG>(a.vb2, i - 1) : 0.f;
+        const float vbz_y = y > 0 ? ldf<CG>(a.vb2, i - W) : 0.f;
+        const float vbx_z = z > 0 ? ldf<CG>(a.vb0, i - WH) : 0.f;
+        const float vby_z = z > 0 ? ldf<CG>(a.vb1, i - WH) : 0.f;
+        const float vbz_z = z > 0 ? ldf<CG>(a.vb2, i - WH) : 0.f;
         const float ezz = vbz_z - vbz;
         const float exz = ((vbz_x - vbz) + (vbx_z - vbx)) * 0.5f;
         const float eyz = ((vbz_y - vbz) + (vby_z - vby)) * 0.5f;
-        qzz = __fmaf_rn(a.sigma, ezz, S::ld(a.qin[2], i, a.qdec));
-        qxz = __fmaf_rn(a.sigma, exz, S::ld(a.qin[4], i, a.qdec));
-        qyz = __fmaf_rn(a.sigma, eyz, S::ld(a.qin[5], i, a.qdec));
+        qzz = __fmaf_rn(a.sigma, ezz, ldd<S, CG>(a.qin[2], i, a.qdec));
+        qxz = __fmaf_rn(a.sigma, exz, ldd<S, CG>(a.qin[4], i, a.qdec));
+        qyz = __fmaf_rn(a.sigma, eyz, ldd<S, CG>(a.qin[5], i, a.qdec));
         s = s + qzz * qzz + 2.f * qxz * qxz + 2.f * qyz * qyz;  // tgv2_common.cu:255-261
     }
     const float qn = fmaxf(1.f, sqrtf(s) / a.alpha0);
@@ -206,14 +229,11 @@ __global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<
     }
 }
 
-// Primal pass.
-template <int PREC, bool THREE, int DATA>
-__global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dual<PREC>::T> a) {
+// The primal update at voxel (x, y, z), in place.
+template <int PREC, bool THREE, int DATA, bool CG>
+__device__ __forceinline__ void primal_update(const TgvArgs<typename Dual<PREC>::T>& a, int x,
+                                              int y, int z) {
     using S = Dual<PREC>;
-    const int x = blockIdx.x * BX + threadIdx.x;
-    const int y = blockIdx.y * BY + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
     if (!TGV_IN_BOUNDS(i, WH * a.D, 2)) return;
@@ -221,19 +241,19 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
     if (a.dom && !a.dom[i]) return;
 
     // u <- prox(u - tau B.p), ubar                       (tgv2_l1.cu:39-52)
-    const float pxi = S::ld(a.p0, i, a.pdec);
-    const float pyi = S::ld(a.p1, i, a.pdec);
-    const float bx = (x > 0 ? S::ld(a.p0, i - 1, a.pdec) : 0.f) - pxi;
-    const float by = (y > 0 ? S::ld(a.p1, i - W, a.pdec) : 0.f) - pyi;
+    const float pxi = ldd<S, CG>(a.p0, i, a.pdec);
+    const float pyi = ldd<S, CG>(a.p1, i, a.pdec);
+    const float bx = (x > 0 ? ldd<S, CG>(a.p0, i - 1, a.pdec) : 0.f) - pxi;
+    const float by = (y > 0 ? ldd<S, CG>(a.p1, i - W, a.pdec) : 0.f) - pyi;
     float div = bx + by;
     float pzi = 0.f;
     if constexpr (THREE) {
-        pzi = S::ld(a.p2, i, a.pdec);
-        const float bz = (z > 0 ? S::ld(a.p2, i - WH, a.pdec) : 0.f) - pzi;
+        pzi = ldd<S, CG>(a.p2, i, a.pdec);
+        const float bz = (z > 0 ? ldd<S, CG>(a.p2, i - WH, a.pdec) : 0.f) - pzi;
         if (!a.skip_bz) div = div + bz;
     }
-    const float uo = a.u_in[i];
-    const float fi = a.f[i];
+    const float uo = ldf<CG>(a.u_in, i);
+    const float fi = ldf<CG>(a.f, i);
     float uu = uo - a.tau * div;
     if constexpr (DATA == TGVDCT_DATA_L1) {
         const float umf = uu - fi;
@@ -247,26 +267,26 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
     a.ubar_out[i] = uu + a.theta * (uu - uo);
 
     // div q with Neumann forward differences          (tgv2_common.cu:290-318)
-    const float qxx = S::ld(a.qxx, i, a.qdec);
-    const float qyy = S::ld(a.qyy, i, a.qdec);
-    const float qxy = S::ld(a.qxy, i, a.qdec);
-    const float fx_qxx = xl ? S::ld(a.qxx, i + 1, a.qdec) - qxx : 0.f;
-    const float fy_qxy = yl ? S::ld(a.qxy, i + W, a.qdec) - qxy : 0.f;
-    const float fy_qyy = yl ? S::ld(a.qyy, i + W, a.qdec) - qyy : 0.f;
-    const float fx_qxy = xl ? S::ld(a.qxy, i + 1, a.qdec) - qxy : 0.f;
+    const float qxx = ldd<S, CG>(a.qxx, i, a.qdec);
+    const float qyy = ldd<S, CG>(a.qyy, i, a.qdec);
+    const float qxy = ldd<S, CG>(a.qxy, i, a.qdec);
+    const float fx_qxx = xl ? ldd<S, CG>(a.qxx, i + 1, a.qdec) - qxx : 0.f;
+    const float fy_qxy = yl ? ldd<S, CG>(a.qxy, i + W, a.qdec) - qxy : 0.f;
+    const float fy_qyy = yl ? ldd<S, CG>(a.qyy, i + W, a.qdec) - qyy : 0.f;
+    const float fx_qxy = xl ? ldd<S, CG>(a.qxy, i + 1, a.qdec) - qxy : 0.f;
     float dx = fx_qxx + fy_qxy;
     float dy = fy_qyy + fx_qxy;
     float dz = 0.f;
     if constexpr (THREE) {
         const bool zl = z + 1 < a.D;
-        const float qzz = S::ld(a.qzz, i, a.qdec);
-        const float qxz = S::ld(a.qxz, i, a.qdec);
-        const float qyz = S::ld(a.qyz, i, a.qdec);
-        const float fz_qxz = zl ? S::ld(a.qxz, i + WH, a.qdec) - qxz : 0.f;
-        const float fz_qyz = zl ? S::ld(a.qyz, i + WH, a.qdec) - qyz : 0.f;
-        const float fz_qzz = zl ? S::ld(a.qzz, i + WH, a.qdec) - qzz : 0.f;
-        const float fx_qxz = xl ? S::ld(a.qxz, i + 1, a.qdec) - qxz : 0.f;
-        const float fy_qyz = yl ? S::ld(a.qyz, i + W, a.qdec) - qyz : 0.f;
+        const float qzz = ldd<S, CG>(a.qzz, i, a.qdec);
+        const float qxz = ldd<S, CG>(a.qxz, i, a.qdec);
+        const float qyz = ldd<S, CG>(a.qyz, i, a.qdec);
+        const float fz_qxz = zl ? ldd<S, CG>(a.qxz, i + WH, a.qdec) - qxz : 0.f;
+        const float fz_qyz = zl ? ldd<S, CG>(a.qyz, i + WH, a.qdec) - qyz : 0.f;
+        const float fz_qzz = zl ? ldd<S, CG>(a.qzz, i + WH, a.qdec) - qzz : 0.f;
+        const float fx_qxz = xl ? ldd<S, CG>(a.qxz, i + 1, a.qdec) - qxz : 0.f;
+        const float fy_qyz = yl ? ldd<S, CG>(a.qyz, i + W, a.qdec) - qyz : 0.f;
         dx = dx + fz_qxz;
         dy = dy + fz_qyz;
         dz = (fz_qzz + fx_qxz) + fy_qyz;
@@ -274,23 +294,41 @@ __global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dua
 
     // v <- v - tau (div q - p), vbar                     (tgv2_common.cu:338-347)
     {
-        const float vo = a.v_in[0][i];
+        const float vo = ldf<CG>(a.v_in[0], i);
         const float vn = vo - a.tau * (dx - pxi);
         a.v0[i] = vn;
         a.vbo[0][i] = vn + a.theta * (vn - vo);
     }
     {
-        const float vo = a.v_in[1][i];
+        const float vo = ldf<CG>(a.v_in[1], i);
         const float vn = vo - a.tau * (dy - pyi);
         a.v1[i] = vn;
         a.vbo[1][i] = vn + a.theta * (vn - vo);
     }
     if constexpr (THREE) {
-        const float vo = a.v_in[2][i];
+        const float vo = ldf<CG>(a.v_in[2], i);
         const float vn = vo - a.tau * (dz - pzi);
         a.v2[i] = vn;
         a.vbo[2][i] = vn + a.theta * (vn - vo);
     }
+}
+
+// Dual pass (one launch per iteration).
+template <int PREC, bool THREE>
+__global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<PREC>::T> a) {
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    if (x >= a.W || y >= a.H) return;
+    dual_update<PREC, THREE, false>(a, x, y, (int)blockIdx.z);
+}
+
+// Primal pass.
+template <int PREC, bool THREE, int DATA>
+__global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dual<PREC>::T> a) {
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    if (x >= a.W || y >= a.H) return;
+    primal_update<PREC, THREE, DATA, false>(a, x, y, (int)blockIdx.z);
 }
 
 // ---- fused single-pass iteration ---------------------------------------------------------
