@@ -26,6 +26,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -1350,6 +1351,152 @@ void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
     launch_two_pass<PREC>(s, k, a, st);
 }
 
+// ---- persistent loop for a single plane --------------------------------------------
+//
+// A single plane (a 2-D image, or a volume of depth 1) of up to a few million pixels
+// keeps its whole state in L2, and one iteration is two short passes over it.  Launched
+// per pass, the launches themselves set the pace: 512 x 512 takes 6.2 us per
+// iteration for 2 x 0.26 M pixel updates.  Here one cooperative launch runs many
+// iterations.  Block b owns the rows [y0, y1) (one block per SM) and runs the two-pass
+// updates on them with loads through L2 (other blocks write the fields between the
+// passes).  Between passes a block waits only for its two neighbours: the dual pass
+// reads ubar and vbar one row either side (written by the neighbours' previous primal
+// pass) and writes p, q (read by their previous primal pass), the primal pass reads p
+// one row up and q one row down (written by the neighbours' dual pass) and writes
+// ubar, vbar (read by it).  Each block publishes a count of finished passes with a
+// release store after a block barrier; a neighbour polls it with acquire loads, a
+// bounded wait (the state's pipeline wait limit) that raises the error flag and ends
+// the launch when it runs out.  The arithmetic is the two-pass kernels' (the same
+// device functions), so the results are bit-identical to theirs.
+constexpr int STRIP_THREADS = 1024;
+constexpr int STRIP_MAX_BLOCKS = 1024;  // per launch; flags for two counts per block
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// One thread waits until *flag >= target; false when the limit ran out (error raised).
+__device__ bool wait_count(const unsigned* flag, unsigned target, uint64_t limit_ns, int* err) {
+    if (ld_acquire_u32(flag) >= target) return true;
+    if (limit_ns == 0) {
+        atomicExch(err, 1);
+        return false;
+    }
+    uint64_t t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    while (true) {
+        if (ld_acquire_u32(flag) >= target) return true;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) {
+            atomicExch(err, 1);
+            return false;
+        }
+        if (*(volatile int*)err) return false;  // another block gave up already
+        __nanosleep(20);
+    }
+}
+
+template <int PREC, bool THREE, int DATA>
+__global__ void __launch_bounds__(STRIP_THREADS, 1)
+    tgv_strips_kernel(TgvArgs<typename Dual<PREC>::T> a, int iterations, unsigned* flags,
+                      unsigned long long wait_ns, int* err) {
+    __shared__ int fail;
+    const int nb = (int)gridDim.x, b = (int)blockIdx.x;
+    const int q = a.H / nb, r = a.H % nb;
+    const int y0 = b * q + min(b, r), y1 = y0 + q + (b < r ? 1 : 0);
+    const int npix = (y1 - y0) * a.W;
+    unsigned* dual_done = flags;
+    unsigned* primal_done = flags + STRIP_MAX_BLOCKS;
+    if (threadIdx.x == 0) fail = *(volatile int*)err;
+    __syncthreads();
+    if (fail) return;
+    // thread 0 waits for both neighbours' count of one kind of pass
+    auto wait_neighbours = [&](const unsigned* done, unsigned target) {
+        if (threadIdx.x == 0) {
+            bool ok = true;
+            if (b > 0) ok = wait_count(done + b - 1, target, wait_ns, err);
+            if (ok && b + 1 < nb) ok = wait_count(done + b + 1, target, wait_ns, err);
+            fail = ok ? 0 : 1;
+        }
+        __syncthreads();
+        return fail == 0;
+    };
+    auto publish = [&](unsigned* done, unsigned count) {
+        __syncthreads();  // every thread's stores of the pass precede the release
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_u32(done + b, count);
+        }
+    };
+    for (int it = 0; it < iterations; ++it) {
+        // the neighbours' primal pass of the previous iteration (the launch's first
+        // iteration follows a finished launch)
+        if (it > 0 && !wait_neighbours(primal_done, (unsigned)it)) return;
+        for (int e = (int)threadIdx.x; e < npix; e += STRIP_THREADS) {
+            const int y = y0 + e / a.W, x = e % a.W;
+            if (TGV_IN_BOUNDS((size_t)y * a.W + x, a.WH, 40))
+                dual_update<PREC, THREE, true>(a, x, y, 0);
+        }
+        publish(dual_done, (unsigned)it + 1);
+        if (!wait_neighbours(dual_done, (unsigned)it + 1)) return;
+        for (int e = (int)threadIdx.x; e < npix; e += STRIP_THREADS) {
+            const int y = y0 + e / a.W, x = e % a.W;
+            if (TGV_IN_BOUNDS((size_t)y * a.W + x, a.WH, 41))
+                primal_update<PREC, THREE, DATA, true>(a, x, y, 0);
+        }
+        publish(primal_done, (unsigned)it + 1);
+    }
+}
+
+// Blocks of one strips launch for this state (0: the kernel cannot run here).
+template <int PREC>
+int strips_blocks(const TgvState& s) {
+    static std::atomic<int> cached{-1};
+    int per_sm = cached.load(std::memory_order_relaxed);
+    if (per_sm < 0) {
+        int dev = 0, coop = 0, n = 0;
+        TGV_CUDA(cudaGetDevice(&dev));
+        TGV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (coop)
+            TGV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &n, tgv_strips_kernel<PREC, true, TGVDCT_DATA_L1>, STRIP_THREADS, 0));
+        per_sm = n > 0 ? 1 : 0;
+        cached.store(per_sm, std::memory_order_relaxed);
+    }
+    if (!per_sm) return 0;
+    int dev = 0, sms = 0;
+    TGV_CUDA(cudaGetDevice(&dev));
+    TGV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return std::min({sms, s.H, STRIP_MAX_BLOCKS});
+}
+
+template <int PREC>
+void iterate_strips(const TgvState& s, const TgvStep& k, int iterations, cudaStream_t st) {
+    const TgvStencilFields& F = s.now();  // in place, as the two-pass kernels
+    float* const v[3] = {s.v[0], s.v[1], s.v[2]};
+    auto a = make_args<PREC>(s, k, F, s.u, v, F, s.u, v);
+    const int nb = strips_blocks<PREC>(s);
+    TGV_CUDA(cudaMemsetAsync(s.strip_flags, 0, 2 * STRIP_MAX_BLOCKS * sizeof(unsigned), st));
+    unsigned* flags = s.strip_flags;
+    unsigned long long wait_ns = s.wait_ns;
+    int* err = s.err;
+    void* args[] = {&a, &iterations, &flags, &wait_ns, &err};
+    const void* kern;
+    if (s.three)
+        kern = k.data_term == TGVDCT_DATA_L1
+                   ? (const void*)tgv_strips_kernel<PREC, true, TGVDCT_DATA_L1>
+                   : (const void*)tgv_strips_kernel<PREC, true, TGVDCT_DATA_L2>;
+    else
+        kern = k.data_term == TGVDCT_DATA_L1
+                   ? (const void*)tgv_strips_kernel<PREC, false, TGVDCT_DATA_L1>
+                   : (const void*)tgv_strips_kernel<PREC, false, TGVDCT_DATA_L2>;
+    TGV_CUDA(cudaLaunchCooperativeKernel(kern, dim3(nb), dim3(STRIP_THREADS), args, 0, st));
+}
+
 constexpr int FUSED_TY = 8;
 
 template <int PREC, bool THREE, int DATA>
@@ -1578,9 +1725,11 @@ size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kerne
     const size_t n = (size_t)W * H * D;
     const size_t f32 = align256(n * 4), dual = align256(n * elem_bytes(precision));
     const int ncomp = three ? 3 : 2, nq = three ? 6 : 3;
-    const int sets = kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
-    // u, f, v + per set: ubar, vbar, p, q; plus a device error flag
-    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq)) + 256;
+    const int sets = in_place_kernel(kernel) ? 1 : 2;
+    // u, f, v + per set: ubar, vbar, p, q; plus a device error flag, and the pass
+    // counts of the persistent single-plane kernel
+    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq)) + 256 +
+           (kernel == TGV_KERNEL_STRIPS ? align256(2 * STRIP_MAX_BLOCKS * sizeof(unsigned)) : 0);
 }
 
 void tgv_state_bind(TgvState& s, char* base) {
@@ -1596,7 +1745,7 @@ void tgv_state_bind(TgvState& s, char* base) {
     s.u = (float*)take(f32);
     s.f = (float*)take(f32);
     for (int k = 0; k < 3; ++k) s.v[k] = k < ncomp ? (float*)take(f32) : nullptr;
-    const int sets = s.kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
+    const int sets = in_place_kernel(s.kernel) ? 1 : 2;
     s.tma_cache.reset();
     // q order: xx yy zz xy xz yz; the 2-D launcher keeps xx yy xy
     const int order2[3] = {0, 1, 3};
@@ -1610,6 +1759,9 @@ void tgv_state_bind(TgvState& s, char* base) {
         for (int k = 0; k < nq; ++k) F.q[s.three ? k : order2[k]] = (void*)take(dual);
     }
     s.err = (int*)take(256);
+    s.strip_flags = s.kernel == TGV_KERNEL_STRIPS
+                        ? (unsigned*)take(align256(2 * STRIP_MAX_BLOCKS * sizeof(unsigned)))
+                        : nullptr;
     s.cur = 0;
 }
 
@@ -1852,7 +2004,9 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     }
     // The register-staged fused kernel has no domain support: a masked run whose
     // shape rules out TMA uses the two-pass kernels in place on the current set.
-    if (s.kernel == TGV_KERNEL_TWO_PASS || s.domain) {
+    // a single iteration of the persistent single-plane kernel's state: the two-pass
+    // kernels (the same arithmetic, in place on the same set)
+    if (in_place_kernel(s.kernel) || s.domain) {
         switch (s.precision) {
             case TGVDCT_STATE_FP32: iterate_two_pass<TGVDCT_STATE_FP32>(s, k, st); return;
             case TGVDCT_STATE_BF16_DUAL: iterate_two_pass<TGVDCT_STATE_BF16_DUAL>(s, k, st); return;
@@ -1868,6 +2022,37 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     TGV_REQUIRE(false, "unknown state precision");
 }
 
-int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL_TWO_PASS ? 2 : 1; }
+void tgv_iterate_n(TgvState& s, const TgvStep& k, int iterations, cudaStream_t st) {
+    if (iterations <= 0) return;
+    if (s.kernel == TGV_KERNEL_STRIPS && !s.domain && iterations > 1 &&
+        tgv_strips_available(s.precision)) {
+        switch (s.precision) {
+            case TGVDCT_STATE_FP32: iterate_strips<TGVDCT_STATE_FP32>(s, k, iterations, st); return;
+            case TGVDCT_STATE_BF16_DUAL:
+                iterate_strips<TGVDCT_STATE_BF16_DUAL>(s, k, iterations, st);
+                return;
+            case TGVDCT_STATE_FX16_DUAL:
+                iterate_strips<TGVDCT_STATE_FX16_DUAL>(s, k, iterations, st);
+                return;
+        }
+        TGV_REQUIRE(false, "unknown state precision");
+    }
+    for (int i = 0; i < iterations; ++i) tgv_iterate(s, k, st);
+}
+
+bool tgv_strips_available(int precision) {
+    TgvState probe;
+    probe.H = 1 << 30;
+    switch (precision) {
+        case TGVDCT_STATE_FP32: return strips_blocks<TGVDCT_STATE_FP32>(probe) > 0;
+        case TGVDCT_STATE_BF16_DUAL: return strips_blocks<TGVDCT_STATE_BF16_DUAL>(probe) > 0;
+        case TGVDCT_STATE_FX16_DUAL: return strips_blocks<TGVDCT_STATE_FX16_DUAL>(probe) > 0;
+    }
+    return false;
+}
+
+int tgv_kernels_per_iteration(const TgvState& s) {
+    return in_place_kernel(s.kernel) ? 2 : 1;
+}
 
 }  // namespace tgvdct
