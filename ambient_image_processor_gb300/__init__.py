@@ -25,7 +25,7 @@ GEOMETRY_3D, GEOMETRY_2D = 0, 1
 STATE_FP32, STATE_BF16_DUAL, STATE_FX16_DUAL = 0, 1, 2
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 EIGEN_REFERENCE, EIGEN_ACCURATE = 0, 1
-KERNEL_AUTO, KERNEL_TWO_PASS, KERNEL_FUSED, KERNEL_FUSED_REGISTER, KERNEL_PERSISTENT_PLANE = range(5)
+KERNEL_AUTO, KERNEL_TWO_PASS, KERNEL_FUSED, KERNEL_FUSED_REGISTER = 0, 1, 2, 3
 
 _STATUS_NAMES = {OK: "ok", ERR_BAD_ARG: "bad argument", ERR_OOM: "out of memory",
                  ERR_CUDA: "CUDA error", ERR_NO_DEVICE: "no suitable CUDA device",

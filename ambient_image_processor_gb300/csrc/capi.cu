@@ -99,10 +99,8 @@ void validate(const tgvdct_params* p) {
     TGV_REQUIRE(std::isfinite(p->sigma) && p->sigma > 0.f, "sigma must be > 0");
     TGV_REQUIRE(std::isfinite(p->theta), "theta must be finite");
     TGV_REQUIRE(p->iteration_kernel >= TGVDCT_KERNEL_AUTO &&
-                    p->iteration_kernel <= TGVDCT_KERNEL_PERSISTENT_PLANE,
+                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED_REGISTER,
                 "unknown iteration kernel");
-    TGV_REQUIRE(p->iteration_kernel != TGVDCT_KERNEL_PERSISTENT_PLANE || p->depth == 1,
-                "the persistent single-plane kernel needs depth == 1");
     TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
     TGV_REQUIRE(p->energy_tolerance >= 0.f && std::isfinite(p->energy_tolerance),
                 "energy_tolerance must be finite and >= 0");
@@ -112,23 +110,12 @@ void validate(const tgvdct_params* p) {
 // for a single plane, where the fused pass has no planes to pipeline (at 512^2,
 // 1024^2 and 2048^2 the two passes take 6.2, 15.5 and 87 ms per 1000 iterations
 // against 11.0, 39.8 and 164 ms).  Every kernel gives the same bits.
-// A single plane whose state fits in L2 several times over runs the persistent
-// single-plane kernel (two-pass arithmetic, one launch for many iterations).
-constexpr size_t kStripsMaxStateBytes = 96ull << 20;
-
 int kernel_of(const tgvdct_params& p) {
-    const bool three = p.geometry == TGVDCT_GEOMETRY_3D;
     switch (p.iteration_kernel) {
         case TGVDCT_KERNEL_TWO_PASS: return TGV_KERNEL_TWO_PASS;
         case TGVDCT_KERNEL_FUSED_REGISTER: return TGV_KERNEL_FUSED_REGISTER;
         case TGVDCT_KERNEL_FUSED: return TGV_KERNEL_FUSED;
-        case TGVDCT_KERNEL_PERSISTENT_PLANE: return TGV_KERNEL_STRIPS;
-        default:
-            if (p.depth != 1) return TGV_KERNEL_FUSED;
-            return tgv_state_bytes((int)p.width, (int)p.height, 1, three, p.state_precision,
-                                   TGV_KERNEL_TWO_PASS) <= kStripsMaxStateBytes
-                       ? TGV_KERNEL_STRIPS
-                       : TGV_KERNEL_TWO_PASS;
+        default: return p.depth == 1 ? TGV_KERNEL_TWO_PASS : TGV_KERNEL_FUSED;
     }
 }
 
@@ -357,51 +344,13 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
     };
     c->iterations_run = 0;
     c->energy_history.clear();
-    // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384),
-    // energy checks after iterations j > 0 with j % check == 0
-    auto due_at = [&](uint32_t j) {
-        return j > 0 && ((cb_on && j % paint == 0) || (check > 0 && j % check == 0));
-    };
-    // the callback and the energy check after iteration j; true: stop
-    auto after = [&](uint32_t j) {
-        if (cb_on && j > 0 && j % paint == 0) {
-            if (on_iteration(j)) {
-                c->iterations_run = j + 1;
-                return true;
-            }
-        }
-        if (check > 0 && j > 0 && j % check == 0) {
-            const double e = state_energy(c, s);
-            const bool settled = tol > 0.0 && !c->energy_history.empty() &&
-                                 std::fabs(e - c->energy_history.back()) <= tol * std::fabs(e);
-            c->energy_history.push_back(e);
-            if (settled) {
-                c->iterations_run = j + 1;
-                return true;
-            }
-        }
-        return false;
-    };
-    const bool strips = c->st.kernel == TGV_KERNEL_STRIPS && !c->st.domain;
     for (uint32_t it = 0; it < n_it;) {
         if (c->stop_requested.exchange(false)) {
             c->iterations_run = it;
             return true;
         }
-        if (strips) {
-            // the persistent single-plane kernel: one launch up to the next callback or
-            // energy check, at most kGraphChunk iterations (the stop-request cadence)
-            uint32_t end = std::min<uint32_t>(n_it, it + kGraphChunk);
-            for (uint32_t j = it; j < end; ++j)
-                if (due_at(j)) {
-                    end = j + 1;
-                    break;
-                }
-            tgv_iterate_n(c->st, k, (int)(end - it), s);
-            if (after(end - 1)) return true;
-            it = end;
-            continue;
-        }
+        // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384),
+        // energy checks after iterations j > 0 with j % check == 0
         if (it > 0 && it + kGraphChunk <= n_it) {
             bool due = false;
             if (cb_on) due = next_multiple(it, paint) < it + kGraphChunk;
@@ -415,7 +364,22 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
             }
         }
         tgv_iterate(c->st, k, s);
-        if (after(it)) return true;
+        if (cb_on && it > 0 && it % paint == 0) {
+            if (on_iteration(it)) {
+                c->iterations_run = it + 1;
+                return true;
+            }
+        }
+        if (check > 0 && it > 0 && it % check == 0) {
+            const double e = state_energy(c, s);
+            const bool settled = tol > 0.0 && !c->energy_history.empty() &&
+                                 std::fabs(e - c->energy_history.back()) <= tol * std::fabs(e);
+            c->energy_history.push_back(e);
+            if (settled) {
+                c->iterations_run = it + 1;
+                return true;
+            }
+        }
         ++it;
     }
     c->iterations_run = n_it;

@@ -52,14 +52,7 @@ struct TgvStencilFields {
     void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
 };
 
-enum TgvKernel {
-    TGV_KERNEL_TWO_PASS = 1,
-    TGV_KERNEL_FUSED = 2,
-    TGV_KERNEL_FUSED_REGISTER = 3,
-    TGV_KERNEL_STRIPS = 4  // the persistent single-plane loop (two-pass arithmetic)
-};
-// kernels that update one stencil set in place (the others ping-pong two)
-inline bool in_place_kernel(int k) { return k == TGV_KERNEL_TWO_PASS || k == TGV_KERNEL_STRIPS; }
+enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
 
 // Bounds-checking builds (-DTGV_CHECK_BOUNDS, libtgvdct_checked.so): kernels check
 // the indices they are about to use and record the first bad one instead of making
@@ -128,7 +121,6 @@ struct TgvState {
     // shapes the TMA stride rules exclude)
     std::shared_ptr<void> tma_cache;
     int* err = nullptr;      // device flag raised by a pipeline wait that timed out
-    unsigned* strip_flags = nullptr;  // pass counts of the persistent single-plane kernel
     // limit of the fused TMA kernel's pipeline waits (tgvdct_set_pipeline_wait_limit)
     uint64_t wait_ns = 200000000ull;
     // Optional domain of the masked deshade: voxels with domain[i] == 0 are never
@@ -168,13 +160,6 @@ void tgv_snapshot_save(const TgvState& s, void* dst, cudaStream_t st);
 void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st);
 // One primal-dual iteration (advances s.cur for the fused kernel).
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
-// `iterations` iterations: one cooperative launch of the persistent single-plane
-// kernel where the state asks for it and the device can run it (two or more
-// iterations), tgv_iterate per iteration otherwise (the same bits).
-void tgv_iterate_n(TgvState& s, const TgvStep& k, int iterations, cudaStream_t st);
-// Whether this device can run the persistent single-plane kernel (cooperative launch,
-// one 1024-thread block per SM).
-bool tgv_strips_available(int precision);
 // Number of kernels tgv_iterate launches.
 int tgv_kernels_per_iteration(const TgvState& s);
 // Whether the fused kernel of this state runs the TMA pipeline.

@@ -26,7 +26,6 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -47,9 +46,6 @@ template <>
 struct Dual<TGVDCT_STATE_FP32> {
     using T = float;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float) { return p[i]; }
-    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float) {
-        return __ldcg(p + i);
-    }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) { p[i] = v; }
     // streaming store (evict-first): the next read of the field is an iteration away
     static __device__ __forceinline__ void st_cs(T* p, size_t i, float v, float) {
@@ -62,9 +58,6 @@ struct Dual<TGVDCT_STATE_BF16_DUAL> {
     using T = __nv_bfloat16;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float) {
         return __bfloat162float(p[i]);
-    }
-    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float) {
-        return __bfloat162float(__ushort_as_bfloat16(__ldcg((const unsigned short*)p + i)));
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float) {
         p[i] = __float2bfloat16_rn(v);
@@ -86,11 +79,6 @@ struct Dual<TGVDCT_STATE_FX16_DUAL> {
     using T = int16_t;
     static __device__ __forceinline__ float ld(const T* p, size_t i, float dec) {
         const float c = __int_as_float(0x4B400000 + (int)p[i]) - 12582912.f;  // exact
-        return c * dec;
-    }
-    static __device__ __forceinline__ float ld_cg(const T* p, size_t i, float dec) {
-        const float c = __int_as_float(0x4B400000 + (int)__ldcg((const short*)p + i)) -
-                        12582912.f;
         return c * dec;
     }
     static __device__ __forceinline__ void st(T* p, size_t i, float v, float enc) {
@@ -144,26 +132,14 @@ struct TgvArgs {
 
 constexpr int BX = 32, BY = 8;
 
-// Loads of the two-pass updates: plain in the per-iteration kernels; through L2 only
-// (ld.global.cg) in the persistent single-plane kernel, whose other blocks write the
-// fields between its passes.
-template <bool CG>
-__device__ __forceinline__ float ldf(const float* p, size_t i) {
-    if constexpr (CG) return __ldcg(p + i);
-    else return p[i];
-}
-template <class S, bool CG>
-__device__ __forceinline__ float ldd(const typename S::T* p, size_t i, float dec) {
-    if constexpr (CG) return S::ld_cg(p, i, dec);
-    else return S::ld(p, i, dec);
-}
-
-// The dual update at voxel (x, y, z), in place.  THREE: 3-D operators (also for
-// D == 1); otherwise the 2-D launcher.
-template <int PREC, bool THREE, bool CG>
-__device__ __forceinline__ void dual_update(const TgvArgs<typename Dual<PREC>::T>& a, int x,
-                                            int y, int z) {
+// Dual pass.  THREE: 3-D operators (also for D == 1); otherwise the 2-D launcher.
+template <int PREC, bool THREE>
+__global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<PREC>::T> a) {
     using S = Dual<PREC>;
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
     if (!TGV_IN_BOUNDS(i, WH * a.D, 1)) return;
@@ -171,17 +147,17 @@ __device__ __forceinline__ void dual_update(const TgvArgs<typename Dual<PREC>::T
     if (a.dom && !a.dom[i]) return;
 
     // p <- proj(p + sigma (F ubar - vbar))          (tgv2_common.cu:118-130)
-    const float ub = ldf<CG>(a.ubar, i);
-    const float gx = (x + 1 < a.W) ? ldf<CG>(a.ubar, i + 1) - ub : 0.f;
-    const float gy = (y + 1 < a.H) ? ldf<CG>(a.ubar, i + W) - ub : 0.f;
-    const float vbx = ldf<CG>(a.vb0, i), vby = ldf<CG>(a.vb1, i);
-    float px = __fmaf_rn(a.sigma, gx - vbx, ldd<S, CG>(a.pin[0], i, a.pdec));
-    float py = __fmaf_rn(a.sigma, gy - vby, ldd<S, CG>(a.pin[1], i, a.pdec));
+    const float ub = a.ubar[i];
+    const float gx = (x + 1 < a.W) ? a.ubar[i + 1] - ub : 0.f;
+    const float gy = (y + 1 < a.H) ? a.ubar[i + W] - ub : 0.f;
+    const float vbx = a.vb0[i], vby = a.vb1[i];
+    float px = __fmaf_rn(a.sigma, gx - vbx, S::ld(a.pin[0], i, a.pdec));
+    float py = __fmaf_rn(a.sigma, gy - vby, S::ld(a.pin[1], i, a.pdec));
     float pz = 0.f, vbz = 0.f, nrm;
     if constexpr (THREE) {
-        const float gz = (z + 1 < a.D) ? ldf<CG>(a.ubar, i + WH) - ub : 0.f;
-        vbz = ldf<CG>(a.vb2, i);
-        pz = __fmaf_rn(a.sigma, gz - vbz, ldd<S, CG>(a.pin[2], i, a.pdec));
+        const float gz = (z + 1 < a.D) ? a.ubar[i + WH] - ub : 0.f;
+        vbz = a.vb2[i];
+        pz = __fmaf_rn(a.sigma, gz - vbz, S::ld(a.pin[2], i, a.pdec));
         nrm = norm3df(px, py, pz);
     } else {
         nrm = sqrtf(px * px + py * py);  // tgv2_common_2d.cu:113
@@ -193,30 +169,30 @@ __device__ __forceinline__ void dual_update(const TgvArgs<typename Dual<PREC>::T
 
     // q <- proj(q + sigma E vbar), E from negated backward differences
     // B w = w[i-e] - w[i], and -w[i] on the first slice   (tgv_common.cu:133-197)
-    const float vbx_x = x > 0 ? ldf<CG>(a.vb0, i - 1) : 0.f;
-    const float vby_x = x > 0 ? ldf<CG>(a.vb1, i - 1) : 0.f;
-    const float vbx_y = y > 0 ? ldf<CG>(a.vb0, i - W) : 0.f;
-    const float vby_y = y > 0 ? ldf<CG>(a.vb1, i - W) : 0.f;
+    const float vbx_x = x > 0 ? a.vb0[i - 1] : 0.f;
+    const float vby_x = x > 0 ? a.vb1[i - 1] : 0.f;
+    const float vbx_y = y > 0 ? a.vb0[i - W] : 0.f;
+    const float vby_y = y > 0 ? a.vb1[i - W] : 0.f;
     const float exx = vbx_x - vbx;
     const float eyy = vby_y - vby;
     const float exy = ((vby_x - vby) + (vbx_y - vbx)) * 0.5f;  // tgv2_common.cu:191-199
-    float qxx = __fmaf_rn(a.sigma, exx, ldd<S, CG>(a.qin[0], i, a.qdec));
-    float qyy = __fmaf_rn(a.sigma, eyy, ldd<S, CG>(a.qin[1], i, a.qdec));
-    float qxy = __fmaf_rn(a.sigma, exy, ldd<S, CG>(a.qin[3], i, a.qdec));
+    float qxx = __fmaf_rn(a.sigma, exx, S::ld(a.qin[0], i, a.qdec));
+    float qyy = __fmaf_rn(a.sigma, eyy, S::ld(a.qin[1], i, a.qdec));
+    float qxy = __fmaf_rn(a.sigma, exy, S::ld(a.qin[3], i, a.qdec));
     float s = qxx * qxx + qyy * qyy + 2.f * qxy * qxy;
     float qzz = 0.f, qxz = 0.f, qyz = 0.f;
     if constexpr (THREE) {
-        const float vbz_x = x > 0 ? ldf<CG>(a.vb2, i - 1) : 0.f;
-        const float vbz_y = y > 0 ? ldf<CG>(a.vb2, i - W) : 0.f;
-        const float vbx_z = z > 0 ? ldf<CG>(a.vb0, i - WH) : 0.f;
-        const float vby_z = z > 0 ? ldf<CG>(a.vb1, i - WH) : 0.f;
-        const float vbz_z = z > 0 ? ldf<CG>(a.vb2, i - WH) : 0.f;
+        const float vbz_x = x > 0 ? a.vb2[i - 1] : 0.f;
+        const float vbz_y = y > 0 ? a.vb2[i - W] : 0.f;
+        const float vbx_z = z > 0 ? a.vb0[i - WH] : 0.f;
+        const float vby_z = z > 0 ? a.vb1[i - WH] : 0.f;
+        const float vbz_z = z > 0 ? a.vb2[i - WH] : 0.f;
         const float ezz = vbz_z - vbz;
         const float exz = ((vbz_x - vbz) + (vbx_z - vbx)) * 0.5f;
         const float eyz = ((vbz_y - vbz) + (vby_z - vby)) * 0.5f;
-        qzz = __fmaf_rn(a.sigma, ezz, ldd<S, CG>(a.qin[2], i, a.qdec));
-        qxz = __fmaf_rn(a.sigma, exz, ldd<S, CG>(a.qin[4], i, a.qdec));
-        qyz = __fmaf_rn(a.sigma, eyz, ldd<S, CG>(a.qin[5], i, a.qdec));
+        qzz = __fmaf_rn(a.sigma, ezz, S::ld(a.qin[2], i, a.qdec));
+        qxz = __fmaf_rn(a.sigma, exz, S::ld(a.qin[4], i, a.qdec));
+        qyz = __fmaf_rn(a.sigma, eyz, S::ld(a.qin[5], i, a.qdec));
         s = s + qzz * qzz + 2.f * qxz * qxz + 2.f * qyz * qyz;  // tgv2_common.cu:255-261
     }
     const float qn = fmaxf(1.f, sqrtf(s) / a.alpha0);
@@ -230,11 +206,14 @@ __device__ __forceinline__ void dual_update(const TgvArgs<typename Dual<PREC>::T
     }
 }
 
-// The primal update at voxel (x, y, z), in place.
-template <int PREC, bool THREE, int DATA, bool CG>
-__device__ __forceinline__ void primal_update(const TgvArgs<typename Dual<PREC>::T>& a, int x,
-                                              int y, int z) {
+// Primal pass.
+template <int PREC, bool THREE, int DATA>
+__global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dual<PREC>::T> a) {
     using S = Dual<PREC>;
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= a.W || y >= a.H) return;
     const size_t W = (size_t)a.W, WH = a.WH;
     const size_t i = ((size_t)z * a.H + y) * W + x;
     if (!TGV_IN_BOUNDS(i, WH * a.D, 2)) return;
@@ -242,19 +221,19 @@ __device__ __forceinline__ void primal_update(const TgvArgs<typename Dual<PREC>:
     if (a.dom && !a.dom[i]) return;
 
     // u <- prox(u - tau B.p), ubar                       (tgv2_l1.cu:39-52)
-    const float pxi = ldd<S, CG>(a.p0, i, a.pdec);
-    const float pyi = ldd<S, CG>(a.p1, i, a.pdec);
-    const float bx = (x > 0 ? ldd<S, CG>(a.p0, i - 1, a.pdec) : 0.f) - pxi;
-    const float by = (y > 0 ? ldd<S, CG>(a.p1, i - W, a.pdec) : 0.f) - pyi;
+    const float pxi = S::ld(a.p0, i, a.pdec);
+    const float pyi = S::ld(a.p1, i, a.pdec);
+    const float bx = (x > 0 ? S::ld(a.p0, i - 1, a.pdec) : 0.f) - pxi;
+    const float by = (y > 0 ? S::ld(a.p1, i - W, a.pdec) : 0.f) - pyi;
     float div = bx + by;
     float pzi = 0.f;
     if constexpr (THREE) {
-        pzi = ldd<S, CG>(a.p2, i, a.pdec);
-        const float bz = (z > 0 ? ldd<S, CG>(a.p2, i - WH, a.pdec) : 0.f) - pzi;
+        pzi = S::ld(a.p2, i, a.pdec);
+        const float bz = (z > 0 ? S::ld(a.p2, i - WH, a.pdec) : 0.f) - pzi;
         if (!a.skip_bz) div = div + bz;
     }
-    const float uo = ldf<CG>(a.u_in, i);
-    const float fi = ldf<CG>(a.f, i);
+    const float uo = a.u_in[i];
+    const float fi = a.f[i];
     float uu = uo - a.tau * div;
     if constexpr (DATA == TGVDCT_DATA_L1) {
         const float umf = uu - fi;
@@ -268,26 +247,26 @@ __device__ __forceinline__ void primal_update(const TgvArgs<typename Dual<PREC>:
     a.ubar_out[i] = uu + a.theta * (uu - uo);
 
     // div q with Neumann forward differences          (tgv2_common.cu:290-318)
-    const float qxx = ldd<S, CG>(a.qxx, i, a.qdec);
-    const float qyy = ldd<S, CG>(a.qyy, i, a.qdec);
-    const float qxy = ldd<S, CG>(a.qxy, i, a.qdec);
-    const float fx_qxx = xl ? ldd<S, CG>(a.qxx, i + 1, a.qdec) - qxx : 0.f;
-    const float fy_qxy = yl ? ldd<S, CG>(a.qxy, i + W, a.qdec) - qxy : 0.f;
-    const float fy_qyy = yl ? ldd<S, CG>(a.qyy, i + W, a.qdec) - qyy : 0.f;
-    const float fx_qxy = xl ? ldd<S, CG>(a.qxy, i + 1, a.qdec) - qxy : 0.f;
+    const float qxx = S::ld(a.qxx, i, a.qdec);
+    const float qyy = S::ld(a.qyy, i, a.qdec);
+    const float qxy = S::ld(a.qxy, i, a.qdec);
+    const float fx_qxx = xl ? S::ld(a.qxx, i + 1, a.qdec) - qxx : 0.f;
+    const float fy_qxy = yl ? S::ld(a.qxy, i + W, a.qdec) - qxy : 0.f;
+    const float fy_qyy = yl ? S::ld(a.qyy, i + W, a.qdec) - qyy : 0.f;
+    const float fx_qxy = xl ? S::ld(a.qxy, i + 1, a.qdec) - qxy : 0.f;
     float dx = fx_qxx + fy_qxy;
     float dy = fy_qyy + fx_qxy;
     float dz = 0.f;
     if constexpr (THREE) {
         const bool zl = z + 1 < a.D;
-        const float qzz = ldd<S, CG>(a.qzz, i, a.qdec);
-        const float qxz = ldd<S, CG>(a.qxz, i, a.qdec);
-        const float qyz = ldd<S, CG>(a.qyz, i, a.qdec);
-        const float fz_qxz = zl ? ldd<S, CG>(a.qxz, i + WH, a.qdec) - qxz : 0.f;
-        const float fz_qyz = zl ? ldd<S, CG>(a.qyz, i + WH, a.qdec) - qyz : 0.f;
-        const float fz_qzz = zl ? ldd<S, CG>(a.qzz, i + WH, a.qdec) - qzz : 0.f;
-        const float fx_qxz = xl ? ldd<S, CG>(a.qxz, i + 1, a.qdec) - qxz : 0.f;
-        const float fy_qyz = yl ? ldd<S, CG>(a.qyz, i + W, a.qdec) - qyz : 0.f;
+        const float qzz = S::ld(a.qzz, i, a.qdec);
+        const float qxz = S::ld(a.qxz, i, a.qdec);
+        const float qyz = S::ld(a.qyz, i, a.qdec);
+        const float fz_qxz = zl ? S::ld(a.qxz, i + WH, a.qdec) - qxz : 0.f;
+        const float fz_qyz = zl ? S::ld(a.qyz, i + WH, a.qdec) - qyz : 0.f;
+        const float fz_qzz = zl ? S::ld(a.qzz, i + WH, a.qdec) - qzz : 0.f;
+        const float fx_qxz = xl ? S::ld(a.qxz, i + 1, a.qdec) - qxz : 0.f;
+        const float fy_qyz = yl ? S::ld(a.qyz, i + W, a.qdec) - qyz : 0.f;
         dx = dx + fz_qxz;
         dy = dy + fz_qyz;
         dz = (fz_qzz + fx_qxz) + fy_qyz;
@@ -295,41 +274,23 @@ __device__ __forceinline__ void primal_update(const TgvArgs<typename Dual<PREC>:
 
     // v <- v - tau (div q - p), vbar                     (tgv2_common.cu:338-347)
     {
-        const float vo = ldf<CG>(a.v_in[0], i);
+        const float vo = a.v_in[0][i];
         const float vn = vo - a.tau * (dx - pxi);
         a.v0[i] = vn;
         a.vbo[0][i] = vn + a.theta * (vn - vo);
     }
     {
-        const float vo = ldf<CG>(a.v_in[1], i);
+        const float vo = a.v_in[1][i];
         const float vn = vo - a.tau * (dy - pyi);
         a.v1[i] = vn;
         a.vbo[1][i] = vn + a.theta * (vn - vo);
     }
     if constexpr (THREE) {
-        const float vo = ldf<CG>(a.v_in[2], i);
+        const float vo = a.v_in[2][i];
         const float vn = vo - a.tau * (dz - pzi);
         a.v2[i] = vn;
         a.vbo[2][i] = vn + a.theta * (vn - vo);
     }
-}
-
-// Dual pass (one launch per iteration).
-template <int PREC, bool THREE>
-__global__ void __launch_bounds__(BX* BY) tgv_dual_kernel(TgvArgs<typename Dual<PREC>::T> a) {
-    const int x = blockIdx.x * BX + threadIdx.x;
-    const int y = blockIdx.y * BY + threadIdx.y;
-    if (x >= a.W || y >= a.H) return;
-    dual_update<PREC, THREE, false>(a, x, y, (int)blockIdx.z);
-}
-
-// Primal pass.
-template <int PREC, bool THREE, int DATA>
-__global__ void __launch_bounds__(BX* BY) tgv_primal_kernel(TgvArgs<typename Dual<PREC>::T> a) {
-    const int x = blockIdx.x * BX + threadIdx.x;
-    const int y = blockIdx.y * BY + threadIdx.y;
-    if (x >= a.W || y >= a.H) return;
-    primal_update<PREC, THREE, DATA, false>(a, x, y, (int)blockIdx.z);
 }
 
 // ---- fused single-pass iteration ---------------------------------------------------------
@@ -1351,152 +1312,6 @@ void iterate_two_pass(const TgvState& s, const TgvStep& k, cudaStream_t st) {
     launch_two_pass<PREC>(s, k, a, st);
 }
 
-// ---- persistent loop for a single plane --------------------------------------------
-//
-// A single plane (a 2-D image, or a volume of depth 1) of up to a few million pixels
-// keeps its whole state in L2, and one iteration is two short passes over it.  Launched
-// per pass, the launches themselves set the pace: 512 x 512 takes 6.2 us per
-// iteration for 2 x 0.26 M pixel updates.  Here one cooperative launch runs many
-// iterations.  Block b owns the rows [y0, y1) (one block per SM) and runs the two-pass
-// updates on them with loads through L2 (other blocks write the fields between the
-// passes).  Between passes a block waits only for its two neighbours: the dual pass
-// reads ubar and vbar one row either side (written by the neighbours' previous primal
-// pass) and writes p, q (read by their previous primal pass), the primal pass reads p
-// one row up and q one row down (written by the neighbours' dual pass) and writes
-// ubar, vbar (read by it).  Each block publishes a count of finished passes with a
-// release store after a block barrier; a neighbour polls it with acquire loads, a
-// bounded wait (the state's pipeline wait limit) that raises the error flag and ends
-// the launch when it runs out.  The arithmetic is the two-pass kernels' (the same
-// device functions), so the results are bit-identical to theirs.
-constexpr int STRIP_THREADS = 1024;
-constexpr int STRIP_MAX_BLOCKS = 1024;  // per launch; flags for two counts per block
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-// One thread waits until *flag >= target; false when the limit ran out (error raised).
-__device__ bool wait_count(const unsigned* flag, unsigned target, uint64_t limit_ns, int* err) {
-    if (ld_acquire_u32(flag) >= target) return true;
-    if (limit_ns == 0) {
-        atomicExch(err, 1);
-        return false;
-    }
-    uint64_t t0, t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-    while (true) {
-        if (ld_acquire_u32(flag) >= target) return true;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        if (t - t0 > limit_ns) {
-            atomicExch(err, 1);
-            return false;
-        }
-        if (*(volatile int*)err) return false;  // another block gave up already
-        __nanosleep(20);
-    }
-}
-
-template <int PREC, bool THREE, int DATA>
-__global__ void __launch_bounds__(STRIP_THREADS, 1)
-    tgv_strips_kernel(TgvArgs<typename Dual<PREC>::T> a, int iterations, unsigned* flags,
-                      unsigned long long wait_ns, int* err) {
-    __shared__ int fail;
-    const int nb = (int)gridDim.x, b = (int)blockIdx.x;
-    const int q = a.H / nb, r = a.H % nb;
-    const int y0 = b * q + min(b, r), y1 = y0 + q + (b < r ? 1 : 0);
-    const int npix = (y1 - y0) * a.W;
-    unsigned* dual_done = flags;
-    unsigned* primal_done = flags + STRIP_MAX_BLOCKS;
-    if (threadIdx.x == 0) fail = *(volatile int*)err;
-    __syncthreads();
-    if (fail) return;
-    // thread 0 waits for both neighbours' count of one kind of pass
-    auto wait_neighbours = [&](const unsigned* done, unsigned target) {
-        if (threadIdx.x == 0) {
-            bool ok = true;
-            if (b > 0) ok = wait_count(done + b - 1, target, wait_ns, err);
-            if (ok && b + 1 < nb) ok = wait_count(done + b + 1, target, wait_ns, err);
-            fail = ok ? 0 : 1;
-        }
-        __syncthreads();
-        return fail == 0;
-    };
-    auto publish = [&](unsigned* done, unsigned count) {
-        __syncthreads();  // every thread's stores of the pass precede the release
-        if (threadIdx.x == 0) {
-            __threadfence();
-            st_release_u32(done + b, count);
-        }
-    };
-    for (int it = 0; it < iterations; ++it) {
-        // the neighbours' primal pass of the previous iteration (the launch's first
-        // iteration follows a finished launch)
-        if (it > 0 && !wait_neighbours(primal_done, (unsigned)it)) return;
-        for (int e = (int)threadIdx.x; e < npix; e += STRIP_THREADS) {
-            const int y = y0 + e / a.W, x = e % a.W;
-            if (TGV_IN_BOUNDS((size_t)y * a.W + x, a.WH, 40))
-                dual_update<PREC, THREE, true>(a, x, y, 0);
-        }
-        publish(dual_done, (unsigned)it + 1);
-        if (!wait_neighbours(dual_done, (unsigned)it + 1)) return;
-        for (int e = (int)threadIdx.x; e < npix; e += STRIP_THREADS) {
-            const int y = y0 + e / a.W, x = e % a.W;
-            if (TGV_IN_BOUNDS((size_t)y * a.W + x, a.WH, 41))
-                primal_update<PREC, THREE, DATA, true>(a, x, y, 0);
-        }
-        publish(primal_done, (unsigned)it + 1);
-    }
-}
-
-// Blocks of one strips launch for this state (0: the kernel cannot run here).
-template <int PREC>
-int strips_blocks(const TgvState& s) {
-    static std::atomic<int> cached{-1};
-    int per_sm = cached.load(std::memory_order_relaxed);
-    if (per_sm < 0) {
-        int dev = 0, coop = 0, n = 0;
-        TGV_CUDA(cudaGetDevice(&dev));
-        TGV_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-        if (coop)
-            TGV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &n, tgv_strips_kernel<PREC, true, TGVDCT_DATA_L1>, STRIP_THREADS, 0));
-        per_sm = n > 0 ? 1 : 0;
-        cached.store(per_sm, std::memory_order_relaxed);
-    }
-    if (!per_sm) return 0;
-    int dev = 0, sms = 0;
-    TGV_CUDA(cudaGetDevice(&dev));
-    TGV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    return std::min({sms, s.H, STRIP_MAX_BLOCKS});
-}
-
-template <int PREC>
-void iterate_strips(const TgvState& s, const TgvStep& k, int iterations, cudaStream_t st) {
-    const TgvStencilFields& F = s.now();  // in place, as the two-pass kernels
-    float* const v[3] = {s.v[0], s.v[1], s.v[2]};
-    auto a = make_args<PREC>(s, k, F, s.u, v, F, s.u, v);
-    const int nb = strips_blocks<PREC>(s);
-    TGV_CUDA(cudaMemsetAsync(s.strip_flags, 0, 2 * STRIP_MAX_BLOCKS * sizeof(unsigned), st));
-    unsigned* flags = s.strip_flags;
-    unsigned long long wait_ns = s.wait_ns;
-    int* err = s.err;
-    void* args[] = {&a, &iterations, &flags, &wait_ns, &err};
-    const void* kern;
-    if (s.three)
-        kern = k.data_term == TGVDCT_DATA_L1
-                   ? (const void*)tgv_strips_kernel<PREC, true, TGVDCT_DATA_L1>
-                   : (const void*)tgv_strips_kernel<PREC, true, TGVDCT_DATA_L2>;
-    else
-        kern = k.data_term == TGVDCT_DATA_L1
-                   ? (const void*)tgv_strips_kernel<PREC, false, TGVDCT_DATA_L1>
-                   : (const void*)tgv_strips_kernel<PREC, false, TGVDCT_DATA_L2>;
-    TGV_CUDA(cudaLaunchCooperativeKernel(kern, dim3(nb), dim3(STRIP_THREADS), args, 0, st));
-}
-
 constexpr int FUSED_TY = 8;
 
 template <int PREC, bool THREE, int DATA>
@@ -1725,11 +1540,9 @@ size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kerne
     const size_t n = (size_t)W * H * D;
     const size_t f32 = align256(n * 4), dual = align256(n * elem_bytes(precision));
     const int ncomp = three ? 3 : 2, nq = three ? 6 : 3;
-    const int sets = in_place_kernel(kernel) ? 1 : 2;
-    // u, f, v + per set: ubar, vbar, p, q; plus a device error flag, and the pass
-    // counts of the persistent single-plane kernel
-    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq)) + 256 +
-           (kernel == TGV_KERNEL_STRIPS ? align256(2 * STRIP_MAX_BLOCKS * sizeof(unsigned)) : 0);
+    const int sets = kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
+    // u, f, v + per set: ubar, vbar, p, q; plus a device error flag
+    return f32 * (2 + ncomp) + sets * (f32 * (1 + ncomp) + dual * (ncomp + nq)) + 256;
 }
 
 void tgv_state_bind(TgvState& s, char* base) {
@@ -1745,7 +1558,7 @@ void tgv_state_bind(TgvState& s, char* base) {
     s.u = (float*)take(f32);
     s.f = (float*)take(f32);
     for (int k = 0; k < 3; ++k) s.v[k] = k < ncomp ? (float*)take(f32) : nullptr;
-    const int sets = in_place_kernel(s.kernel) ? 1 : 2;
+    const int sets = s.kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
     s.tma_cache.reset();
     // q order: xx yy zz xy xz yz; the 2-D launcher keeps xx yy xy
     const int order2[3] = {0, 1, 3};
@@ -1759,9 +1572,6 @@ void tgv_state_bind(TgvState& s, char* base) {
         for (int k = 0; k < nq; ++k) F.q[s.three ? k : order2[k]] = (void*)take(dual);
     }
     s.err = (int*)take(256);
-    s.strip_flags = s.kernel == TGV_KERNEL_STRIPS
-                        ? (unsigned*)take(align256(2 * STRIP_MAX_BLOCKS * sizeof(unsigned)))
-                        : nullptr;
     s.cur = 0;
 }
 
@@ -2004,9 +1814,7 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     }
     // The register-staged fused kernel has no domain support: a masked run whose
     // shape rules out TMA uses the two-pass kernels in place on the current set.
-    // a single iteration of the persistent single-plane kernel's state: the two-pass
-    // kernels (the same arithmetic, in place on the same set)
-    if (in_place_kernel(s.kernel) || s.domain) {
+    if (s.kernel == TGV_KERNEL_TWO_PASS || s.domain) {
         switch (s.precision) {
             case TGVDCT_STATE_FP32: iterate_two_pass<TGVDCT_STATE_FP32>(s, k, st); return;
             case TGVDCT_STATE_BF16_DUAL: iterate_two_pass<TGVDCT_STATE_BF16_DUAL>(s, k, st); return;
@@ -2022,37 +1830,6 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
     TGV_REQUIRE(false, "unknown state precision");
 }
 
-void tgv_iterate_n(TgvState& s, const TgvStep& k, int iterations, cudaStream_t st) {
-    if (iterations <= 0) return;
-    if (s.kernel == TGV_KERNEL_STRIPS && !s.domain && iterations > 1 &&
-        tgv_strips_available(s.precision)) {
-        switch (s.precision) {
-            case TGVDCT_STATE_FP32: iterate_strips<TGVDCT_STATE_FP32>(s, k, iterations, st); return;
-            case TGVDCT_STATE_BF16_DUAL:
-                iterate_strips<TGVDCT_STATE_BF16_DUAL>(s, k, iterations, st);
-                return;
-            case TGVDCT_STATE_FX16_DUAL:
-                iterate_strips<TGVDCT_STATE_FX16_DUAL>(s, k, iterations, st);
-                return;
-        }
-        TGV_REQUIRE(false, "unknown state precision");
-    }
-    for (int i = 0; i < iterations; ++i) tgv_iterate(s, k, st);
-}
-
-bool tgv_strips_available(int precision) {
-    TgvState probe;
-    probe.H = 1 << 30;
-    switch (precision) {
-        case TGVDCT_STATE_FP32: return strips_blocks<TGVDCT_STATE_FP32>(probe) > 0;
-        case TGVDCT_STATE_BF16_DUAL: return strips_blocks<TGVDCT_STATE_BF16_DUAL>(probe) > 0;
-        case TGVDCT_STATE_FX16_DUAL: return strips_blocks<TGVDCT_STATE_FX16_DUAL>(probe) > 0;
-    }
-    return false;
-}
-
-int tgv_kernels_per_iteration(const TgvState& s) {
-    return in_place_kernel(s.kernel) ? 2 : 1;
-}
+int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL_TWO_PASS ? 2 : 1; }
 
 }  // namespace tgvdct

@@ -83,9 +83,8 @@ typedef enum tgvdct_dct_mode {
 } tgvdct_dct_mode;
 
 typedef enum tgvdct_iteration_kernel {
-    TGVDCT_KERNEL_AUTO = 0,     /* the fused single pass for volumes; for a single plane
-                                   (depth 1) the persistent single-plane kernel when
-                                   the state fits in 96 MB, else the two-pass kernels */
+    TGVDCT_KERNEL_AUTO = 0,     /* the fused single pass for volumes, the two-pass
+                                   kernels for a single plane (depth 1) */
     /* two coalesced passes per iteration (dual, then primal), every field updated
        in place: 176 bytes per voxel-iteration in FP32 */
     TGVDCT_KERNEL_TWO_PASS = 1,
@@ -96,12 +95,7 @@ typedef enum tgvdct_iteration_kernel {
     /* the fused pass with the input planes staged through registers instead of
        the TMA pipeline (the fused kernel uses it by itself when the width is not a
        multiple of 4, or of 8 with 16-bit dual fields) */
-    TGVDCT_KERNEL_FUSED_REGISTER = 3,
-    /* single planes only: the two-pass arithmetic, many iterations in one cooperative
-       launch; each block owns a strip of rows and waits only for its two neighbours
-       between passes (bounded waits, tgvdct_set_pipeline_wait_limit).  Falls back to
-       the two-pass kernels, with the same bits, where the device cannot run it. */
-    TGVDCT_KERNEL_PERSISTENT_PLANE = 4
+    TGVDCT_KERNEL_FUSED_REGISTER = 3
 } tgvdct_iteration_kernel;
 
 typedef enum tgvdct_poisson_eigen {

@@ -80,35 +80,3 @@ def test_tensor_core_dct_wait_runs_out_and_the_context_recovers(gpu_lib, mode):
         torch.cuda.synchronize()
         fresh.check_device_error()
     assert torch.equal(out, ref)
-
-
-def test_persistent_plane_wait_runs_out_and_the_context_recovers(gpu_lib):
-    """The persistent single-plane kernel's blocks wait for their neighbours between
-    passes; with the limit at 0 the first wait that finds a neighbour not yet done
-    gives up, and every other block leaves at its next wait."""
-    import torch
-    from ambient_image_processor_gb300.phantoms import rectangles_ellipses_2d
-    f = torch.from_numpy(rectangles_ellipses_2d(512, 512, seed=2)).cuda()
-    prm = pkg.default_params(width=512, height=512, depth=1, iteration_count=64,
-                             geometry=pkg.GEOMETRY_2D,
-                             iteration_kernel=pkg.KERNEL_PERSISTENT_PLANE)
-    out = [torch.empty_like(f) for _ in range(4)]
-    ref = [torch.empty_like(f) for _ in range(4)]
-
-    def run(ctx, bufs):
-        ctx.run_dev(f.data_ptr(), *(b.data_ptr() for b in bufs))
-
-    with pkg.Context(prm) as ctx:
-        ctx.set_pipeline_wait_limit(0)
-        run(ctx, out)
-        _expect_timeout(ctx)
-        ctx.set_pipeline_wait_limit(DEFAULT_NS)
-        run(ctx, out)
-        torch.cuda.synchronize()
-        ctx.check_device_error()
-    with pkg.Context(prm) as fresh:
-        run(fresh, ref)
-        torch.cuda.synchronize()
-        fresh.check_device_error()
-    for a, b in zip(out, ref):
-        assert torch.equal(a, b)
