@@ -18,6 +18,7 @@
 // inverse passes.  Forward x8 and inverse /(8 W H D) follow the reference's scale
 // factors (cosine_transform.cu:222, inverse_cosine_transform.cu:163), so the round
 // trip is the identity.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -297,19 +298,21 @@ void pass(const DctPlan* p, int axis, const float* Mat, const float* in, float* 
 }
 
 // ---- element-wise kernels --------------------------------------------------------------
+// One block row of threads per (y, z) row: x from the thread, no per-element divisions.
 __global__ void divergence_kernel(const float* __restrict__ vx, const float* __restrict__ vy,
                                   const float* __restrict__ vz, int W, int H, int D,
                                   float* __restrict__ out) {
-    const size_t n = (size_t)W * H * D;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(idx % W);
-        const int y = (int)((idx / W) % H);
-        const int z = (int)(idx / ((size_t)W * H));
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    const size_t WH = (size_t)W * H;
+    const long long rows = (long long)H * D;
+    for (long long row = blockIdx.y; row < rows; row += gridDim.y) {
+        const int y = (int)(row % H), z = (int)(row / H);
+        const size_t idx = (size_t)row * W + x;
         const float bx = (x > 0 ? vx[idx - 1] : 0.f) - vx[idx];
         const float by = (y > 0 ? vy[idx - W] : 0.f) - vy[idx];
         float s = bx + by;
-        if (D > 1) s = s + ((z > 0 ? vz[idx - (size_t)W * H] : 0.f) - vz[idx]);
+        if (D > 1) s = s + ((z > 0 ? vz[idx - WH] : 0.f) - vz[idx]);
         out[idx] = s;
     }
 }
@@ -498,8 +501,9 @@ void dct_plan_destroy(DctPlan* p) {
 
 void divergence(DctPlan* p, const float* vx, const float* vy, const float* vz, float* out,
                 cudaStream_t st) {
-    const size_t n = (size_t)p->W * p->H * p->D;
-    divergence_kernel<<<ew_grid(n), 256, 0, st>>>(vx, vy, vz, p->W, p->H, p->D, out);
+    const long long rows = (long long)p->H * p->D;
+    const dim3 grid(ceil_div((size_t)p->W, 128), (unsigned)std::min(rows, 65535ll));
+    divergence_kernel<<<grid, 128, 0, st>>>(vx, vy, vz, p->W, p->H, p->D, out);
     TGV_CHECK_LAUNCH();
 }
 
