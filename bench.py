@@ -612,13 +612,16 @@ def accuracy_vs_fp64(pkg, torch, f_host, iters, stream):
                                  state_precision=prec, dct_mode=DCT_MODES[dct],
                                  poisson_eigen=eig)
         with pkg.Context(prm) as ctx:
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            ctx.process_dev(f.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
-                            set_negative_values_to_zero=False, log_domain=True,
-                            stream=stream.cuda_stream)
-            e1.record(stream)
-            torch.cuda.synchronize()
+            # the first deshade builds the context's DCT plan; the second is timed
+            for timed in (False, True):
+                e0, e1 = (torch.cuda.Event(enable_timing=True),
+                          torch.cuda.Event(enable_timing=True))
+                e0.record(stream)
+                ctx.process_dev(f.data_ptr(), u.data_ptr(), l.data_ptr(), r.data_ptr(),
+                                set_negative_values_to_zero=False, log_domain=True,
+                                stream=stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
             ctx.check_device_error(stream.cuda_stream)
         got = {"u": u.cpu().numpy(), "l": l.cpu().numpy(), "r": r.cpu().numpy()}
         err = {k: float(np.linalg.norm(got[k] - ref[k]) / np.linalg.norm(ref[k])) for k in ref}
