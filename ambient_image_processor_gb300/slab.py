@@ -122,29 +122,34 @@ def deshade_rank(geo: SlabGeometry, backend, f_local, iterations: int, *,
                  set_negative_values_to_zero: bool = False):
     """One rank's deshade as a generator of communication requests.
 
-    Yields ("halo", send_down, send_up) and expects (from_below, from_above) back
-    (None where there is no neighbour); yields ("alltoall", chunks) with one chunk
-    per destination rank and expects the list of chunks received, by source rank.
-    Returns (u, v_x, v_y, v_z, l, r) of the rank's own planes."""
+    Yields ("halo", send_down, send_up, n_below, n_above): the planes for the rank
+    below and above (None where nothing goes there) and the number of values expected
+    from the rank below and above (None where nothing comes); expects (from_below,
+    from_above) back.  Yields ("alltoall", chunks) with one chunk per destination rank
+    and expects the list of chunks received, by source rank.  Returns (u, v_x, v_y,
+    v_z, l, r) of the rank's own planes."""
     import torch
 
     geo.check()
     W, H, D = geo.width, geo.height, geo.depth
     Dl, lo = geo.local_depth, geo.below
     first, last = lo, lo + geo.own_planes - 1
+    n_halo = field_count(HALO_FIELDS) * W * H
     backend.init(f_local)
     for _ in range(iterations):
         backend.step()
         send_down = backend.read(HALO_FIELDS, first) if geo.below else None
         send_up = backend.read(HALO_FIELDS, last) if geo.above else None
-        from_below, from_above = yield ("halo", send_down, send_up)
+        from_below, from_above = yield ("halo", send_down, send_up,
+                                        n_halo if geo.below else None,
+                                        n_halo if geo.above else None)
         if from_below is not None:
             backend.write(HALO_FIELDS, 0, from_below)
         if from_above is not None:
             backend.write(HALO_FIELDS, Dl - 1, from_above)
     # the divergence reads v_z one plane below
     send_up = backend.read(FIELD_V_Z, last) if geo.above else None
-    from_below, _ = yield ("halo", None, send_up)
+    from_below, _ = yield ("halo", None, send_up, W * H if geo.below else None, None)
     if from_below is not None:
         backend.write(FIELD_V_Z, 0, from_below)
     u, vx, vy, vz = backend.read_all(FIELD_U | FIELD_V).view(4, Dl, H, W).unbind(0)
@@ -223,46 +228,30 @@ def run_distributed(gen, rank: int, ranks: int, group=None):
 
 
 def _halo_exchange(req, rank, ranks, group):
-    """Sends a rank's two halo planes and receives its neighbours'.  The message from
-    the rank below is that rank's send_up, whose size is announced first (the field
-    sets differ by direction and by stage)."""
+    """Sends a rank's halo planes to its neighbours and receives theirs (sizes known
+    to both sides), as one batch of point-to-point operations."""
     import torch
     import torch.distributed as dist
 
-    _, send_down, send_up = req
-    dev = (send_down if send_down is not None else send_up)
-    device = dev.device if dev is not None else torch.device("cpu")
-    # sizes first (an int64 each way), then the planes
-    size_ops, sizes_in = [], {}
-    n_down = torch.tensor([send_down.numel() if send_down is not None else -1],
-                          dtype=torch.int64, device=device)
-    n_up = torch.tensor([send_up.numel() if send_up is not None else -1], dtype=torch.int64,
-                        device=device)
-    if rank > 0:
-        sizes_in["below"] = torch.empty(1, dtype=torch.int64, device=device)
-        size_ops += [dist.P2POp(dist.isend, n_down, rank - 1, group),
-                     dist.P2POp(dist.irecv, sizes_in["below"], rank - 1, group)]
-    if rank < ranks - 1:
-        sizes_in["above"] = torch.empty(1, dtype=torch.int64, device=device)
-        size_ops += [dist.P2POp(dist.isend, n_up, rank + 1, group),
-                     dist.P2POp(dist.irecv, sizes_in["above"], rank + 1, group)]
-    for w in dist.batch_isend_irecv(size_ops) if size_ops else []:
-        w.wait()
+    _, send_down, send_up, n_below, n_above = req
+    ref = send_down if send_down is not None else send_up
+    if ref is not None:
+        device = ref.device
+    elif dist.get_backend(group) == "nccl":  # a rank that only receives
+        device = torch.device("cuda", torch.cuda.current_device())
+    else:
+        device = torch.device("cpu")
     ops, from_below, from_above = [], None, None
-    if rank > 0:
-        nb = int(sizes_in["below"].item())
-        if send_down is not None:
-            ops.append(dist.P2POp(dist.isend, send_down, rank - 1, group))
-        if nb >= 0:
-            from_below = torch.empty(nb, dtype=torch.float32, device=device)
-            ops.append(dist.P2POp(dist.irecv, from_below, rank - 1, group))
-    if rank < ranks - 1:
-        na = int(sizes_in["above"].item())
-        if send_up is not None:
-            ops.append(dist.P2POp(dist.isend, send_up, rank + 1, group))
-        if na >= 0:
-            from_above = torch.empty(na, dtype=torch.float32, device=device)
-            ops.append(dist.P2POp(dist.irecv, from_above, rank + 1, group))
+    if send_down is not None:
+        ops.append(dist.P2POp(dist.isend, send_down.contiguous(), rank - 1, group))
+    if send_up is not None:
+        ops.append(dist.P2POp(dist.isend, send_up.contiguous(), rank + 1, group))
+    if n_below is not None:
+        from_below = torch.empty(n_below, dtype=torch.float32, device=device)
+        ops.append(dist.P2POp(dist.irecv, from_below, rank - 1, group))
+    if n_above is not None:
+        from_above = torch.empty(n_above, dtype=torch.float32, device=device)
+        ops.append(dist.P2POp(dist.irecv, from_above, rank + 1, group))
     for w in dist.batch_isend_irecv(ops) if ops else []:
         w.wait()
     return from_below, from_above
