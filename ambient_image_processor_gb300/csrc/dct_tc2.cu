@@ -563,6 +563,12 @@ template <int MODE>
 constexpr size_t pipe_smem() {
     return (size_t)PGeo<PM_BF16X3>::NS * PGeo<PM_BF16X3>::STAGE + 1024;
 }
+// the TF32 ring must fit in the footprint both modes request
+static_assert(PGeo<PM_TF32>::NS * PGeo<PM_TF32>::STAGE <=
+                  PGeo<PM_BF16X3>::NS * PGeo<PM_BF16X3>::STAGE,
+              "the TF32 stages overflow the shared memory both modes request");
+static_assert(PGeo<PM_BF16X3>::NS <= P_STAGES_MAX && PGeo<PM_TF32>::NS <= P_STAGES_MAX,
+              "more stages than mbarriers");
 
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
