@@ -14,11 +14,11 @@ from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
 pytestmark = pytest.mark.gpu
 
 
-def _whole(f, iterations, eigen):
+def _whole(f, iterations, eigen, data=pkg.DATA_L1):
     import torch
     D, H, W = f.shape
     prm = pkg.default_params(width=W, height=H, depth=D, iteration_count=iterations,
-                             poisson_eigen=eigen)
+                             poisson_eigen=eigen, data_term=data)
     u, vx, vy, vz, l = (torch.empty_like(f) for _ in range(5))
     with pkg.Context(prm) as ctx:
         ctx.run_dev(f.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(), vz.data_ptr())
@@ -28,17 +28,21 @@ def _whole(f, iterations, eigen):
     return u, vx, vy, vz, l
 
 
-@pytest.mark.parametrize("shape,ranks,iterations,eigen", [
-    ((24, 40, 48), 2, 60, pkg.EIGEN_REFERENCE),
-    ((31, 36, 44), 3, 45, pkg.EIGEN_ACCURATE),
-    ((64, 96, 128), 4, 40, pkg.EIGEN_REFERENCE),
+@pytest.mark.parametrize("shape,ranks,iterations,eigen,data", [
+    ((24, 40, 48), 2, 60, pkg.EIGEN_REFERENCE, pkg.DATA_L1),
+    ((31, 36, 44), 3, 45, pkg.EIGEN_ACCURATE, pkg.DATA_L1),
+    ((64, 96, 128), 4, 40, pkg.EIGEN_REFERENCE, pkg.DATA_L1),
+    # a width that rules out TMA: the register-staged fused kernel on every slab
+    ((20, 30, 42), 2, 35, pkg.EIGEN_REFERENCE, pkg.DATA_L1),
+    ((40, 24, 32), 5, 30, pkg.EIGEN_ACCURATE, pkg.DATA_L2),
 ])
-def test_emulated_ranks_equal_the_single_volume(gpu_lib, shape, ranks, iterations, eigen):
+def test_emulated_ranks_equal_the_single_volume(gpu_lib, shape, ranks, iterations, eigen,
+                                                data):
     import torch
     D, H, W = shape
     f = torch.from_numpy(np.log(tissue_phantom_3d(D, H, W, seed=6))).cuda()
-    ref = _whole(f, iterations, eigen)
-    prm = pkg.default_params(width=W, height=H, depth=D, poisson_eigen=eigen)
+    ref = _whole(f, iterations, eigen, data)
+    prm = pkg.default_params(width=W, height=H, depth=D, poisson_eigen=eigen, data_term=data)
     backends, gens = [], []
     for r in range(ranks):
         geo = slab.SlabGeometry(W, H, D, ranks, r)
