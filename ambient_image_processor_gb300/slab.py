@@ -283,7 +283,7 @@ class CudaSlabBackend:
     and FP32 contractions (the combination whose results the slab split reproduces
     bit for bit)."""
 
-    def __init__(self, params, geo: SlabGeometry, stream=None):
+    def __init__(self, params, geo: SlabGeometry):
         import copy
 
         import torch
@@ -294,12 +294,19 @@ class CudaSlabBackend:
         self.geo = geo
         self.params = copy.copy(params)
         self.params.depth = geo.local_depth
+        self.device = torch.device("cuda", torch.cuda.current_device())
         self.ctx = Context(self.params)
-        self.stream = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         self._lib = lib
         self._pencil = None
         self.W, self.H = geo.width, geo.height
         self.Dl = geo.local_depth
+
+    @property
+    def stream(self):
+        """torch's current stream on this device: the library's calls and the torch
+        operations of the driver (slicing, concatenation) stay in one order."""
+        import torch
+        return torch.cuda.current_stream(self.device).cuda_stream
 
     def close(self):
         if self._pencil:
@@ -321,7 +328,7 @@ class CudaSlabBackend:
     def _read(self, mask, plane, count):
         import torch
         out = torch.empty(field_count(mask) * count * self.W * self.H, dtype=torch.float32,
-                          device="cuda")
+                          device=self.device)
         self._check(self._lib().tgvdct_state_read_dev(self.ctx._ctx, mask, plane, count,
                                                       out.data_ptr(), self.stream))
         return out
@@ -339,7 +346,7 @@ class CudaSlabBackend:
 
     def poisson_xy(self, vx, vy, vz):
         import torch
-        out = torch.empty(self.Dl, self.H, self.W, dtype=torch.float32, device="cuda")
+        out = torch.empty(self.Dl, self.H, self.W, dtype=torch.float32, device=self.device)
         vx, vy, vz = (t.contiguous() for t in (vx, vy, vz))
         self._check(self._lib().tgvdct_slab_poisson_xy_dev(
             self.ctx._ctx, vx.data_ptr(), vy.data_ptr(), vz.data_ptr(), out.data_ptr(),
