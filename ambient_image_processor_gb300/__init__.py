@@ -26,6 +26,7 @@ STATE_FP32, STATE_BF16_DUAL, STATE_FX16_DUAL = 0, 1, 2
 DCT_FP32, DCT_TF32, DCT_BF16X3 = 0, 1, 2
 EIGEN_REFERENCE, EIGEN_ACCURATE = 0, 1
 KERNEL_AUTO, KERNEL_TWO_PASS, KERNEL_FUSED, KERNEL_FUSED_REGISTER = 0, 1, 2, 3
+KERNEL_FUSED_SHIFTED = 4
 
 _STATUS_NAMES = {OK: "ok", ERR_BAD_ARG: "bad argument", ERR_OOM: "out of memory",
                  ERR_CUDA: "CUDA error", ERR_NO_DEVICE: "no suitable CUDA device",
@@ -76,6 +77,7 @@ _SIGS = {
     "tgvdct_destroy": [_vp],
     "tgvdct_set_params": [_vp, ctypes.POINTER(Params)],
     "tgvdct_iterations_run": [_vp],
+    "tgvdct_loop_launches": [_vp],
     "tgvdct_tgv2_l1_deshade_launch": [_f32p, _u32, _u32, _u32, _flt, _u32, _u32, ctypes.c_int,
                                       CALLBACK, _vp, _flt, _flt, _f32p, _f32p, _f32p, _f32p],
     "tgvdct_tgv2_l1_deshade_launch_2d": [_f32p, _u32, _u32, _flt, _u32, _u32, CALLBACK, _vp,
@@ -151,6 +153,7 @@ _SIGS = {
 }
 _RESTYPES = {"tgvdct_params_init": None, "tgvdct_workspace_bytes": ctypes.c_size_t,
              "tgvdct_iterations_run": ctypes.c_uint32, "tgvdct_version": ctypes.c_char_p,
+             "tgvdct_loop_launches": ctypes.c_uint64,
              "tgvdct_last_error": ctypes.c_char_p, "tgvdct_status_string": ctypes.c_char_p,
              "tgvdct_resize_factor_extent": ctypes.c_uint32,
              "tgvdct_state_bytes": ctypes.c_size_t,
@@ -677,6 +680,10 @@ class Context:
     @property
     def iterations_run(self) -> int:
         return int(lib().tgvdct_iterations_run(self._ctx))
+
+    def loop_launches(self) -> int:
+        """Iteration kernels the context's last loop launched (graph replays included)."""
+        return int(lib().tgvdct_loop_launches(self._ctx))
 
     def set_params(self, params: Params):
         _check(lib().tgvdct_set_params(self._ctx, ctypes.byref(params)), allow_stop=False)

@@ -25,6 +25,7 @@ struct tgvdct_context {
     void* state_block = nullptr;
     DctPlan* plan = nullptr;
     uint32_t iterations_run = 0;
+    uint64_t loop_launches = 0;  // iteration kernels the last loop launched
     // stopping: a request from any thread, and the energy checks of the last loop
     std::atomic<bool> stop_requested{false};
     double* energy_dev = nullptr;  // 3 sums of one energy evaluation
@@ -39,10 +40,11 @@ struct tgvdct_context {
     float* domain_mask = nullptr;
     uint8_t* domain = nullptr;
     uint32_t* tile_flags = nullptr;  // per-block plane ranges of the fused TMA kernel
-    // CUDA graph of kGraphChunk iterations (an even number, so the ping-pong parity
-    // of the state is unchanged after a replay), captured on a private stream and
-    // replayed on the caller's; rebuilt when the step or the state changes
+    // CUDA graph of graph_chunk(st) iterations (an even number, so the ping-pong
+    // parity of the state is unchanged after a replay), captured on a private stream
+    // and replayed on the caller's; rebuilt when the step or the state changes
     cudaGraphExec_t graph = nullptr;
+    int graph_launches = 0;
     cudaStream_t capture_stream = nullptr;
     TgvStep graph_step{};
     const void* graph_domain = nullptr;
@@ -99,7 +101,7 @@ void validate(const tgvdct_params* p) {
     TGV_REQUIRE(std::isfinite(p->sigma) && p->sigma > 0.f, "sigma must be > 0");
     TGV_REQUIRE(std::isfinite(p->theta), "theta must be finite");
     TGV_REQUIRE(p->iteration_kernel >= TGVDCT_KERNEL_AUTO &&
-                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED_REGISTER,
+                    p->iteration_kernel <= TGVDCT_KERNEL_FUSED_SHIFTED,
                 "unknown iteration kernel");
     TGV_REQUIRE(p->z_chunk >= 0, "z_chunk must be >= 0");
     TGV_REQUIRE(p->energy_tolerance >= 0.f && std::isfinite(p->energy_tolerance),
@@ -115,6 +117,7 @@ int kernel_of(const tgvdct_params& p) {
         case TGVDCT_KERNEL_TWO_PASS: return TGV_KERNEL_TWO_PASS;
         case TGVDCT_KERNEL_FUSED_REGISTER: return TGV_KERNEL_FUSED_REGISTER;
         case TGVDCT_KERNEL_FUSED: return TGV_KERNEL_FUSED;
+        case TGVDCT_KERNEL_FUSED_SHIFTED: return TGV_KERNEL_SHIFTED;
         default: return p.depth == 1 ? TGV_KERNEL_TWO_PASS : TGV_KERNEL_FUSED;
     }
 }
@@ -258,16 +261,18 @@ int deliver(tgvdct_context* c, tgvdct_iteration_callback cb, void* user, uint32_
     return cb(it, c->prm.iteration_count, dst[0], dst[1], dst[2], dst[3], user);
 }
 
-constexpr uint32_t kGraphChunk = 32;  // iterations per graph replay (even)
+// Iterations per graph replay (even).  Runs of shifted passes pay a dual and a primal
+// step of the two-pass kernels per run, so their graphs hold longer runs.
+uint32_t graph_chunk(const TgvState& s) { return tgv_uses_shifted(s) ? 128u : 32u; }
 
 bool same_step(const TgvStep& a, const TgvStep& b) {
     return a.tau == b.tau && a.sigma == b.sigma && a.theta == b.theta && a.lambda == b.lambda &&
            a.alpha0 == b.alpha0 && a.alpha1 == b.alpha1 && a.data_term == b.data_term;
 }
 
-// A graph of kGraphChunk iterations for the state's current parity and step, built
-// on first use (the first iteration of the loop has already run outside capture, so
-// every kernel attribute is set).  Null when capture is not possible.
+// A graph of graph_chunk iterations for the state's current parity and step, built
+// on first use (every kernel attribute is set before the capture).  Null when
+// capture is not possible.
 cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
     if (c->graph && same_step(c->graph_step, k) && c->graph_domain == c->st.domain &&
         c->graph_cur == c->st.cur && c->graph_zchunk == c->st.zchunk)
@@ -282,12 +287,13 @@ cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
         return nullptr;
     }
     cudaGraph_t g = nullptr;
+    tgv_prepare_launches(c->st);
     if (cudaStreamBeginCapture(c->capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
     const int cur = c->st.cur;
-    for (uint32_t i = 0; i < kGraphChunk; ++i) tgv_iterate(c->st, k, c->capture_stream);
+    const int launches = tgv_iterate_n(c->st, k, graph_chunk(c->st), c->capture_stream);
     const cudaError_t e = cudaStreamEndCapture(c->capture_stream, &g);
     TGV_REQUIRE(c->st.cur == cur, "a graph chunk must keep the state's parity");
     if (e != cudaSuccess || !g) {
@@ -302,16 +308,13 @@ cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
         return nullptr;
     }
     c->graph_step = k;
+    c->graph_launches = launches;
     c->graph_domain = c->st.domain;
     c->graph_cur = cur;
     c->graph_zchunk = c->st.zchunk;
     return c->graph;
 }
 
-// The iteration loop on the context's state (st.f already holds the input).
-// `on_iteration` decides what a callback sees; returns true if stopped.  Stretches
-// of kGraphChunk iterations with no callback due run as one CUDA graph replay (the
-// small-volume loops are launch-bound otherwise).
 // The weighted primal energy of the loop's current (u, v) (synchronous).
 double state_energy(tgvdct_context* c, cudaStream_t s) {
     if (!c->energy_dev) TGV_CUDA(cudaMalloc(&c->energy_dev, 3 * sizeof(double)));
@@ -325,10 +328,13 @@ double state_energy(tgvdct_context* c, cudaStream_t s) {
 }
 
 // The iteration loop on the context's state (st.f already holds the input).
-// `on_iteration` decides what a callback sees; returns true if stopped.  Stretches
-// of kGraphChunk iterations with no callback or energy check due run as one CUDA
-// graph replay (the small-volume loops are launch-bound otherwise).  A stop request
-// is honoured between host-side steps; the energy test after its checks.
+// `on_iteration` decides what a callback sees; returns true if stopped.  The host
+// looks at the state only after iterations j > 0 with j % paint == 0 (callbacks,
+// tgv2_common.cu:381-384) or j % check == 0 (energy checks): the iterations up to
+// the next such j run as one stretch (tgv_iterate_n, shifted passes where the state
+// allows), whose full graph_chunk parts are CUDA graph replays (the small-volume
+// loops are launch-bound otherwise).  A stop request is honoured between stretches
+// and graph replays; the energy test after its checks.
 template <class OnIteration>
 bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration,
               bool from_initial_state = true) {
@@ -342,45 +348,64 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
     auto next_multiple = [](uint32_t it, uint32_t m) {
         return (it % m == 0) ? it : (it / m + 1) * m;
     };
+    const uint32_t chunk = graph_chunk(c->st);
     c->iterations_run = 0;
+    c->loop_launches = 0;
     c->energy_history.clear();
+    tgv_prepare_launches(c->st);
     for (uint32_t it = 0; it < n_it;) {
         if (c->stop_requested.exchange(false)) {
             c->iterations_run = it;
             return true;
         }
-        // callbacks come after iterations j > 0 with j % paint == 0 (tgv2_common.cu:381-384),
-        // energy checks after iterations j > 0 with j % check == 0
-        if (it > 0 && it + kGraphChunk <= n_it) {
-            bool due = false;
-            if (cb_on) due = next_multiple(it, paint) < it + kGraphChunk;
-            if (check > 0) due = due || next_multiple(it, check) < it + kGraphChunk;
-            if (!due) {
-                if (cudaGraphExec_t g = loop_graph(c, k)) {
-                    TGV_CUDA(cudaGraphLaunch(g, s));
-                    it += kGraphChunk;
-                    continue;
-                }
+        // the last iteration of this stretch: the next one the host looks after
+        uint32_t last = n_it - 1;
+        const uint32_t from = std::max<uint32_t>(it, 1);
+        if (cb_on) last = std::min(last, next_multiple(from, paint));
+        if (check > 0) last = std::min(last, next_multiple(from, check));
+        uint32_t run = last + 1 - it;
+        bool stopped = false;
+        // graph replays where a whole chunk fits; not at the loop's first iteration,
+        // so that a short loop never pays a capture
+        while (it > 0 && run >= chunk) {
+            cudaGraphExec_t g = loop_graph(c, k);
+            if (!g) break;
+            TGV_CUDA(cudaGraphLaunch(g, s));
+            c->loop_launches += (uint64_t)c->graph_launches;
+            it += chunk;
+            run -= chunk;
+            if (run > 0 && c->stop_requested.exchange(false)) {
+                stopped = true;
+                break;
             }
         }
-        tgv_iterate(c->st, k, s);
-        if (cb_on && it > 0 && it % paint == 0) {
-            if (on_iteration(it)) {
-                c->iterations_run = it + 1;
+        if (stopped) {
+            c->iterations_run = it;
+            return true;
+        }
+        if (it == 0 && run > chunk) run = 1;  // the first iteration alone, then graphs
+        if (run > 0) {
+            c->loop_launches += (uint64_t)tgv_iterate_n(c->st, k, run, s);
+            it += run;
+        }
+        const uint32_t j = it - 1;  // the last iteration run
+        if (j != last) continue;
+        if (cb_on && j > 0 && j % paint == 0) {
+            if (on_iteration(j)) {
+                c->iterations_run = j + 1;
                 return true;
             }
         }
-        if (check > 0 && it > 0 && it % check == 0) {
+        if (check > 0 && j > 0 && j % check == 0) {
             const double e = state_energy(c, s);
             const bool settled = tol > 0.0 && !c->energy_history.empty() &&
                                  std::fabs(e - c->energy_history.back()) <= tol * std::fabs(e);
             c->energy_history.push_back(e);
             if (settled) {
-                c->iterations_run = it + 1;
+                c->iterations_run = j + 1;
                 return true;
             }
         }
-        ++it;
     }
     c->iterations_run = n_it;
     return false;
@@ -923,6 +948,8 @@ tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p) {
 
 uint32_t tgvdct_iterations_run(const tgvdct_context* ctx) { return ctx ? ctx->iterations_run : 0; }
 
+uint64_t tgvdct_loop_launches(const tgvdct_context* ctx) { return ctx ? ctx->loop_launches : 0; }
+
 tgvdct_status tgvdct_tgv2_run_dev(tgvdct_context* c, const float* f_dev, float* u_dev,
                                   float* v_x_dev, float* v_y_dev, float* v_z_dev,
                                   tgvdct_iteration_callback cb, void* user, void* stream) {
@@ -1057,7 +1084,7 @@ tgvdct_status tgvdct_tgv2_step_dev(tgvdct_context* c, uint32_t iterations, void*
     return guarded([&] {
         TGV_REQUIRE(c != nullptr, "null context");
         const TgvStep k = step_of(c->prm);
-        for (uint32_t i = 0; i < iterations; ++i) tgv_iterate(c->st, k, (cudaStream_t)stream);
+        c->loop_launches = (uint64_t)tgv_iterate_n(c->st, k, iterations, (cudaStream_t)stream);
         c->iterations_run = iterations;
         return TGVDCT_OK;
     });
@@ -1221,10 +1248,12 @@ tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const floa
         TGV_CUDA(cudaMemcpyAsync(c->st.f, f_dev, n * 4, cudaMemcpyDeviceToDevice, s));
         tgv_state_init(c->st, s);
         const TgvStep k = step_of(c->prm);
-        for (uint32_t it = 0; it < K; ++it) {
-            if (it % checkpoint_every == 0)
-                tgv_save_state(c->st, full_state_at(c->ckpt_block, it / checkpoint_every, n), s);
-            tgv_iterate(c->st, k, s);
+        for (uint32_t it = 0; it < K;) {
+            // the iterations between two checkpoints as one stretch
+            tgv_save_state(c->st, full_state_at(c->ckpt_block, it / checkpoint_every, n), s);
+            const uint32_t len = std::min(checkpoint_every, K - it);
+            tgv_iterate_n(c->st, k, len, s);
+            it += len;
         }
         tgv_save_state(c->st, full_state_at(c->ckpt_block, count, n), s);
         c->iterations_run = K;

@@ -52,7 +52,14 @@ struct TgvStencilFields {
     void* q[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // xx yy zz xy xz yz
 };
 
-enum TgvKernel { TGV_KERNEL_TWO_PASS = 1, TGV_KERNEL_FUSED = 2, TGV_KERNEL_FUSED_REGISTER = 3 };
+enum TgvKernel {
+    TGV_KERNEL_TWO_PASS = 1,
+    TGV_KERNEL_FUSED = 2,
+    TGV_KERNEL_FUSED_REGISTER = 3,
+    // runs of iterations as shifted passes (primal of n, dual of n + 1); single
+    // iterations and the shapes it cannot take as TGV_KERNEL_FUSED
+    TGV_KERNEL_SHIFTED = 4
+};
 
 // Bounds-checking builds (-DTGV_CHECK_BOUNDS, libtgvdct_checked.so): kernels check
 // the indices they are about to use and record the first bad one instead of making
@@ -120,6 +127,8 @@ struct TgvState {
     // (built on first use; the fused kernel falls back to register prefetch for
     // shapes the TMA stride rules exclude)
     std::shared_ptr<void> tma_cache;
+    // tensor maps of the shifted passes (built on first use)
+    std::shared_ptr<void> shifted_cache;
     int* err = nullptr;      // device flag raised by a pipeline wait that timed out
     // limit of the fused TMA kernel's pipeline waits (tgvdct_set_pipeline_wait_limit)
     uint64_t wait_ns = 200000000ull;
@@ -162,6 +171,16 @@ void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st);
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.
 int tgv_kernels_per_iteration(const TgvState& s);
+// n iterations.  With TGV_KERNEL_SHIFTED (FP32, 3-D, depth >= 2, width a multiple of 4,
+// no domain) and n >= 2 they run as a dual step, n - 1 shifted passes and a primal
+// step; otherwise as n calls of tgv_iterate.  Either way the state ends in the
+// standard form with the parity n single iterations give.  Returns the launches.
+int tgv_iterate_n(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st);
+// Whether tgv_iterate_n runs shifted passes for this state.
+bool tgv_uses_shifted(const TgvState& s);
+// Sets the launch attributes of the kernels tgv_iterate_n may launch (before a
+// stream capture).
+void tgv_prepare_launches(const TgvState& s);
 // Whether the fused kernel of this state runs the TMA pipeline.
 bool tgv_uses_tma(const TgvState& s);
 

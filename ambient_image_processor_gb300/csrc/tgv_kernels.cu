@@ -1228,6 +1228,426 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     __syncthreads();
 }
 
+// ---- shifted pass: the primal step of iteration n, then the dual step of n + 1 --------
+//
+// Between two passes the loop keeps (u^n, v^n, p^(n+1), q^(n+1)): the duals run half an
+// iteration ahead of the primals.  One pass computes the primal step of iteration n
+// (u, ubar, v, vbar from u^n, v^n, f and the stencils of p^(n+1), q^(n+1)) and then the
+// dual step of iteration n + 1 (p^(n+2), q^(n+2) from the stencils of ubar^(n+1),
+// vbar^(n+1) and the own p^(n+1), q^(n+1)).  ubar and vbar never leave the chip, so a
+// voxel-iteration moves u, v, p, q, f in (14 floats) and u, v, p, q out (13): 108
+// bytes, against 140 for the pass that starts with the dual step.  Every update is the
+// same arithmetic in the same order as in the other kernels (bit-identical results).
+// A dual step (tgv_dual_kernel) before the first pass and a primal step
+// (tgv_primal_kernel) after the last convert the loop state to this form and back.
+//
+// A block owns a 32 x 8 column tile and marches along z through its planes.  Step t
+// computes the primal of plane t + 1, then the dual of plane t:
+//   256 tile threads   primal (u, ubar, v, vbar; u and v stored) and dual (p, q stored)
+//   40 rim threads     ubar only, on the +x column and the +y row the dual's forward
+//                      differences read
+//   40 rim threads     vbar only, on the -x column and the -y row its backward
+//                      differences read
+// ubar and vbar pass through a two-plane shared-memory ring: the dual of plane t reads
+// plane t's, written one step earlier; the own values of planes t - 1 .. t + 1 stay in
+// registers.  p and q of every plane arrive by TMA as 40 x 10 boxes (x0 - 4 .. x0 + 35,
+// y0 - 1 .. y0 + 8) into a ring of NS stages, completing on the stage's mbarrier; step t
+// reads planes t .. t + 2, so NS - 3 planes are in flight while it computes.  u, f and v
+// are loaded per thread two planes ahead, with an L2 prefetch one plane further.  The
+// block meets one barrier per plane.  Blocks whose every access lies inside the volume
+// (the tile and two voxels around it) run an instance without boundary tests.
+namespace shp {
+
+constexpr int TX = 32, TY = 8;
+constexpr int EXW = TX + 2, EYH = TY + 2, NE = EXW * EYH;  // tile and rim: 34 x 10
+constexpr int NTHREADS = 352;                              // 8 tile warps, 80 rim threads
+constexpr int PRODUCER = 256;                              // first rim thread issues TMA
+constexpr int XO = 4, BW = TX + 8, BH = TY + 2;            // boxes x0-4 .. x0+35, 10 rows
+constexpr int BOX = (BW * BH * 4 + 127) / 128 * 128;       // bytes per box in a stage
+constexpr int BOXF = BOX / 4;                              // floats per box
+constexpr int QOFF = 3 * BOXF;                             // first q box (floats)
+constexpr int STAGE = 9 * BOX;                             // p[3] | q[6] in slot order
+constexpr uint32_t TX_BYTES = 9u * BW * BH * 4;            // what expect_tx announces
+constexpr int RING = 2 * 4 * NE;                           // [plane & 1][ubar, vbar x3][NE]
+
+enum Role { IDLE = 0, TILE = 1, RIM_U = 2, RIM_V = 3 };
+
+struct alignas(64) Maps {
+    CUtensorMap p[3], q[6];  // q in kernel slot order: xx yy xy zz xz yz
+};
+
+struct Args {
+    Maps maps;
+    int W, H, D, zchunk;
+    size_t WH;
+    const float* f;
+    const float* u;  // u^n, v^n of the input
+    const float* v[3];
+    float* u_out;    // u^(n+1), v^(n+1), p^(n+2), q^(n+2) (distinct from the inputs)
+    float* v_out[3];
+    float* p_out[3];
+    float* q_out[6];  // state order: xx yy zz xy xz yz
+    float tau, sigma, theta, tau_lambda, alpha0, alpha1;
+    float thr_p, thr_q;  // squared-norm bounds below which the projections are skipped
+    int skip_bz;
+    int* err;
+    unsigned long long wait_ns;  // limit of the consumers' pipeline waits (0: one test)
+};
+
+template <int NS>
+constexpr size_t smem_bytes() {
+    return (size_t)NS * STAGE + (size_t)RING * 4 + 128;
+}
+
+}  // namespace shp
+
+template <int DATA, int NS, bool BF>
+__device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages, float* ring,
+                                             uint64_t* full) {
+    using namespace shp;
+    using tma::su32;
+    static_assert(NS >= 4, "step t reads three planes; one more must be in flight");
+    const int z0 = (int)blockIdx.z * a.zchunk, z1 = min(a.D, z0 + a.zchunk);
+    const int tid = threadIdx.x;
+    int ex = 0, ey = 0, role = IDLE;
+    if (tid < 256) {
+        ex = (tid & 31) + 1;
+        ey = (tid >> 5) + 1;
+        role = TILE;
+    } else {
+        const int h = tid - 256;
+        if (h < 32) { ex = h + 1; ey = 0; role = RIM_V; }                 // -y row
+        else if (h < 64) { ex = h - 31; ey = EYH - 1; role = RIM_U; }     // +y row
+        else if (h < 72) { ex = 0; ey = h - 63; role = RIM_V; }           // -x column
+        else if (h < 80) { ex = EXW - 1; ey = h - 71; role = RIM_U; }     // +x column
+    }
+    const int x0 = (int)blockIdx.x * TX, y0 = (int)blockIdx.y * TY;
+    const int x = x0 - 1 + ex, y = y0 - 1 + ey;
+    if (!BF && !(x >= 0 && x < a.W && y >= 0 && y < a.H)) role = IDLE;
+    const bool tile = role == TILE;
+    const bool need_u = tile || role == RIM_U, need_v = tile || role == RIM_V;
+    const bool xl = BF || x + 1 < a.W, yl = BF || y + 1 < a.H;
+    const bool xg = BF || x > 0, yg = BF || y > 0;
+    const int e = ey * EXW + ex;            // position in the ubar / vbar ring
+    const int ob = ey * BW + ex + XO - 1;   // position in the p and q boxes
+    const int D = a.D;
+    const int pbase = max(z0 - 1, 0);       // first plane of p, q this block loads
+    const int plast = min(D - 1, z1);       // last one
+    const int qlast = min(D - 1, z1);       // last plane of a primal step here
+    const size_t col = role != IDLE ? (size_t)y * a.W + x : 0;
+    if constexpr (kCheckBounds) {
+        // every index this thread's role uses: its column over the chunk, the staged
+        // boxes with the neighbours the primal reads, and the ring
+        constexpr int nB = BW * BH;
+        bool ok = true;
+        if (role != IDLE) {
+            ok = TGV_IN_BOUNDS(col, a.WH, 40) && ok;
+            ok = TGV_IN_BOUNDS((size_t)qlast * a.WH + col, a.WH * (size_t)D, 41) && ok;
+            ok = TGV_IN_BOUNDS(ob, nB, 42) && ok;
+            ok = TGV_IN_BOUNDS(e, NE, 43) && ok;
+        }
+        if (need_u) {
+            if (xg) ok = TGV_IN_BOUNDS(ob - 1, nB, 44) && ok;
+            if (yg) ok = TGV_IN_BOUNDS(ob - BW, nB, 45) && ok;
+        }
+        if (need_v) {
+            if (xl) ok = TGV_IN_BOUNDS(ob + 1, nB, 46) && ok;
+            if (yl) ok = TGV_IN_BOUNDS(ob + BW, nB, 47) && ok;
+        }
+        if (tile) {
+            if (xl) ok = TGV_IN_BOUNDS(e + 1, NE, 48) && ok;
+            if (yl) ok = TGV_IN_BOUNDS(e + EXW, NE, 49) && ok;
+            if (xg) ok = TGV_IN_BOUNDS(e - 1, NE, 50) && ok;
+            if (yg) ok = TGV_IN_BOUNDS(e - EXW, NE, 51) && ok;
+        }
+        if (__syncthreads_or(!ok)) return;
+    }
+    auto stage_at = [&](int plane) {
+        return (const float*)(stages + ((plane - pbase) % NS) * STAGE);
+    };
+    auto issue = [&](int plane) {  // producer thread only
+        if (plane < 0 || plane > plast) return;
+        const int slot = (plane - pbase) % NS;
+        uint8_t* st = stages + slot * STAGE;
+        uint64_t* bar = &full[slot];
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
+                     "r"(TX_BYTES)
+                     : "memory");
+        const int xb = x0 - XO, yb = y0 - 1;
+        for (int c = 0; c < 3; ++c) tma::tma_load(st + c * BOX, &a.maps.p[c], xb, yb, plane, bar);
+        for (int k = 0; k < 6; ++k)
+            tma::tma_load(st + (3 + k) * BOX, &a.maps.q[k], xb, yb, plane, bar);
+    };
+    bool ok = true;
+    int waited_upto = pbase - 1;  // every plane <= this one has landed
+    auto wait_plane = [&](int plane) {
+        if (plane < 0 || plane > plast || plane <= waited_upto) return;
+        const int j = (plane - pbase) / NS;
+        if (!tma::mwait(&full[(plane - pbase) % NS], j & 1, a.err, a.wait_ns)) ok = false;
+        else waited_upto = plane;
+    };
+
+    // u, f (ubar roles) and v (vbar roles) of the primal planes, a two-deep register
+    // queue: a plane's loads are issued two steps before its primal step
+    float tu = 0.f, tf = 0.f, tv0 = 0.f, tv1 = 0.f, tv2 = 0.f;
+    float nu = 0.f, nf = 0.f, nv0 = 0.f, nv1 = 0.f, nv2 = 0.f;
+    auto load = [&](int z, float& lu, float& lf, float& l0, float& l1, float& l2) {
+        if (role == IDLE || z > qlast) return;
+        const size_t i = (size_t)z * a.WH + col;
+        if (tile) {  // the last read of this voxel in this pass: evict first
+            lu = __ldcs(a.u + i);
+            lf = __ldcs(a.f + i);
+            l0 = __ldcs(a.v[0] + i);
+            l1 = __ldcs(a.v[1] + i);
+            l2 = __ldcs(a.v[2] + i);
+        } else if (need_u) {
+            lu = __ldg(a.u + i);
+            lf = __ldg(a.f + i);
+        } else {
+            l0 = __ldg(a.v[0] + i);
+            l1 = __ldg(a.v[1] + i);
+            l2 = __ldg(a.v[2] + i);
+        }
+    };
+    auto prefetch = [&](int z) {
+        if (role == IDLE || z > qlast) return;
+        const size_t i = (size_t)z * a.WH + col;
+        if (need_u) {
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.u + i));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.f + i));
+        }
+        if (need_v)
+            for (int c = 0; c < 3; ++c) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.v[c] + i));
+    };
+    const int qfirst = z0 > 0 ? z0 - 1 : z0;
+    int next_load = qfirst + 2;
+    auto pop = [&](float& pu, float& pf, float* vo) {
+        pu = tu;
+        pf = tf;
+        vo[0] = tv0;
+        vo[1] = tv1;
+        vo[2] = tv2;
+        tu = nu;
+        tf = nf;
+        tv0 = nv0;
+        tv1 = nv1;
+        tv2 = nv2;
+        load(next_load, nu, nf, nv0, nv1, nv2);
+        prefetch(next_load + 1);
+        ++next_load;
+    };
+
+    // ---- the primal step of this thread's role at plane z (stage S; Sn: plane z + 1,
+    // read when has_next).  pzm: p_z of plane z - 1 here (0 under the volume).  full:
+    // the plane is one of the block's (u and v stored); otherwise only the tile's own
+    // ubar is wanted (the dual of the block's last plane reads it).
+    float pzm = 0.f;
+    auto primal_at = [&](const float* S, const float* Sn, bool has_next, float* R, float pu,
+                         float pf, const float* vo, size_t i, bool full, float& ub_out,
+                         float* vb_out) {
+        const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+        if (need_u) {
+            // u <- prox(u - tau B.p), ubar                (tgv2_l1.cu:39-52)
+            const float bx = (xg ? S[ob - 1] : 0.f) - pv[0];
+            const float by = (yg ? S[BOXF + ob - BW] : 0.f) - pv[1];
+            float div = bx + by;
+            const float bz = pzm - pv[2];
+            if (!a.skip_bz) div = div + bz;
+            float uu = pu - a.tau * div;
+            if constexpr (DATA == TGVDCT_DATA_L1) {
+                const float umf = uu - pf;
+                if (umf > a.tau_lambda) uu = uu - a.tau_lambda;
+                else if (umf < -a.tau_lambda) uu = uu + a.tau_lambda;
+                else uu = pf;
+            } else {
+                uu = (uu + a.tau_lambda * pf) / (1.f + a.tau_lambda);
+            }
+            const float ub = uu + a.theta * (uu - pu);
+            ub_out = ub;
+            if (full) {
+                R[e] = ub;
+                if (tile) __stcs(a.u_out + i, uu);
+            }
+        }
+        if (need_v && full) {
+            // v <- v - tau (div q - p), vbar               (tgv2_common.cu:290-347)
+            const float* Q = S + QOFF;
+            const float* Qn = Sn + QOFF;
+            const float qxx = Q[ob], qyy = Q[BOXF + ob], qxy = Q[2 * BOXF + ob];
+            const float qzz = Q[3 * BOXF + ob], qxz = Q[4 * BOXF + ob], qyz = Q[5 * BOXF + ob];
+            float d[3];
+            d[0] = (xl ? Q[ob + 1] - qxx : 0.f) + (yl ? Q[2 * BOXF + ob + BW] - qxy : 0.f);
+            d[1] = (yl ? Q[BOXF + ob + BW] - qyy : 0.f) + (xl ? Q[2 * BOXF + ob + 1] - qxy : 0.f);
+            d[0] = d[0] + (has_next ? Qn[4 * BOXF + ob] - qxz : 0.f);
+            d[1] = d[1] + (has_next ? Qn[5 * BOXF + ob] - qyz : 0.f);
+            d[2] = ((has_next ? Qn[3 * BOXF + ob] - qzz : 0.f) +
+                    (xl ? Q[4 * BOXF + ob + 1] - qxz : 0.f)) +
+                   (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float vn = vo[c] - a.tau * (d[c] - pv[c]);
+                const float vb = vn + a.theta * (vn - vo[c]);
+                R[(1 + c) * NE + e] = vb;
+                vb_out[c] = vb;
+                if (tile) __stcs(a.v_out[c] + i, vn);
+            }
+        }
+        pzm = pv[2];
+    };
+    // ---- the dual step at plane t (stage S, ring slot R of plane t), tile threads:
+    // ubar own of planes t, t + 1 and vbar own of planes t - 1, t from registers, the
+    // neighbours from the ring
+    auto dual_at = [&](const float* S, const float* R, float ubc, float ubn, bool has_next,
+                       const float* vbc, const float* vbm, bool has_prev, size_t i) {
+        float g[3] = {xl ? R[e + 1] - ubc : 0.f, yl ? R[e + EXW] - ubc : 0.f,
+                      has_next ? ubn - ubc : 0.f};
+        float vb[3] = {vbc[0], vbc[1], vbc[2]};
+        float pp[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+        dual_p_update<true>(g, vb, pp, a.sigma, a.alpha1, a.thr_p);
+        float xm[3], ym[3], zm[3], q[6];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float* V = R + (1 + c) * NE;
+            xm[c] = xg ? V[e - 1] : 0.f;
+            ym[c] = yg ? V[e - EXW] : 0.f;
+            zm[c] = has_prev ? vbm[c] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = S[QOFF + k * BOXF + ob];
+        dual_q_update<true>(vb, xm, ym, zm, q, a.sigma, a.alpha0, a.thr_q);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) __stcs(a.p_out[c] + i, pp[c]);
+        __stcs(a.q_out[0] + i, q[0]);
+        __stcs(a.q_out[1] + i, q[1]);
+        __stcs(a.q_out[3] + i, q[2]);
+        __stcs(a.q_out[2] + i, q[3]);
+        __stcs(a.q_out[4] + i, q[4]);
+        __stcs(a.q_out[5] + i, q[5]);
+    };
+
+    if (tid == 0) {
+        for (int k = 0; k < NS; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[k])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == PRODUCER)
+        for (int k = 0; k < NS; ++k) issue(pbase + k);
+    int issued_upto = pbase + NS - 1;  // meaningful in the producer only
+    load(qfirst, tu, tf, tv0, tv1, tv2);
+    load(qfirst + 1, nu, nf, nv0, nv1, nv2);
+    prefetch(qfirst + 2);
+
+    // ---- prologue: vbar own at plane z0 - 1 (tile), the primal of plane z0 (all roles)
+    wait_plane(z0 - 1);
+    wait_plane(z0);
+    wait_plane(z0 + 1);
+    float ubc = 0.f, vbc[3] = {0.f, 0.f, 0.f}, vbm[3] = {0.f, 0.f, 0.f};
+    if (ok) {
+        float pu, pf, vo[3];
+        if (z0 > 0) {
+            pop(pu, pf, vo);  // plane z0 - 1
+            const float* S = stage_at(z0 - 1);
+            if (tile) {
+                const float* Q = S + QOFF;
+                const float* Qn = stage_at(z0) + QOFF;
+                const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+                const float qxx = Q[ob], qyy = Q[BOXF + ob], qxy = Q[2 * BOXF + ob];
+                const float qzz = Q[3 * BOXF + ob], qxz = Q[4 * BOXF + ob];
+                const float qyz = Q[5 * BOXF + ob];
+                float d[3];
+                d[0] = (xl ? Q[ob + 1] - qxx : 0.f) + (yl ? Q[2 * BOXF + ob + BW] - qxy : 0.f);
+                d[1] = (yl ? Q[BOXF + ob + BW] - qyy : 0.f) +
+                       (xl ? Q[2 * BOXF + ob + 1] - qxy : 0.f);
+                d[0] = d[0] + (Qn[4 * BOXF + ob] - qxz);
+                d[1] = d[1] + (Qn[5 * BOXF + ob] - qyz);
+                d[2] = ((Qn[3 * BOXF + ob] - qzz) + (xl ? Q[4 * BOXF + ob + 1] - qxz : 0.f)) +
+                       (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float vn = vo[c] - a.tau * (d[c] - pv[c]);
+                    vbm[c] = vn + a.theta * (vn - vo[c]);
+                }
+            }
+            if (role != IDLE) pzm = S[2 * BOXF + ob];
+        }
+        pop(pu, pf, vo);  // plane z0
+        const bool hn = z0 + 1 < D;
+        const float* S = stage_at(z0);
+        if (role != IDLE)
+            primal_at(S, hn ? stage_at(z0 + 1) : S, hn, ring + (z0 & 1) * 4 * NE, pu, pf, vo,
+                      (size_t)z0 * a.WH + col, true, ubc, vbc);
+    }
+    ok = __syncthreads_and(ok);
+    if (ok && tid == PRODUCER && z0 > 0) issue(++issued_upto);  // plane z0 - 1 is done
+
+    int s0 = (z0 - pbase) % NS;  // stage slot of plane t
+    for (int t = z0; t < z1 && ok; ++t) {
+        wait_plane(min(t + 2, plast));
+        const int s1 = s0 + 1 == NS ? 0 : s0 + 1;
+        const int s2 = s1 + 1 == NS ? 0 : s1 + 1;
+        const float* St = (const float*)(stages + s0 * STAGE);  // plane t
+        const float* S1 = (const float*)(stages + s1 * STAGE);  // plane t + 1
+        const float* S2 = (const float*)(stages + s2 * STAGE);  // plane t + 2
+        // A thread whose wait gave up skips the plane; the barrier below shares the
+        // outcome and the whole block leaves together.
+        if (ok) {
+            float ubn = 0.f, vbn[3] = {0.f, 0.f, 0.f};
+            const bool p1 = t + 1 < D;  // there is a plane t + 1
+            if (p1) {
+                float pu, pf, vo[3];
+                pop(pu, pf, vo);  // plane t + 1
+                const bool full = t + 1 < z1;
+                const bool hn = t + 2 < D;
+                if (role != IDLE && (full || tile))
+                    primal_at(S1, hn ? S2 : S1, hn, ring + ((t + 1) & 1) * 4 * NE, pu, pf, vo,
+                              (size_t)(t + 1) * a.WH + col, full, ubn, vbn);
+            }
+            if (tile)
+                dual_at(St, ring + (t & 1) * 4 * NE, ubc, ubn, p1, vbc, vbm, t > 0,
+                        (size_t)t * a.WH + col);
+            ubc = ubn;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vbm[c] = vbc[c];
+                vbc[c] = vbn[c];
+            }
+        }
+        // The block's one barrier per plane: the ring slot written above becomes
+        // readable, and the stage of plane t is no longer read.
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        if (tid == PRODUCER) issue(++issued_upto);  // plane t's slot takes t + NS
+        s0 = s1;
+    }
+    // On an error exit, let every load this block issued land before the block's
+    // shared memory goes away (bounded waits; the flag is already raised).
+    if (!ok && tid == PRODUCER) {
+        for (int pl = max(waited_upto + 1, 0); pl <= min(issued_upto, plast); ++pl) {
+            const int j = (pl - pbase) / NS;
+            tma::mwait(&full[(pl - pbase) % NS], j & 1, a.err, tma::WAIT_NS);
+        }
+    }
+    __syncthreads();
+}
+
+template <int DATA, int NS>
+__global__ void __launch_bounds__(shp::NTHREADS, 2)
+    tgv_shifted_tma_kernel(const __grid_constant__ shp::Args a) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+    __shared__ uint64_t full[NS];
+    // a pipeline wait of an earlier block or launch timed out: do nothing more
+    if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
+    float* ring = (float*)(smem + NS * shp::STAGE);
+    // every position the block touches (the tile, its rim and their neighbours) is
+    // inside the volume: the instance without boundary tests (one branch per block)
+    const int x0 = (int)blockIdx.x * shp::TX, y0 = (int)blockIdx.y * shp::TY;
+    const bool inside = x0 >= 2 && x0 + shp::TX + 2 <= a.W && y0 >= 2 && y0 + shp::TY + 2 <= a.H;
+    if (inside) shifted_pass<DATA, NS, true>(a, smem, ring, full);
+    else shifted_pass<DATA, NS, false>(a, smem, ring, full);
+}
+
 size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2; }
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -1360,7 +1780,7 @@ void encode_box(CUtensorMap* m, const void* base, int es, const TgvState& s, int
 // of 8 (16-bit dual fields).
 bool tma_shape_ok(const TgvState& s) {
     const int need = s.precision == TGVDCT_STATE_FP32 ? 4 : 8;
-    return s.W % need == 0 && s.kernel == TGV_KERNEL_FUSED;
+    return s.W % need == 0 && (s.kernel == TGV_KERNEL_FUSED || s.kernel == TGV_KERNEL_SHIFTED);
 }
 
 template <int PREC>
@@ -1534,6 +1954,146 @@ void iterate_fused(TgvState& s, const TgvStep& k, cudaStream_t st) {
     s.cur ^= 1;
 }
 
+// ---- the shifted passes: host side ----------------------------------------------------
+// Stages of p and q in flight: step t reads planes t .. t + 2, so SHIFTED_NS - 3 planes
+// land while it computes.
+constexpr int SHIFTED_NS = 5;
+
+bool shifted_ok(const TgvState& s) {
+    return s.kernel == TGV_KERNEL_SHIFTED && s.precision == TGVDCT_STATE_FP32 && s.three &&
+           s.D >= 2 && s.W % 4 == 0 && !s.domain && s.err;
+}
+
+// Where the shifted form (u^n, v^n, p^(n+1), q^(n+1)) of a run that started from stencil
+// set c lives after an even or odd number of passes.  Even: u, v in their own buffers,
+// p, q in set c ^ 1 (the dual step before the first pass writes there).  Odd: u, v in
+// set c's ubar and vbar (dead while the duals run ahead), p, q in set c.  A pass reads
+// one and writes the other, so no block overwrites what another still reads.
+struct ShiftedSlot {
+    float* u;
+    float* v[3];
+    float* p[3];
+    float* q[6];  // state order
+};
+
+ShiftedSlot shifted_slot(const TgvState& s, int c, int parity) {
+    ShiftedSlot r;
+    const TgvStencilFields& F = s.set[parity ? c : c ^ 1];
+    r.u = parity ? s.set[c].ubar : s.u;
+    for (int k = 0; k < 3; ++k) {
+        r.v[k] = parity ? s.set[c].vbar[k] : s.v[k];
+        r.p[k] = (float*)F.p[k];
+    }
+    for (int k = 0; k < 6; ++k) r.q[k] = (float*)F.q[k];
+    return r;
+}
+
+struct ShiftedCache {
+    shp::Args args[2][2];  // [c][parity of the input]: tensor maps and pointers of a pass
+};
+
+ShiftedCache* shifted_cache(TgvState& s) {
+    if (!s.shifted_cache) {
+        auto cache = std::make_shared<ShiftedCache>();
+        const int qmap[6] = {0, 1, 3, 2, 4, 5};  // kernel slot -> state order
+        for (int c = 0; c < 2; ++c)
+            for (int par = 0; par < 2; ++par) {
+                shp::Args& a = cache->args[c][par];
+                std::memset(&a, 0, sizeof(a));
+                const ShiftedSlot in = shifted_slot(s, c, par), out = shifted_slot(s, c, par ^ 1);
+                for (int k = 0; k < 3; ++k)
+                    encode_box(&a.maps.p[k], in.p[k], 4, s, shp::BW, shp::BH);
+                for (int k = 0; k < 6; ++k)
+                    encode_box(&a.maps.q[k], in.q[qmap[k]], 4, s, shp::BW, shp::BH);
+                a.W = s.W;
+                a.H = s.H;
+                a.D = s.D;
+                a.WH = (size_t)s.W * s.H;
+                a.f = s.f;
+                a.u = in.u;
+                a.u_out = out.u;
+                for (int k = 0; k < 3; ++k) {
+                    a.v[k] = in.v[k];
+                    a.v_out[k] = out.v[k];
+                    a.p_out[k] = out.p[k];
+                }
+                for (int k = 0; k < 6; ++k) a.q_out[k] = out.q[k];
+            }
+        s.shifted_cache = cache;
+    }
+    return (ShiftedCache*)s.shifted_cache.get();
+}
+
+// Raises the shared-memory limit of the shifted kernel on the current device, once.
+template <int DATA>
+void shifted_attr() {
+    static std::atomic<uint64_t> configured{0};  // per template instance
+    smem_attr_once((const void*)tgv_shifted_tma_kernel<DATA, SHIFTED_NS>,
+                   shp::smem_bytes<SHIFTED_NS>(), configured);
+}
+
+template <int DATA>
+void launch_shifted(const shp::Args& a, cudaStream_t st) {
+    constexpr int NS = SHIFTED_NS;
+    auto kern = tgv_shifted_tma_kernel<DATA, NS>;
+    constexpr size_t smem = shp::smem_bytes<NS>();
+    shifted_attr<DATA>();
+    const dim3 grid(ceil_div(a.W, shp::TX), ceil_div(a.H, shp::TY), ceil_div(a.D, a.zchunk));
+    kern<<<grid, shp::NTHREADS, smem, st>>>(a);
+    TGV_CHECK_LAUNCH();
+}
+
+// n >= 2 iterations from the standard state of set c = s.cur: the dual step of the
+// first, n - 1 shifted passes, the primal step of the last.  The standard state ends in
+// set c when n is even and in set c ^ 1 when n is odd (as after n single passes).
+// Returns the number of kernel launches.
+int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) {
+    constexpr int FP = TGVDCT_STATE_FP32;
+    const int c = s.cur;
+    ShiftedCache* cache = shifted_cache(s);
+    const dim3 block(BX, BY, 1);
+    const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
+    {   // p^(n+1), q^(n+1) of the current state into set c ^ 1
+        float* const v[3] = {s.v[0], s.v[1], s.v[2]};
+        const auto a = make_args<FP>(s, k, s.set[c], s.u, v, s.set[c ^ 1], s.u, v);
+        tgv_dual_kernel<FP, true><<<grid, block, 0, st>>>(a);
+        TGV_CHECK_LAUNCH();
+    }
+    for (uint32_t j = 0; j + 1 < n; ++j) {
+        shp::Args a = cache->args[c][j & 1];
+        a.zchunk = tma_zchunk(s);
+        a.tau = k.tau;
+        a.sigma = k.sigma;
+        a.theta = k.theta;
+        a.tau_lambda = k.tau * k.lambda;
+        a.alpha0 = k.alpha0;
+        a.alpha1 = k.alpha1;
+        a.thr_p = projection_skip_bound(k.alpha1);
+        a.thr_q = projection_skip_bound(k.alpha0);
+        a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
+        a.err = s.err;
+        a.wait_ns = s.wait_ns;
+        if (k.data_term == TGVDCT_DATA_L1) launch_shifted<TGVDCT_DATA_L1>(a, st);
+        else launch_shifted<TGVDCT_DATA_L2>(a, st);
+    }
+    {   // the primal step of the last iteration, into the standard state: u, v to their
+        // own buffers, ubar, vbar to the set that holds the last p, q
+        const int par = (int)((n - 1) & 1);
+        const ShiftedSlot d = shifted_slot(s, c, par);
+        const int set = par ? c : c ^ 1;
+        float* const v_in[3] = {d.v[0], d.v[1], d.v[2]};
+        float* const v_out[3] = {s.v[0], s.v[1], s.v[2]};
+        const auto a = make_args<FP>(s, k, s.set[set], d.u, v_in, s.set[set], s.u, v_out);
+        if (k.data_term == TGVDCT_DATA_L1)
+            tgv_primal_kernel<FP, true, TGVDCT_DATA_L1><<<grid, block, 0, st>>>(a);
+        else
+            tgv_primal_kernel<FP, true, TGVDCT_DATA_L2><<<grid, block, 0, st>>>(a);
+        TGV_CHECK_LAUNCH();
+        s.cur = set;
+    }
+    return (int)n + 1;
+}
+
 }  // namespace
 
 size_t tgv_state_bytes(int W, int H, int D, bool three, int precision, int kernel) {
@@ -1560,6 +2120,7 @@ void tgv_state_bind(TgvState& s, char* base) {
     for (int k = 0; k < 3; ++k) s.v[k] = k < ncomp ? (float*)take(f32) : nullptr;
     const int sets = s.kernel == TGV_KERNEL_TWO_PASS ? 1 : 2;
     s.tma_cache.reset();
+    s.shifted_cache.reset();
     // q order: xx yy zz xy xz yz; the 2-D launcher keeps xx yy xy
     const int order2[3] = {0, 1, 3};
     for (int t = 0; t < 2; ++t) {
@@ -1831,5 +2392,19 @@ void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st) {
 }
 
 int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL_TWO_PASS ? 2 : 1; }
+
+bool tgv_uses_shifted(const TgvState& s) { return shifted_ok(s); }
+
+int tgv_iterate_n(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) {
+    if (n >= 2 && shifted_ok(s)) return iterate_shifted(s, k, n, st);
+    for (uint32_t i = 0; i < n; ++i) tgv_iterate(s, k, st);
+    return (int)n * tgv_kernels_per_iteration(s);
+}
+
+void tgv_prepare_launches(const TgvState& s) {
+    if (!shifted_ok(s)) return;
+    shifted_attr<TGVDCT_DATA_L1>();
+    shifted_attr<TGVDCT_DATA_L2>();
+}
 
 }  // namespace tgvdct

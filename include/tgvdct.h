@@ -95,7 +95,14 @@ typedef enum tgvdct_iteration_kernel {
     /* the fused pass with the input planes staged through registers instead of
        the TMA pipeline (the fused kernel uses it by itself when the width is not a
        multiple of 4, or of 8 with 16-bit dual fields) */
-    TGVDCT_KERNEL_FUSED_REGISTER = 3
+    TGVDCT_KERNEL_FUSED_REGISTER = 3,
+    /* runs of iterations as shifted passes: each pass does the primal step of one
+       iteration and the dual step of the next, so ubar and vbar stay on chip and a
+       voxel-iteration moves 108 bytes (FP32 state, 3-D, depth >= 2, width a
+       multiple of 4, no mask); one dual step before a run and one primal step
+       after it (the two-pass kernels) convert the state.  Single iterations and the
+       cases it does not take run as TGVDCT_KERNEL_FUSED.  Same bits as the others. */
+    TGVDCT_KERNEL_FUSED_SHIFTED = 4
 } tgvdct_iteration_kernel;
 
 typedef enum tgvdct_poisson_eigen {
@@ -173,6 +180,9 @@ tgvdct_status tgvdct_set_params(tgvdct_context* ctx, const tgvdct_params* p);
 /* Number of iterations the last run completed (less than iteration_count when a
    callback stopped it). */
 uint32_t tgvdct_iterations_run(const tgvdct_context* ctx);
+/* Number of iteration kernels (fused or shifted passes and the two-pass kernels)
+   the last loop of the context launched, graph replays included. */
+uint64_t tgvdct_loop_launches(const tgvdct_context* ctx);
 
 /* ---- the TGV2 loop ------------------------------------------------------ */
 /* Replaces tgv2_l1_deshade_launch<float> (tgv_deshade/tgv2_l1_deshade.cu:33-41),

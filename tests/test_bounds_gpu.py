@@ -42,6 +42,9 @@ SHAPES = [
     ((1, 33, 47), {"geometry": pkg.GEOMETRY_2D}),                 # 2-D (two-pass)
     ((1, 40, 64), {"geometry": pkg.GEOMETRY_2D, "iteration_kernel": pkg.KERNEL_FUSED}),
     ((5, 8, 8), {}),
+    # shifted passes: edge blocks only, then blocks without boundary tests as well
+    ((13, 24, 32), {"iteration_kernel": pkg.KERNEL_FUSED_SHIFTED}),
+    ((6, 30, 100), {"iteration_kernel": pkg.KERNEL_FUSED_SHIFTED, "z_chunk": 2}),
 ]
 
 

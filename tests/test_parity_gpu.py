@@ -175,7 +175,8 @@ def test_bad_arguments_raise(gpu_lib):
 
 
 @pytest.mark.parametrize("prec", [pkg.STATE_FP32, pkg.STATE_FX16_DUAL, pkg.STATE_BF16_DUAL])
-@pytest.mark.parametrize("kernel", [pkg.KERNEL_FUSED, pkg.KERNEL_FUSED_REGISTER])
+@pytest.mark.parametrize("kernel", [pkg.KERNEL_FUSED, pkg.KERNEL_FUSED_REGISTER,
+                                    pkg.KERNEL_FUSED_SHIFTED])
 @pytest.mark.parametrize("shape,z_chunk,two_d,data_term", [
     ((37, 45, 72), 5, False, pkg.DATA_L1),   # width % 8 == 0: the TMA pipeline
     ((37, 45, 70), 5, False, pkg.DATA_L1),   # width % 4 != 0: register prefetch
