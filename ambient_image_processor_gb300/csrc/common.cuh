@@ -97,6 +97,18 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
+// The first A-byte boundary at or after the shared-memory pointer p, as a pointer
+// derived from p by pointer arithmetic.  The compiler then keeps the shared address
+// space and accesses through the result are LDS / STS with 32-bit addresses; rounding
+// through an integer (uintptr_t) loses it and turns every access into a generic load
+// or store with 64-bit address arithmetic.
+template <unsigned A, class T>
+__device__ __forceinline__ T* align_shared(T* p) {
+    static_assert((A & (A - 1)) == 0, "alignment must be a power of two");
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    return (T*)((uint8_t*)p + ((A - (a & (A - 1))) & (A - 1)));
+}
+
 // cudaFuncAttributeMaxDynamicSharedMemorySize is per device: raise it for `kern` once
 // on every device that launches it (`done` holds one bit per device ordinal).
 inline void smem_attr_once(const void* kern, size_t smem, std::atomic<uint64_t>& done) {

@@ -241,7 +241,7 @@ template <int MODE, bool DIV, int EPI>
 __global__ void __launch_bounds__(TC_THREADS, 1) dct_tc_kernel(TcArgs g) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte aligned staging area
-    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* base = align_shared<1024>(smem_raw);
     constexpr uint32_t SB = stage_bytes<MODE>();
     __shared__ uint64_t bar_free[2];
     __shared__ uint32_t tmem_base_s;

@@ -291,7 +291,7 @@ template <int MODE, int AXIS, int EPI>
 __global__ void __launch_bounds__(P_THREADS, 1) dct_pipe_kernel(const __grid_constant__ PArgs g) {
     using G = PGeo<MODE>;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* base = align_shared<1024>(smem_raw);
     constexpr int P_STAGES = G::NS;
     __shared__ uint64_t full[P_STAGES_MAX], conv[P_STAGES_MAX], empty[P_STAGES_MAX];
     __shared__ uint64_t acc_full[2], acc_empty[2];

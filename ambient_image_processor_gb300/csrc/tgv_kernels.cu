@@ -736,6 +736,19 @@ __device__ __forceinline__ bool mtest(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// One potentially blocking test: the thread is suspended until the phase completes
+// or a hardware time window ends, so a waiting warp neither spins nor oversleeps.
+__device__ __forceinline__ bool mtry(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 // Bounded wait; limit_ns == 0 gives up at the first test that finds the phase open.
 __device__ bool mwait(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_ns) {
     if (mtest(bar, parity)) return true;
@@ -746,13 +759,12 @@ __device__ bool mwait(uint64_t* bar, uint32_t parity, int* err, uint64_t limit_n
     uint64_t t0, t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
     while (true) {
-        if (mtest(bar, parity)) return true;
+        if (mtry(bar, parity)) return true;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
         if (t - t0 > limit_ns) {
             atomicExch(err, 1);
             return false;
         }
-        __nanosleep(32);
     }
 }
 __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int x, int y, int z,
@@ -835,7 +847,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     using T = typename S::T;
     constexpr int NC = THREE ? 3 : 2, NQ = THREE ? 6 : 3;
     extern __shared__ __align__(128) uint8_t smem_raw[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+    uint8_t* smem = align_shared<128>(smem_raw);
     uint8_t* stages = smem;                                  // NS x STAGE
     float* sP = (float*)(smem + NS * G::STAGE);              // [2][3][NE]
     float* sQ = sP + 2 * 3 * NE;                             // [3][6][NE]
@@ -888,7 +900,9 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     const int z0 = zr0, z1 = zr1;      // this block's planes
     const int pbase = max(z0 - 1, 0);  // first plane this block loads; slots count from it
     const int plast = min(D - 1, z1);  // last plane this block reads
-    const size_t col = in_dom ? (size_t)y * a.W + x : 0;
+    // 32-bit voxel indices: the host runs this kernel only on volumes of < 2^32 voxels
+    const uint32_t wh = (uint32_t)a.WH;
+    const uint32_t col = in_dom ? (uint32_t)y * (uint32_t)a.W + (uint32_t)x : 0u;
 
     const int of = ey * G::BW_F + ex + G::XO_F - 1;  // offset in FP32 stencil boxes
     const int odp = ey * G::BW_P + ex + G::XO_P - 1;  // offset in p boxes (R_p only)
@@ -976,7 +990,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     // ubar(z) own/+x/+y, ubar(z+1) own, vbar(z) own, p(z)
     // a voxel outside the masked deshade's domain keeps p = q = 0 and u, v unchanged
     auto live = [&](int plane) {
-        if constexpr (MASKED) return a.dom[(size_t)plane * a.WH + col] != 0;
+        if constexpr (MASKED) return a.dom[(uint32_t)plane * wh + col] != 0;
         else return true;
     };
     auto dual_p_at = [&](const uint8_t* sz, const uint8_t* sn, bool lv) {
@@ -1023,7 +1037,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     float nu = 0.f, nf = 0.f, nv[3] = {0.f, 0.f, 0.f};
     auto load_tile = [&](int z) {  // into the second slot
         if (interior && z < z1) {
-            const size_t i = (size_t)z * a.WH + col;
+            const uint32_t i = (uint32_t)z * wh + col;
             nu = __ldcs(a.u + i);  // read once per iteration: evict-first
             nf = __ldcs(a.f + i);
             for (int c = 0; c < NC; ++c) nv[c] = __ldcs(a.v[c] + i);
@@ -1037,7 +1051,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
     // and a plane further ahead into L2 (no register waits on a prefetch)
     auto prefetch_tile = [&](int z) {
         if (interior && z < z1) {
-            const size_t i = (size_t)z * a.WH + col;
+            const uint32_t i = (uint32_t)z * wh + col;
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a.u + i));
             asm volatile("prefetch.global.L2 [%0];" ::"l"(a.f + i));
             for (int c = 0; c < NC; ++c) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.v[c] + i));
@@ -1135,7 +1149,7 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
         if (in_rq && q_next) dual_q_at(S2, S1, Qnn, lq2);
         // ---- primal at (x, y, t)
         if (interior) {
-            const size_t i = (size_t)t * a.WH + col;
+            const uint32_t i = (uint32_t)t * wh + col;
             float pv[3] = {Pt[e], Pt[NE + e], THREE ? Pt[2 * NE + e] : 0.f};
             const float bx = (x > 0 ? Pt[e - 1] : 0.f) - pv[0];
             const float by = (y > 0 ? Pt[NE + e - EXW] : 0.f) - pv[1];
@@ -1253,9 +1267,9 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
 // registers.  p and q of every plane arrive by TMA as 40 x 10 boxes (x0 - 4 .. x0 + 35,
 // y0 - 1 .. y0 + 8) into a ring of NS stages, completing on the stage's mbarrier; step t
 // reads planes t .. t + 2, so NS - 3 planes are in flight while it computes.  u, f and v
-// are loaded per thread two planes ahead, with an L2 prefetch one plane further.  The
-// block meets one barrier per plane.  Blocks whose every access lies inside the volume
-// (the tile and two voxels around it) run an instance without boundary tests.
+// arrive the same way into a ring of NU stages of their own (step t reads plane t + 1,
+// so NU - 1 planes are in flight); no thread loads from global memory.  The block meets
+// one barrier per plane.
 namespace shp {
 
 constexpr int TX = 32, TY = 8;
@@ -1269,11 +1283,15 @@ constexpr int QOFF = 3 * BOXF;                             // first q box (float
 constexpr int STAGE = 9 * BOX;                             // p[3] | q[6] in slot order
 constexpr uint32_t TX_BYTES = 9u * BW * BH * 4;            // what expect_tx announces
 constexpr int RING = 2 * 4 * NE;                           // [plane & 1][ubar, vbar x3][NE]
+constexpr int NU = 3;                                      // stages of u, f, v
+constexpr int USTAGE = 5 * BOX;                            // u | f | v[3], same boxes
+constexpr uint32_t UTX_BYTES = 5u * BW * BH * 4;
 
 enum Role { IDLE = 0, TILE = 1, RIM_U = 2, RIM_V = 3 };
 
 struct alignas(64) Maps {
     CUtensorMap p[3], q[6];  // q in kernel slot order: xx yy xy zz xz yz
+    CUtensorMap uf[5];       // u, f, v_x, v_y, v_z
 };
 
 struct Args {
@@ -1296,14 +1314,15 @@ struct Args {
 
 template <int NS>
 constexpr size_t smem_bytes() {
-    return (size_t)NS * STAGE + (size_t)RING * 4 + 128;
+    return (size_t)NS * STAGE + (size_t)NU * USTAGE + (size_t)RING * 4 + 128;
 }
 
 }  // namespace shp
 
-template <int DATA, int NS, bool BF>
-__device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages, float* ring,
-                                             uint64_t* full) {
+template <int DATA, int NS>
+__device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages,
+                                             uint8_t* ustages, float* ring, uint64_t* full,
+                                             uint64_t* ufull) {
     using namespace shp;
     using tma::su32;
     static_assert(NS >= 4, "step t reads three planes; one more must be in flight");
@@ -1323,18 +1342,20 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     }
     const int x0 = (int)blockIdx.x * TX, y0 = (int)blockIdx.y * TY;
     const int x = x0 - 1 + ex, y = y0 - 1 + ey;
-    if (!BF && !(x >= 0 && x < a.W && y >= 0 && y < a.H)) role = IDLE;
+    if (!(x >= 0 && x < a.W && y >= 0 && y < a.H)) role = IDLE;
     const bool tile = role == TILE;
     const bool need_u = tile || role == RIM_U, need_v = tile || role == RIM_V;
-    const bool xl = BF || x + 1 < a.W, yl = BF || y + 1 < a.H;
-    const bool xg = BF || x > 0, yg = BF || y > 0;
+    const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
+    const bool xg = x > 0, yg = y > 0;
     const int e = ey * EXW + ex;            // position in the ubar / vbar ring
     const int ob = ey * BW + ex + XO - 1;   // position in the p and q boxes
     const int D = a.D;
     const int pbase = max(z0 - 1, 0);       // first plane of p, q this block loads
     const int plast = min(D - 1, z1);       // last one
     const int qlast = min(D - 1, z1);       // last plane of a primal step here
-    const size_t col = role != IDLE ? (size_t)y * a.W + x : 0;
+    // 32-bit voxel indices: the host runs this kernel only on volumes of < 2^32 voxels
+    const uint32_t wh = (uint32_t)a.WH;
+    const uint32_t col = role != IDLE ? (uint32_t)y * (uint32_t)a.W + (uint32_t)x : 0u;
     if constexpr (kCheckBounds) {
         // every index this thread's role uses: its column over the chunk, the staged
         // boxes with the neighbours the primal reads, and the ring
@@ -1387,54 +1408,28 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         else waited_upto = plane;
     };
 
-    // u, f (ubar roles) and v (vbar roles) of the primal planes, a two-deep register
-    // queue: a plane's loads are issued two steps before its primal step
-    float tu = 0.f, tf = 0.f, tv0 = 0.f, tv1 = 0.f, tv2 = 0.f;
-    float nu = 0.f, nf = 0.f, nv0 = 0.f, nv1 = 0.f, nv2 = 0.f;
-    auto load = [&](int z, float& lu, float& lf, float& l0, float& l1, float& l2) {
-        if (role == IDLE || z > qlast) return;
-        const size_t i = (size_t)z * a.WH + col;
-        if (tile) {  // the last read of this voxel in this pass: evict first
-            lu = __ldcs(a.u + i);
-            lf = __ldcs(a.f + i);
-            l0 = __ldcs(a.v[0] + i);
-            l1 = __ldcs(a.v[1] + i);
-            l2 = __ldcs(a.v[2] + i);
-        } else if (need_u) {
-            lu = __ldg(a.u + i);
-            lf = __ldg(a.f + i);
-        } else {
-            l0 = __ldg(a.v[0] + i);
-            l1 = __ldg(a.v[1] + i);
-            l2 = __ldg(a.v[2] + i);
-        }
-    };
-    auto prefetch = [&](int z) {
-        if (role == IDLE || z > qlast) return;
-        const size_t i = (size_t)z * a.WH + col;
-        if (need_u) {
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.u + i));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.f + i));
-        }
-        if (need_v)
-            for (int c = 0; c < 3; ++c) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.v[c] + i));
-    };
+    // u, f, v of the primal planes qfirst .. qlast: a ring of NU stages of their own
     const int qfirst = z0 > 0 ? z0 - 1 : z0;
-    int next_load = qfirst + 2;
-    auto pop = [&](float& pu, float& pf, float* vo) {
-        pu = tu;
-        pf = tf;
-        vo[0] = tv0;
-        vo[1] = tv1;
-        vo[2] = tv2;
-        tu = nu;
-        tf = nf;
-        tv0 = nv0;
-        tv1 = nv1;
-        tv2 = nv2;
-        load(next_load, nu, nf, nv0, nv1, nv2);
-        prefetch(next_load + 1);
-        ++next_load;
+    auto issue_u = [&](int plane) {  // producer thread only
+        if (plane < qfirst || plane > qlast) return;
+        const int slot = (plane - qfirst) % NU;
+        uint8_t* st = ustages + slot * USTAGE;
+        uint64_t* bar = &ufull[slot];
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
+                     "r"(UTX_BYTES)
+                     : "memory");
+        for (int k = 0; k < 5; ++k)
+            tma::tma_load(st + k * BOX, &a.maps.uf[k], x0 - XO, y0 - 1, plane, bar);
+    };
+    int uwaited_upto = qfirst - 1;
+    auto wait_u = [&](int plane) {
+        if (plane < qfirst || plane > qlast || plane <= uwaited_upto) return;
+        const int j = (plane - qfirst) / NU;
+        if (!tma::mwait(&ufull[(plane - qfirst) % NU], j & 1, a.err, a.wait_ns)) ok = false;
+        else uwaited_upto = plane;
+    };
+    auto ustage_at = [&](int plane) {
+        return (const float*)(ustages + ((plane - qfirst) % NU) * USTAGE);
     };
 
     // ---- the primal step of this thread's role at plane z (stage S; Sn: plane z + 1,
@@ -1442,12 +1437,13 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // the plane is one of the block's (u and v stored); otherwise only the tile's own
     // ubar is wanted (the dual of the block's last plane reads it).
     float pzm = 0.f;
-    auto primal_at = [&](const float* S, const float* Sn, bool has_next, float* R, float pu,
-                         float pf, const float* vo, size_t i, bool full, float& ub_out,
+    auto primal_at = [&](const float* S, const float* Sn, bool has_next, float* R,
+                         const float* Us, uint32_t i, bool full, float& ub_out,
                          float* vb_out) {
         const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
         if (need_u) {
             // u <- prox(u - tau B.p), ubar                (tgv2_l1.cu:39-52)
+            const float pu = Us[ob], pf = Us[BOXF + ob];
             const float bx = (xg ? S[ob - 1] : 0.f) - pv[0];
             const float by = (yg ? S[BOXF + ob - BW] : 0.f) - pv[1];
             float div = bx + by;
@@ -1485,8 +1481,9 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
                    (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float vn = vo[c] - a.tau * (d[c] - pv[c]);
-                const float vb = vn + a.theta * (vn - vo[c]);
+                const float vo = Us[(2 + c) * BOXF + ob];
+                const float vn = vo - a.tau * (d[c] - pv[c]);
+                const float vb = vn + a.theta * (vn - vo);
                 R[(1 + c) * NE + e] = vb;
                 vb_out[c] = vb;
                 if (tile) __stcs(a.v_out[c] + i, vn);
@@ -1498,7 +1495,7 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // ubar own of planes t, t + 1 and vbar own of planes t - 1, t from registers, the
     // neighbours from the ring
     auto dual_at = [&](const float* S, const float* R, float ubc, float ubn, bool has_next,
-                       const float* vbc, const float* vbm, bool has_prev, size_t i) {
+                       const float* vbc, const float* vbm, bool has_prev, uint32_t i) {
         float g[3] = {xl ? R[e + 1] - ubc : 0.f, yl ? R[e + EXW] - ubc : 0.f,
                       has_next ? ubn - ubc : 0.f};
         float vb[3] = {vbc[0], vbc[1], vbc[2]};
@@ -1528,27 +1525,30 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     if (tid == 0) {
         for (int k = 0; k < NS; ++k)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[k])) : "memory");
+        for (int k = 0; k < NU; ++k)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&ufull[k])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == PRODUCER)
+    if (tid == PRODUCER) {
         for (int k = 0; k < NS; ++k) issue(pbase + k);
-    int issued_upto = pbase + NS - 1;  // meaningful in the producer only
-    load(qfirst, tu, tf, tv0, tv1, tv2);
-    load(qfirst + 1, nu, nf, nv0, nv1, nv2);
-    prefetch(qfirst + 2);
+        for (int k = 0; k < NU; ++k) issue_u(qfirst + k);
+    }
+    int issued_upto = pbase + NS - 1;    // meaningful in the producer only
+    int uissued_upto = qfirst + NU - 1;  // likewise
 
     // ---- prologue: vbar own at plane z0 - 1 (tile), the primal of plane z0 (all roles)
     wait_plane(z0 - 1);
     wait_plane(z0);
     wait_plane(z0 + 1);
+    wait_u(z0 - 1);
+    wait_u(z0);
     float ubc = 0.f, vbc[3] = {0.f, 0.f, 0.f}, vbm[3] = {0.f, 0.f, 0.f};
     if (ok) {
-        float pu, pf, vo[3];
         if (z0 > 0) {
-            pop(pu, pf, vo);  // plane z0 - 1
             const float* S = stage_at(z0 - 1);
             if (tile) {
+                const float* Us = ustage_at(z0 - 1);
                 const float* Q = S + QOFF;
                 const float* Qn = stage_at(z0) + QOFF;
                 const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
@@ -1565,25 +1565,33 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
                        (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float vn = vo[c] - a.tau * (d[c] - pv[c]);
-                    vbm[c] = vn + a.theta * (vn - vo[c]);
+                    const float vo = Us[(2 + c) * BOXF + ob];
+                    const float vn = vo - a.tau * (d[c] - pv[c]);
+                    vbm[c] = vn + a.theta * (vn - vo);
                 }
             }
             if (role != IDLE) pzm = S[2 * BOXF + ob];
         }
-        pop(pu, pf, vo);  // plane z0
         const bool hn = z0 + 1 < D;
         const float* S = stage_at(z0);
         if (role != IDLE)
-            primal_at(S, hn ? stage_at(z0 + 1) : S, hn, ring + (z0 & 1) * 4 * NE, pu, pf, vo,
-                      (size_t)z0 * a.WH + col, true, ubc, vbc);
+            primal_at(S, hn ? stage_at(z0 + 1) : S, hn, ring + (z0 & 1) * 4 * NE, ustage_at(z0),
+                      (uint32_t)z0 * wh + col, true, ubc, vbc);
     }
     ok = __syncthreads_and(ok);
-    if (ok && tid == PRODUCER && z0 > 0) issue(++issued_upto);  // plane z0 - 1 is done
+    if (ok && tid == PRODUCER) {  // planes z0 - 1 (if any) and z0 are done
+        if (z0 > 0) {
+            issue(++issued_upto);
+            issue_u(++uissued_upto);
+        }
+        issue_u(++uissued_upto);
+    }
 
-    int s0 = (z0 - pbase) % NS;  // stage slot of plane t
+    int s0 = (z0 - pbase) % NS;        // stage slot of plane t
+    int us = (z0 + 1 - qfirst) % NU;   // u stage slot of plane t + 1
     for (int t = z0; t < z1 && ok; ++t) {
         wait_plane(min(t + 2, plast));
+        wait_u(t + 1);
         const int s1 = s0 + 1 == NS ? 0 : s0 + 1;
         const int s2 = s1 + 1 == NS ? 0 : s1 + 1;
         const float* St = (const float*)(stages + s0 * STAGE);  // plane t
@@ -1595,17 +1603,16 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
             float ubn = 0.f, vbn[3] = {0.f, 0.f, 0.f};
             const bool p1 = t + 1 < D;  // there is a plane t + 1
             if (p1) {
-                float pu, pf, vo[3];
-                pop(pu, pf, vo);  // plane t + 1
                 const bool full = t + 1 < z1;
                 const bool hn = t + 2 < D;
                 if (role != IDLE && (full || tile))
-                    primal_at(S1, hn ? S2 : S1, hn, ring + ((t + 1) & 1) * 4 * NE, pu, pf, vo,
-                              (size_t)(t + 1) * a.WH + col, full, ubn, vbn);
+                    primal_at(S1, hn ? S2 : S1, hn, ring + ((t + 1) & 1) * 4 * NE,
+                              (const float*)(ustages + us * USTAGE),
+                              (uint32_t)(t + 1) * wh + col, full, ubn, vbn);
             }
             if (tile)
                 dual_at(St, ring + (t & 1) * 4 * NE, ubc, ubn, p1, vbc, vbm, t > 0,
-                        (size_t)t * a.WH + col);
+                        (uint32_t)t * wh + col);
             ubc = ubn;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -1617,8 +1624,12 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         // readable, and the stage of plane t is no longer read.
         ok = __syncthreads_and(ok);
         if (!ok) break;
-        if (tid == PRODUCER) issue(++issued_upto);  // plane t's slot takes t + NS
+        if (tid == PRODUCER) {
+            issue(++issued_upto);                  // plane t's slot takes t + NS
+            if (t + 1 < D) issue_u(++uissued_upto);  // plane t + 1's, t + 1 + NU
+        }
         s0 = s1;
+        us = us + 1 == NU ? 0 : us + 1;
     }
     // On an error exit, let every load this block issued land before the block's
     // shared memory goes away (bounded waits; the flag is already raised).
@@ -1626,6 +1637,10 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         for (int pl = max(waited_upto + 1, 0); pl <= min(issued_upto, plast); ++pl) {
             const int j = (pl - pbase) / NS;
             tma::mwait(&full[(pl - pbase) % NS], j & 1, a.err, tma::WAIT_NS);
+        }
+        for (int pl = uwaited_upto + 1; pl <= min(uissued_upto, qlast); ++pl) {
+            const int j = (pl - qfirst) / NU;
+            tma::mwait(&ufull[(pl - qfirst) % NU], j & 1, a.err, tma::WAIT_NS);
         }
     }
     __syncthreads();
@@ -1635,17 +1650,13 @@ template <int DATA, int NS>
 __global__ void __launch_bounds__(shp::NTHREADS, 2)
     tgv_shifted_tma_kernel(const __grid_constant__ shp::Args a) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
-    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
-    __shared__ uint64_t full[NS];
+    uint8_t* smem = align_shared<128>(smem_raw);
+    __shared__ uint64_t full[NS + shp::NU];
     // a pipeline wait of an earlier block or launch timed out: do nothing more
     if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
-    float* ring = (float*)(smem + NS * shp::STAGE);
-    // every position the block touches (the tile, its rim and their neighbours) is
-    // inside the volume: the instance without boundary tests (one branch per block)
-    const int x0 = (int)blockIdx.x * shp::TX, y0 = (int)blockIdx.y * shp::TY;
-    const bool inside = x0 >= 2 && x0 + shp::TX + 2 <= a.W && y0 >= 2 && y0 + shp::TY + 2 <= a.H;
-    if (inside) shifted_pass<DATA, NS, true>(a, smem, ring, full);
-    else shifted_pass<DATA, NS, false>(a, smem, ring, full);
+    uint8_t* ustages = smem + NS * shp::STAGE;
+    float* ring = (float*)(ustages + shp::NU * shp::USTAGE);
+    shifted_pass<DATA, NS>(a, smem, ustages, ring, full, full + NS);
 }
 
 size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2; }
@@ -1780,7 +1791,9 @@ void encode_box(CUtensorMap* m, const void* base, int es, const TgvState& s, int
 // of 8 (16-bit dual fields).
 bool tma_shape_ok(const TgvState& s) {
     const int need = s.precision == TGVDCT_STATE_FP32 ? 4 : 8;
-    return s.W % need == 0 && (s.kernel == TGV_KERNEL_FUSED || s.kernel == TGV_KERNEL_SHIFTED);
+    // (and 32-bit voxel indices)
+    return s.W % need == 0 && (s.kernel == TGV_KERNEL_FUSED || s.kernel == TGV_KERNEL_SHIFTED) &&
+           (uint64_t)s.W * s.H * s.D < (1ull << 32);
 }
 
 template <int PREC>
@@ -1961,7 +1974,8 @@ constexpr int SHIFTED_NS = 5;
 
 bool shifted_ok(const TgvState& s) {
     return s.kernel == TGV_KERNEL_SHIFTED && s.precision == TGVDCT_STATE_FP32 && s.three &&
-           s.D >= 2 && s.W % 4 == 0 && !s.domain && s.err;
+           s.D >= 2 && s.W % 4 == 0 && !s.domain && s.err &&
+           (uint64_t)s.W * s.H * s.D < (1ull << 32);  // 32-bit voxel indices
 }
 
 // Where the shifted form (u^n, v^n, p^(n+1), q^(n+1)) of a run that started from stencil
@@ -2005,6 +2019,8 @@ ShiftedCache* shifted_cache(TgvState& s) {
                     encode_box(&a.maps.p[k], in.p[k], 4, s, shp::BW, shp::BH);
                 for (int k = 0; k < 6; ++k)
                     encode_box(&a.maps.q[k], in.q[qmap[k]], 4, s, shp::BW, shp::BH);
+                const float* uf[5] = {in.u, s.f, in.v[0], in.v[1], in.v[2]};
+                for (int k = 0; k < 5; ++k) encode_box(&a.maps.uf[k], uf[k], 4, s, shp::BW, shp::BH);
                 a.W = s.W;
                 a.H = s.H;
                 a.D = s.D;

@@ -42,7 +42,18 @@ WORKLOADS = {
 # algorithmic bytes per voxel-iteration of one TGV2 iteration (read f, u, ubar, v3,
 # vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
 ALGO_BYTES = {0: 140, 1: 104, 2: 104}
-KERNELS = {"fused": 2, "two_pass": 1}
+# the shifted pass (primal of one iteration, dual of the next) keeps ubar and vbar on
+# chip: read f, u, v3, p3, q6, write u, v3, p3, q6 (FP32 state only)
+ALGO_BYTES_SHIFTED = 108
+KERNELS = {"shifted": 4, "fused": 2, "two_pass": 1}
+# the kernel a roofline line times, per --kernel
+KERNEL_NAMES = {"shifted": "tgv_shifted_tma_kernel", "fused": "tgv_fused_tma_kernel",
+                "two_pass": "tgv_dual_kernel + tgv_primal_kernel"}
+
+
+def algo_bytes(kernel, precision):
+    """Algorithmic bytes per voxel-iteration of the iteration kernel that runs."""
+    return ALGO_BYTES_SHIFTED if (kernel, precision) == ("shifted", 0) else ALGO_BYTES[precision]
 # the extra measurements a default run adds to its line, in the order they run
 EXTRAS = ["iteration_variants", "dct_poisson_256cube", "adjoint", "adjoint_256x256x192",
           "other_configs", "downsampled_deshade", "masked_deshade", "accuracy_vs_fp64"]
@@ -192,10 +203,37 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------------------------
-# DRAM bytes (read + write) of one launch of the fused TMA kernel on this workload,
-# FP32 state: dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full
-# capture of that launch (its summary is under profiles/).
-TRAFFIC_FUSED_FP32_256x256x192 = 914891776 + 801782528
+# DRAM bytes (read + write) of one launch of the iteration kernel on this workload,
+# FP32 state: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of that
+# launch (the summaries are under profiles/).
+TRAFFIC_256x256x192 = {("fused", 0): 914891776 + 801782528,
+                       ("shifted", 0): 715630000 + 606720000}
+
+
+def time_shifted_pass(pkg, torch, w, h, d, f, stream, n_pass=100):
+    """Milliseconds per launch of the shifted pass: tgvdct_tgv2_step_dev runs n iterations
+    as one dual step, n - 1 shifted passes and one primal step, so the difference of
+    runs of n_pass + 2 and 2 iterations is n_pass launches of the pass alone (CUDA events
+    on `stream`)."""
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=1,
+                             iteration_kernel=KERNELS["shifted"])
+    L = pkg.lib()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    with pkg.Context(prm) as ctx:
+        def run(n):
+            assert L.tgvdct_state_init_dev(ctx._ctx, ctypes.c_void_p(f.data_ptr()), sh) == pkg.OK
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert L.tgvdct_tgv2_step_dev(ctx._ctx, n, sh) == pkg.OK
+            e1.record(stream)
+            torch.cuda.synchronize()
+            assert ctx.loop_launches() == n + 1
+            return e0.elapsed_time(e1)
+        run(n_pass + 2)  # warm-up
+        t_long = min(run(n_pass + 2) for _ in range(2))
+        t_short = min(run(2) for _ in range(3))
+        ctx.check_device_error(stream.cuda_stream)
+    return (t_long - t_short) / n_pass
 
 
 def time_iterations(pkg, torch, w, h, d, f, kernel, precision, n_it, stream):
@@ -466,18 +504,23 @@ def run_ours(args):
     ctx.check_device_error(sh)
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, dev)
     value = replica_throughput(V * iters, world, ms)
+    loop_launches = ctx.loop_launches()  # iteration kernels of one deshade (the last step)
     ctx.close()
 
     # ---- roofline of the iteration kernel, timed alone on its stream
     it_ms = time_iterations(pkg, torch, w, h, d, f, args.kernel, args.precision,
                             args.profile_iterations, stream)
-    launches_per_it = 1 if args.kernel == "fused" else 2
+    launches_per_it = 2 if args.kernel == "two_pass" else 1
+    launch_ms = it_ms / launches_per_it
+    shifted = (args.kernel, args.precision) == ("shifted", 0)
+    if shifted:  # the pass itself, without the dual and primal steps around each run
+        launch_ms = time_shifted_pass(pkg, torch, w, h, d, f, stream)
     peak, peak_kind = hbm_peak()
-    algo = ALGO_BYTES[args.precision]
-    achieved = algo * V / (it_ms * 1e-3) / 1e9  # algorithmic bytes of one iteration per second
-    traffic = (TRAFFIC_FUSED_FP32_256x256x192
-               if (args.kernel, args.precision, args.workload) == ("fused", 0, "deshade_256x256x192")
-               else None)
+    algo = algo_bytes(args.kernel, args.precision)
+    # algorithmic bytes of one iteration per second of the dominant kernel
+    achieved = algo * V / (launch_ms * launches_per_it * 1e-3) / 1e9
+    traffic = TRAFFIC_256x256x192.get((args.kernel, args.precision)) \
+        if args.workload == "deshade_256x256x192" else None
 
     # ---- e2e through the host-buffer C-ABI call (reference-facing)
     e2e_ms, e2e_calls = None, []
@@ -510,12 +553,12 @@ def run_ours(args):
         if not args.no_variants:
             if "iteration_variants" in want:
                 var = {}
-                for kernel, prec in (("two_pass", 0), ("fused", 0), ("two_pass", 2),
-                                     ("fused", 2), ("fused", 1)):
-                    t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 40, stream)
+                for kernel, prec in (("two_pass", 0), ("fused", 0), ("shifted", 0),
+                                     ("two_pass", 2), ("fused", 2), ("fused", 1)):
+                    t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 200, stream)
                     var[f"{kernel}_{PREC_NAMES[prec]}"] = {
                         "ms_per_iteration": t, "voxel_iters_per_s": V / (t * 1e-3),
-                        "algorithmic_gbs": ALGO_BYTES[prec] * V / (t * 1e-3) / 1e9}
+                        "algorithmic_gbs": algo_bytes(kernel, prec) * V / (t * 1e-3) / 1e9}
                 extra["iteration_variants"] = var
             if "dct_poisson_256cube" in want:
                 extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
@@ -542,7 +585,7 @@ def run_ours(args):
         # the loop; the six DCT contractions (the tensor-core passes take the divergence
         # as a kernel of its own); the epilogue; the log of f and the exp of u, l, r
         dct_launches = 6 if args.dct == "fp32" else 7
-        gpu_launches = iters * launches_per_it + dct_launches + 1 + 4
+        gpu_launches = loop_launches + dct_launches + 1 + 4
         line = {
             "metric": "voxel_iters_per_s", "value": value, "unit": "voxel-iter/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -564,10 +607,10 @@ def run_ours(args):
             "gpu_launches": gpu_launches * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": ("tgv_fused_tma_kernel" if args.kernel == "fused"
-                                    else "tgv_dual_kernel + tgv_primal_kernel"),
+                         "kernel": KERNEL_NAMES[args.kernel],
                          "algorithmic_bytes_per_launch": algo * V / launches_per_it,
-                         "launch_ms": it_ms / launches_per_it,
+                         "launch_ms": launch_ms,
+                         "loop_ms_per_iteration": it_ms,
                          "peak_source": peak_kind},
             "cpu_baseline": cpu,
         }
@@ -661,7 +704,7 @@ def main():
     # shading field, against 7.2e-6 for the reference's float formula
     ap.add_argument("--eigen", type=int, default=1, choices=[0, 1])
     ap.add_argument("--dct", default="bf16x3", choices=sorted(DCT_MODES))
-    ap.add_argument("--kernel", default="fused", choices=sorted(KERNELS))
+    ap.add_argument("--kernel", default="shifted", choices=sorted(KERNELS))
     ap.add_argument("--z-chunk", type=int, default=0)
     ap.add_argument("--iterations", type=int, default=0, help="override the iteration count")
     ap.add_argument("--profile-iterations", type=int, default=200)

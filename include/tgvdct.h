@@ -83,8 +83,8 @@ typedef enum tgvdct_dct_mode {
 } tgvdct_dct_mode;
 
 typedef enum tgvdct_iteration_kernel {
-    TGVDCT_KERNEL_AUTO = 0,     /* the fused single pass for volumes, the two-pass
-                                   kernels for a single plane (depth 1) */
+    TGVDCT_KERNEL_AUTO = 0,     /* shifted passes for volumes, the two-pass kernels
+                                   for a single plane (depth 1) */
     /* two coalesced passes per iteration (dual, then primal), every field updated
        in place: 176 bytes per voxel-iteration in FP32 */
     TGVDCT_KERNEL_TWO_PASS = 1,
