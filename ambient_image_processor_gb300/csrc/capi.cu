@@ -40,15 +40,20 @@ struct tgvdct_context {
     float* domain_mask = nullptr;
     uint8_t* domain = nullptr;
     uint32_t* tile_flags = nullptr;  // per-block plane ranges of the fused TMA kernel
-    // CUDA graph of graph_chunk(st) iterations (an even number, so the ping-pong
-    // parity of the state is unchanged after a replay), captured on a private stream
-    // and replayed on the caller's; rebuilt when the step or the state changes
-    cudaGraphExec_t graph = nullptr;
-    int graph_launches = 0;
+    // CUDA graphs of loop stretches, captured on a private stream and replayed on the
+    // caller's.  Each is valid for its length, starting parity, step, domain and
+    // z-chunk; a few are kept (least recently used goes first).
+    struct LoopGraph {
+        cudaGraphExec_t exec = nullptr;
+        uint32_t len = 0;
+        int cur = -1, end_cur = -1, zchunk = 0, launches = 0;
+        TgvStep step{};
+        const void* domain = nullptr;
+        uint64_t used = 0;
+    };
+    LoopGraph graphs[4];
+    uint64_t graph_clock = 0;
     cudaStream_t capture_stream = nullptr;
-    TgvStep graph_step{};
-    const void* graph_domain = nullptr;
-    int graph_cur = -1, graph_zchunk = 0;
     // reverse mode: checkpoints of the last checkpointed forward run, the states of
     // one recomputed segment, and the adjoint state with its scratch fields
     void* ckpt_block = nullptr;
@@ -264,26 +269,39 @@ int deliver(tgvdct_context* c, tgvdct_iteration_callback cb, void* user, uint32_
     return cb(it, c->prm.iteration_count, dst[0], dst[1], dst[2], dst[3], user);
 }
 
-// Iterations per graph replay (even).  Runs of shifted passes pay a dual and a primal
-// step of the two-pass kernels per run, so their graphs hold longer runs.
-uint32_t graph_chunk(const TgvState& s) { return tgv_uses_shifted(s) ? 128u : 32u; }
+// Stretches of at least kMinGraphRun iterations run as CUDA graph replays of at most
+// kMaxGraphRun iterations (a stop request is honoured between replays).  Longer
+// replays also mean fewer runs of shifted passes, each of which pays one dual and one
+// primal step of the two-pass kernels.
+constexpr uint32_t kMinGraphRun = 16, kMaxGraphRun = 512;
 
 bool same_step(const TgvStep& a, const TgvStep& b) {
     return a.tau == b.tau && a.sigma == b.sigma && a.theta == b.theta && a.lambda == b.lambda &&
            a.alpha0 == b.alpha0 && a.alpha1 == b.alpha1 && a.data_term == b.data_term;
 }
 
-// A graph of graph_chunk iterations for the state's current parity and step, built
-// on first use (every kernel attribute is set before the capture).  Null when
-// capture is not possible.
-cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
-    if (c->graph && same_step(c->graph_step, k) && c->graph_domain == c->st.domain &&
-        c->graph_cur == c->st.cur && c->graph_zchunk == c->st.zchunk)
-        return c->graph;
-    if (c->graph) {
-        cudaGraphExecDestroy(c->graph);
-        c->graph = nullptr;
+void drop_loop_graphs(tgvdct_context* c) {
+    for (auto& g : c->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = tgvdct_context::LoopGraph();
     }
+}
+
+// The graph of `len` iterations from the state's current parity with step k, built on
+// first use (every kernel attribute is set before the capture; the capture runs
+// nothing, so the state's parity is put back).  Null when capture is not possible.
+tgvdct_context::LoopGraph* loop_graph(tgvdct_context* c, const TgvStep& k, uint32_t len) {
+    for (auto& g : c->graphs)
+        if (g.exec && g.len == len && same_step(g.step, k) && g.domain == c->st.domain &&
+            g.cur == c->st.cur && g.zchunk == c->st.zchunk) {
+            g.used = ++c->graph_clock;
+            return &g;
+        }
+    tgvdct_context::LoopGraph* slot = &c->graphs[0];
+    for (auto& g : c->graphs)
+        if (!g.exec || (slot->exec && g.used < slot->used)) slot = &g;
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    *slot = tgvdct_context::LoopGraph();
     if (!c->capture_stream &&
         cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
@@ -296,26 +314,30 @@ cudaGraphExec_t loop_graph(tgvdct_context* c, const TgvStep& k) {
         return nullptr;
     }
     const int cur = c->st.cur;
-    const int launches = tgv_iterate_n(c->st, k, graph_chunk(c->st), c->capture_stream);
+    const int launches = tgv_iterate_n(c->st, k, len, c->capture_stream);
+    const int end_cur = c->st.cur;
+    c->st.cur = cur;
     const cudaError_t e = cudaStreamEndCapture(c->capture_stream, &g);
-    TGV_REQUIRE(c->st.cur == cur, "a graph chunk must keep the state's parity");
     if (e != cudaSuccess || !g) {
         cudaGetLastError();
         return nullptr;
     }
-    const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+    const cudaError_t ie = cudaGraphInstantiate(&slot->exec, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) {
         cudaGetLastError();
-        c->graph = nullptr;
+        slot->exec = nullptr;
         return nullptr;
     }
-    c->graph_step = k;
-    c->graph_launches = launches;
-    c->graph_domain = c->st.domain;
-    c->graph_cur = cur;
-    c->graph_zchunk = c->st.zchunk;
-    return c->graph;
+    slot->len = len;
+    slot->cur = cur;
+    slot->end_cur = end_cur;
+    slot->zchunk = c->st.zchunk;
+    slot->launches = launches;
+    slot->step = k;
+    slot->domain = c->st.domain;
+    slot->used = ++c->graph_clock;
+    return slot;
 }
 
 // The weighted primal energy of the loop's current (u, v) (synchronous).
@@ -335,9 +357,10 @@ double state_energy(tgvdct_context* c, cudaStream_t s) {
 // looks at the state only after iterations j > 0 with j % paint == 0 (callbacks,
 // tgv2_common.cu:381-384) or j % check == 0 (energy checks): the iterations up to
 // the next such j run as one stretch (tgv_iterate_n, shifted passes where the state
-// allows), whose full graph_chunk parts are CUDA graph replays (the small-volume
-// loops are launch-bound otherwise).  A stop request is honoured between stretches
-// and graph replays; the energy test after its checks.
+// allows), as CUDA graph replays of up to kMaxGraphRun iterations where it has at
+// least kMinGraphRun (the small-volume loops are launch-bound otherwise).  A stop
+// request is honoured between stretches and graph replays; the energy test after its
+// checks.
 template <class OnIteration>
 bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_iteration,
               bool from_initial_state = true) {
@@ -351,7 +374,6 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
     auto next_multiple = [](uint32_t it, uint32_t m) {
         return (it % m == 0) ? it : (it / m + 1) * m;
     };
-    const uint32_t chunk = graph_chunk(c->st);
     c->iterations_run = 0;
     c->loop_launches = 0;
     c->energy_history.clear();
@@ -368,15 +390,17 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
         if (check > 0) last = std::min(last, next_multiple(from, check));
         uint32_t run = last + 1 - it;
         bool stopped = false;
-        // graph replays where a whole chunk fits; not at the loop's first iteration,
-        // so that a short loop never pays a capture
-        while (it > 0 && run >= chunk) {
-            cudaGraphExec_t g = loop_graph(c, k);
+        // graph replays; not at the loop's first iteration, so that a short loop never
+        // pays a capture
+        while (it > 0 && run >= kMinGraphRun) {
+            const uint32_t len = std::min(run, kMaxGraphRun);
+            tgvdct_context::LoopGraph* g = loop_graph(c, k, len);
             if (!g) break;
-            TGV_CUDA(cudaGraphLaunch(g, s));
-            c->loop_launches += (uint64_t)c->graph_launches;
-            it += chunk;
-            run -= chunk;
+            TGV_CUDA(cudaGraphLaunch(g->exec, s));
+            c->st.cur = g->end_cur;
+            c->loop_launches += (uint64_t)g->launches;
+            it += len;
+            run -= len;
             if (run > 0 && c->stop_requested.exchange(false)) {
                 stopped = true;
                 break;
@@ -386,7 +410,7 @@ bool run_loop(tgvdct_context* c, cudaStream_t s, bool have_cb, OnIteration&& on_
             c->iterations_run = it;
             return true;
         }
-        if (it == 0 && run > chunk) run = 1;  // the first iteration alone, then graphs
+        if (it == 0 && run > kMinGraphRun) run = 1;  // the first iteration alone, then graphs
         if (run > 0) {
             c->loop_launches += (uint64_t)tgv_iterate_n(c->st, k, run, s);
             it += run;
@@ -464,7 +488,7 @@ void destroy_ctx(tgvdct_context* c) {
     if (c->domain) cudaFree(c->domain);
     if (c->tile_flags) cudaFree(c->tile_flags);
     if (c->host_cb) cudaFreeHost(c->host_cb);
-    if (c->graph) cudaGraphExecDestroy(c->graph);
+    drop_loop_graphs(c);
     if (c->bwd_graph) cudaGraphExecDestroy(c->bwd_graph);
     if (c->energy_dev) cudaFree(c->energy_dev);
     if (c->capture_stream) cudaStreamDestroy(c->capture_stream);
@@ -1709,10 +1733,7 @@ tgvdct_status tgvdct_set_pipeline_wait_limit(tgvdct_context* c, uint64_t limit_n
         c->st.wait_ns = limit_ns;
         if (c->plan) c->plan->wait_ns = limit_ns;
         // the loop and backward graphs hold the old limit in their kernel arguments
-        if (c->graph) {
-            cudaGraphExecDestroy(c->graph);
-            c->graph = nullptr;
-        }
+        drop_loop_graphs(c);
         if (c->bwd_graph) {
             cudaGraphExecDestroy(c->bwd_graph);
             c->bwd_graph = nullptr;

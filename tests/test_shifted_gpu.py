@@ -47,7 +47,7 @@ def test_runs_equal_two_pass(gpu_lib, iterations, shape, z_chunk):
 
 @pytest.mark.parametrize("data_term", [pkg.DATA_L1, pkg.DATA_L2])
 def test_data_terms_and_long_runs(gpu_lib, data_term):
-    # 300 iterations: the first alone, two graph replays of 128, a run of 43
+    # 300 iterations: the first alone, then one graph replay of 299
     f = tissue_phantom_3d(10, 24, 64, seed=22)
     ref = _process(f, pkg.KERNEL_TWO_PASS, 300, data_term=data_term)
     _equal(ref, _process(f, pkg.KERNEL_FUSED_SHIFTED, 300, data_term=data_term))
@@ -121,6 +121,14 @@ def test_loop_launch_count(gpu_lib):
             counts[kernel] = ctx.loop_launches()
     assert counts[pkg.KERNEL_FUSED] == 300
     assert counts[pkg.KERNEL_TWO_PASS] == 600
-    # the first iteration alone, two graph replays of 128 (129 launches each), a run
-    # of 43 (44 launches)
-    assert counts[pkg.KERNEL_FUSED_SHIFTED] == 1 + 2 * 129 + 44
+    # the first iteration alone, then a graph of 299 (a dual step, 298 shifted passes,
+    # a primal step)
+    assert counts[pkg.KERNEL_FUSED_SHIFTED] == 1 + 300
+    prm = pkg.default_params(width=32, height=16, depth=6, iteration_count=1300,
+                             iteration_kernel=pkg.KERNEL_FUSED_SHIFTED)
+    with pkg.Context(prm) as ctx:
+        for _ in range(2):  # the second run replays the graphs of the first
+            ctx.run_dev(f.data_ptr(), *(o.data_ptr() for o in out))
+            torch.cuda.synchronize()
+            # replays of at most 512 iterations: 1 + (512 + 1) + (512 + 1) + (275 + 1)
+            assert ctx.loop_launches() == 1 + 513 + 513 + 276
