@@ -183,8 +183,8 @@ void tgv_snapshot_load(TgvState& s, const void* src, cudaStream_t st);
 void tgv_iterate(TgvState& s, const TgvStep& k, cudaStream_t st);
 // Number of kernels tgv_iterate launches.
 int tgv_kernels_per_iteration(const TgvState& s);
-// n iterations.  With TGV_KERNEL_SHIFTED (FP32, 3-D, depth >= 2, width a multiple of 4,
-// no domain) and n >= 2 they run as a dual step, n - 1 shifted passes and a primal
+// n iterations.  With TGV_KERNEL_SHIFTED (FP32, 3-D, depth >= 2, width a multiple of 4)
+// and n >= 2 they run as a dual step, n - 1 shifted passes and a primal
 // step; otherwise as n calls of tgv_iterate.  Either way the state ends in the
 // standard form with the parity n single iterations give.  Returns the launches.
 int tgv_iterate_n(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st);

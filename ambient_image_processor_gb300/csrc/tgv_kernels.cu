@@ -1310,6 +1310,9 @@ struct Args {
     int skip_bz;
     int* err;
     unsigned long long wait_ns;  // limit of the consumers' pipeline waits (0: one test)
+    const uint8_t* dom;          // masked deshade domain (the MASKED instance only)
+    // per-block plane ranges of this grid for that domain (null: whole chunks)
+    const uint32_t* tile_active;
 };
 
 template <int NS>
@@ -1319,14 +1322,27 @@ constexpr size_t smem_bytes() {
 
 }  // namespace shp
 
-template <int DATA, int NS>
+template <int DATA, int NS, bool MASKED>
 __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages,
                                              uint8_t* ustages, float* ring, uint64_t* full,
                                              uint64_t* ufull) {
     using namespace shp;
     using tma::su32;
     static_assert(NS >= 4, "step t reads three planes; one more must be in flight");
-    const int z0 = (int)blockIdx.z * a.zchunk, z1 = min(a.D, z0 + a.zchunk);
+    int z0 = (int)blockIdx.z * a.zchunk, z1 = min(a.D, z0 + a.zchunk);
+    if constexpr (MASKED) {
+        // Only the planes in which some of the tile's voxels are in the domain have
+        // anything to update; none: the block leaves.  A voxel outside the domain keeps
+        // u = ubar = f, v = vbar = 0, p = q = 0, in both slots of the shifted form, so
+        // the frozen planes need no work.  One entry per block (a uniform branch).
+        if (a.tile_active) {
+            const uint32_t r = a.tile_active[((size_t)blockIdx.z * gridDim.y + blockIdx.y) *
+                                                 gridDim.x + blockIdx.x];
+            if (r == 0) return;
+            z0 = (int)(r >> 16);
+            z1 = (int)(r & 0xffffu);
+        }
+    }
     const int tid = threadIdx.x;
     int ex = 0, ey = 0, role = IDLE;
     if (tid < 256) {
@@ -1356,6 +1372,11 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // 32-bit voxel indices: the host runs this kernel only on volumes of < 2^32 voxels
     const uint32_t wh = (uint32_t)a.WH;
     const uint32_t col = role != IDLE ? (uint32_t)y * (uint32_t)a.W + (uint32_t)x : 0u;
+    // whether this thread's voxel of plane z is in the masked deshade's domain
+    auto live = [&](int z) {
+        if constexpr (MASKED) return a.dom[(uint32_t)z * wh + col] != 0;
+        else return true;
+    };
     if constexpr (kCheckBounds) {
         // every index this thread's role uses: its column over the chunk, the staged
         // boxes with the neighbours the primal reads, and the ring
@@ -1439,8 +1460,19 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     float pzm = 0.f;
     auto primal_at = [&](const float* S, const float* Sn, bool has_next, float* R,
                          const float* Us, uint32_t i, bool full, float& ub_out,
-                         float* vb_out) {
+                         float* vb_out, bool lv) {
         const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+        if (!lv) {  // frozen: ubar = u, vbar = 0 (p = 0 here), nothing stored
+            const float ub = Us[ob];
+            ub_out = ub;
+            if (full) {
+                if (need_u) R[e] = ub;
+                if (need_v)
+                    for (int c = 0; c < 3; ++c) R[(1 + c) * NE + e] = 0.f;
+            }
+            pzm = pv[2];
+            return;
+        }
         if (need_u) {
             // u <- prox(u - tau B.p), ubar                (tgv2_l1.cu:39-52)
             const float pu = Us[ob], pf = Us[BOXF + ob];
@@ -1495,7 +1527,8 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // ubar own of planes t, t + 1 and vbar own of planes t - 1, t from registers, the
     // neighbours from the ring
     auto dual_at = [&](const float* S, const float* R, float ubc, float ubn, bool has_next,
-                       const float* vbc, const float* vbm, bool has_prev, uint32_t i) {
+                       const float* vbc, const float* vbm, bool has_prev, uint32_t i, bool lv) {
+        if (!lv) return;  // p = q = 0 already, in both slots
         float g[3] = {xl ? R[e + 1] - ubc : 0.f, yl ? R[e + EXW] - ubc : 0.f,
                       has_next ? ubn - ubc : 0.f};
         float vb[3] = {vbc[0], vbc[1], vbc[2]};
@@ -1547,7 +1580,7 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     if (ok) {
         if (z0 > 0) {
             const float* S = stage_at(z0 - 1);
-            if (tile) {
+            if (tile && live(z0 - 1)) {
                 const float* Us = ustage_at(z0 - 1);
                 const float* Q = S + QOFF;
                 const float* Qn = stage_at(z0) + QOFF;
@@ -1576,7 +1609,7 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         const float* S = stage_at(z0);
         if (role != IDLE)
             primal_at(S, hn ? stage_at(z0 + 1) : S, hn, ring + (z0 & 1) * 4 * NE, ustage_at(z0),
-                      (uint32_t)z0 * wh + col, true, ubc, vbc);
+                      (uint32_t)z0 * wh + col, true, ubc, vbc, live(z0));
     }
     ok = __syncthreads_and(ok);
     if (ok && tid == PRODUCER) {  // planes z0 - 1 (if any) and z0 are done
@@ -1608,11 +1641,17 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
                 if (role != IDLE && (full || tile))
                     primal_at(S1, hn ? S2 : S1, hn, ring + ((t + 1) & 1) * 4 * NE,
                               (const float*)(ustages + us * USTAGE),
-                              (uint32_t)(t + 1) * wh + col, full, ubn, vbn);
+                              (uint32_t)(t + 1) * wh + col, full, ubn, vbn, live(t + 1));
+                if constexpr (MASKED) {  // the flags two planes ahead into L2
+                    if (role != IDLE && t + 3 <= qlast) {
+                        const uint8_t* fl = a.dom + (uint32_t)(t + 3) * wh + col;
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(fl));
+                    }
+                }
             }
             if (tile)
                 dual_at(St, ring + (t & 1) * 4 * NE, ubc, ubn, p1, vbc, vbm, t > 0,
-                        (uint32_t)t * wh + col);
+                        (uint32_t)t * wh + col, live(t));
             ubc = ubn;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -1646,7 +1685,7 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     __syncthreads();
 }
 
-template <int DATA, int NS>
+template <int DATA, int NS, bool MASKED>
 __global__ void __launch_bounds__(shp::NTHREADS, 2)
     tgv_shifted_tma_kernel(const __grid_constant__ shp::Args a) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -1656,7 +1695,7 @@ __global__ void __launch_bounds__(shp::NTHREADS, 2)
     if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
     uint8_t* ustages = smem + NS * shp::STAGE;
     float* ring = (float*)(ustages + shp::NU * shp::USTAGE);
-    shifted_pass<DATA, NS>(a, smem, ustages, ring, full, full + NS);
+    shifted_pass<DATA, NS, MASKED>(a, smem, ustages, ring, full, full + NS);
 }
 
 size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2; }
@@ -1974,7 +2013,7 @@ constexpr int SHIFTED_NS = 5;
 
 bool shifted_ok(const TgvState& s) {
     return s.kernel == TGV_KERNEL_SHIFTED && s.precision == TGVDCT_STATE_FP32 && s.three &&
-           s.D >= 2 && s.W % 4 == 0 && !s.domain && s.err &&
+           s.D >= 2 && s.W % 4 == 0 && s.err &&
            (uint64_t)s.W * s.H * s.D < (1ull << 32);  // 32-bit voxel indices
 }
 
@@ -2041,19 +2080,19 @@ ShiftedCache* shifted_cache(TgvState& s) {
 }
 
 // Raises the shared-memory limit of the shifted kernel on the current device, once.
-template <int DATA>
+template <int DATA, bool MASKED>
 void shifted_attr() {
     static std::atomic<uint64_t> configured{0};  // per template instance
-    smem_attr_once((const void*)tgv_shifted_tma_kernel<DATA, SHIFTED_NS>,
+    smem_attr_once((const void*)tgv_shifted_tma_kernel<DATA, SHIFTED_NS, MASKED>,
                    shp::smem_bytes<SHIFTED_NS>(), configured);
 }
 
-template <int DATA>
+template <int DATA, bool MASKED>
 void launch_shifted(const shp::Args& a, cudaStream_t st) {
     constexpr int NS = SHIFTED_NS;
-    auto kern = tgv_shifted_tma_kernel<DATA, NS>;
+    auto kern = tgv_shifted_tma_kernel<DATA, NS, MASKED>;
     constexpr size_t smem = shp::smem_bytes<NS>();
-    shifted_attr<DATA>();
+    shifted_attr<DATA, MASKED>();
     const dim3 grid(ceil_div(a.W, shp::TX), ceil_div(a.H, shp::TY), ceil_div(a.D, a.zchunk));
     kern<<<grid, shp::NTHREADS, smem, st>>>(a);
     TGV_CHECK_LAUNCH();
@@ -2089,8 +2128,17 @@ int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) 
         a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
         a.err = s.err;
         a.wait_ns = s.wait_ns;
-        if (k.data_term == TGVDCT_DATA_L1) launch_shifted<TGVDCT_DATA_L1>(a, st);
-        else launch_shifted<TGVDCT_DATA_L2>(a, st);
+        a.dom = s.domain;
+        a.tile_active = (s.domain && s.tile_active && s.tile_zchunk == a.zchunk) ? s.tile_active
+                                                                                  : nullptr;
+        const bool m = a.dom != nullptr;
+        if (k.data_term == TGVDCT_DATA_L1) {
+            if (m) launch_shifted<TGVDCT_DATA_L1, true>(a, st);
+            else launch_shifted<TGVDCT_DATA_L1, false>(a, st);
+        } else {
+            if (m) launch_shifted<TGVDCT_DATA_L2, true>(a, st);
+            else launch_shifted<TGVDCT_DATA_L2, false>(a, st);
+        }
     }
     {   // the primal step of the last iteration, into the standard state: u, v to their
         // own buffers, ubar, vbar to the set that holds the last p, q
@@ -2419,8 +2467,10 @@ int tgv_iterate_n(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) {
 
 void tgv_prepare_launches(const TgvState& s) {
     if (!shifted_ok(s)) return;
-    shifted_attr<TGVDCT_DATA_L1>();
-    shifted_attr<TGVDCT_DATA_L2>();
+    shifted_attr<TGVDCT_DATA_L1, false>();
+    shifted_attr<TGVDCT_DATA_L2, false>();
+    shifted_attr<TGVDCT_DATA_L1, true>();
+    shifted_attr<TGVDCT_DATA_L2, true>();
 }
 
 }  // namespace tgvdct

@@ -99,7 +99,7 @@ typedef enum tgvdct_iteration_kernel {
     /* runs of iterations as shifted passes: each pass does the primal step of one
        iteration and the dual step of the next, so ubar and vbar stay on chip and a
        voxel-iteration moves 108 bytes (FP32 state, 3-D, depth >= 2, width a
-       multiple of 4, no mask); one dual step before a run and one primal step
+       multiple of 4; masked runs too); one dual step before a run and one primal step
        after it (the two-pass kernels) convert the state.  Single iterations and the
        cases it does not take run as TGVDCT_KERNEL_FUSED.  Same bits as the others. */
     TGVDCT_KERNEL_FUSED_SHIFTED = 4

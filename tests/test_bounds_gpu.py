@@ -69,6 +69,15 @@ def test_masked_and_downsampled_paths_stay_in_bounds(gpu_lib):
     assert _first_bad(Lc) == 0
     for a, b in zip(got, _process(L, f, mask=m)):
         assert np.array_equal(a, b, equal_nan=True) and np.isfinite(a).any()
+    # the masked shifted passes, on blocks away from every face as well
+    g = tissue_phantom_3d(10, 30, 100, seed=15).astype(np.float32)
+    gm = (np.indices(g.shape).sum(axis=0) % 7 != 0).astype(np.float32)
+    gm[:, :, :20] = 0.0
+    kw = {"iteration_kernel": pkg.KERNEL_FUSED_SHIFTED, "z_chunk": 3}
+    got = _process(Lc, g, mask=gm, **kw)
+    assert _first_bad(Lc) == 0
+    for a, b in zip(got, _process(L, g, mask=gm, **kw)):
+        assert np.array_equal(a, b, equal_nan=True) and np.isfinite(a).any()
     alpha = np.array([1.0, 2.0], np.float32)
     outs = []
     for lib in (Lc, L):

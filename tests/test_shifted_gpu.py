@@ -7,7 +7,7 @@ sequence as in the two-pass and fused kernels, so the results must be bit-identi
 theirs: for both parities of a run, every z-chunking, shapes whose blocks all touch the
 volume's faces and shapes with blocks that run without boundary tests, both data terms,
 callbacks between runs, CUDA graph replays of long runs, the stepping entry point and
-the state snapshot."""
+the state snapshot, and masked runs (frozen voxels outside the domain)."""
 import ctypes
 
 import numpy as np
@@ -43,6 +43,42 @@ def test_runs_equal_two_pass(gpu_lib, iterations, shape, z_chunk):
     f = tissue_phantom_3d(*shape, seed=21)
     ref = _process(f, pkg.KERNEL_TWO_PASS, iterations)
     _equal(ref, _process(f, pkg.KERNEL_FUSED_SHIFTED, iterations, z_chunk=z_chunk))
+
+
+# extreme shapes: one row, a width of 4 (one column of TMA alignment), two planes,
+# heights and widths that leave a single tile with idle rows and columns
+@pytest.mark.parametrize("shape,z_chunk", [((2, 1, 4), 0), ((5, 1, 36), 2), ((3, 9, 4), 1),
+                                           ((2, 2, 8), 0), ((40, 3, 12), 7)])
+def test_extreme_shapes(gpu_lib, shape, z_chunk):
+    f = tissue_phantom_3d(*shape, seed=26)
+    ref = _process(f, pkg.KERNEL_TWO_PASS, 9)
+    _equal(ref, _process(f, pkg.KERNEL_FUSED_SHIFTED, 9, z_chunk=z_chunk))
+
+
+def _mask(shape):
+    """An off-centre ellipsoid with scattered holes: blocks wholly outside the domain,
+    wholly inside, and mixed, and plane ranges trimmed at both ends."""
+    d, h, w = shape
+    z, y, x = np.indices(shape, dtype=np.float64)
+    r = ((z - 0.55 * d) / (0.4 * d)) ** 2 + ((y - 0.45 * h) / (0.45 * h)) ** 2 + \
+        ((x - 0.5 * w) / (0.4 * w)) ** 2
+    holes = (z * 7 + y * 3 + x) % 11 == 0
+    return ((r < 1.0) & ~holes).astype(np.float32) * 2.0  # the domain is mask >= 1
+
+
+@pytest.mark.parametrize("iterations", [2, 7])
+@pytest.mark.parametrize("shape,z_chunk", [((9, 26, 100), 0), ((12, 40, 132), 5),
+                                           ((3, 20, 36), 1), ((20, 24, 64), 3)])
+def test_masked_runs_equal_two_pass(gpu_lib, iterations, shape, z_chunk):
+    f = tissue_phantom_3d(*shape, seed=27)
+    m = _mask(shape)
+    kw = dict(mask=m, set_negative_values_to_zero=False)
+    a = pkg.TGVDeshadeMaskedProcessor.processTGV2L1GPUCuda(
+        f, 0.9, 2.0, 1.0, iterations, iteration_kernel=pkg.KERNEL_TWO_PASS, **kw)
+    b = pkg.TGVDeshadeMaskedProcessor.processTGV2L1GPUCuda(
+        f, 0.9, 2.0, 1.0, iterations, iteration_kernel=pkg.KERNEL_FUSED_SHIFTED,
+        z_chunk=z_chunk, **kw)
+    _equal(a, b)
 
 
 @pytest.mark.parametrize("data_term", [pkg.DATA_L1, pkg.DATA_L2])
