@@ -1276,13 +1276,23 @@ constexpr int TX = 32, TY = 8;
 constexpr int EXW = TX + 2, EYH = TY + 2, NE = EXW * EYH;  // tile and rim: 34 x 10
 constexpr int NTHREADS = 352;                              // 8 tile warps, 80 rim threads
 constexpr int PRODUCER = 256;                              // first rim thread issues TMA
-constexpr int XO = 4, BW = TX + 8, BH = TY + 2;            // boxes x0-4 .. x0+35, 10 rows
+// FP32 boxes (u, f, v): x0-4 .. x0+35, rows y0-1 .. y0+8
+constexpr int XO = 4, BW = TX + 8, BH = TY + 2;
 constexpr int BOX = (BW * BH * 4 + 127) / 128 * 128;       // bytes per box in a stage
 constexpr int BOXF = BOX / 4;                              // floats per box
-constexpr int QOFF = 3 * BOXF;                             // first q box (floats)
-constexpr int STAGE = 9 * BOX;                             // p[3] | q[6] in slot order
-constexpr uint32_t TX_BYTES = 9u * BW * BH * 4;            // what expect_tx announces
 constexpr int RING = 2 * 4 * NE;                           // [plane & 1][ubar, vbar x3][NE]
+// p, q boxes in the state's dual element type: the same rows, x from a 16-byte boundary
+// (x0-4 for FP32, x0-8 for 16-bit elements) to at least x0+32
+template <int PREC>
+struct PQ {
+    static constexpr int DES = PREC == TGVDCT_STATE_FP32 ? 4 : 2;
+    static constexpr int XO = DES == 4 ? 4 : 8;
+    static constexpr int BW = DES == 4 ? TX + 8 : TX + 16;
+    static constexpr int BOX = (BW * BH * DES + 127) / 128 * 128;  // bytes per box
+    static constexpr int BOXE = BOX / DES;                          // elements per box
+    static constexpr int STAGE = 9 * BOX;                           // p[3] | q[6], slot order
+    static constexpr uint32_t TX_BYTES = 9u * BW * BH * DES;        // what expect_tx announces
+};
 constexpr int NU = 3;                                      // stages of u, f, v
 constexpr int USTAGE = 5 * BOX;                            // u | f | v[3], same boxes
 constexpr uint32_t UTX_BYTES = 5u * BW * BH * 4;
@@ -1303,9 +1313,10 @@ struct Args {
     const float* v[3];
     float* u_out;    // u^(n+1), v^(n+1), p^(n+2), q^(n+2) (distinct from the inputs)
     float* v_out[3];
-    float* p_out[3];
-    float* q_out[6];  // state order: xx yy zz xy xz yz
+    void* p_out[3];  // the state's dual element type
+    void* q_out[6];  // state order: xx yy zz xy xz yz
     float tau, sigma, theta, tau_lambda, alpha0, alpha1;
+    float penc, pdec, qenc, qdec;  // 16-bit fixed-point scales (Dual<FX16>)
     float thr_p, thr_q;  // squared-norm bounds below which the projections are skipped
     int skip_bz;
     int* err;
@@ -1315,19 +1326,22 @@ struct Args {
     const uint32_t* tile_active;
 };
 
-template <int NS>
+template <int NS, int PREC>
 constexpr size_t smem_bytes() {
-    return (size_t)NS * STAGE + (size_t)NU * USTAGE + (size_t)RING * 4 + 128;
+    return (size_t)NS * PQ<PREC>::STAGE + (size_t)NU * USTAGE + (size_t)RING * 4 + 128;
 }
 
 }  // namespace shp
 
-template <int DATA, int NS, bool MASKED>
+template <int PREC, int DATA, int NS, bool MASKED>
 __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages,
                                              uint8_t* ustages, float* ring, uint64_t* full,
                                              uint64_t* ufull) {
     using namespace shp;
     using tma::su32;
+    using DS = Dual<PREC>;
+    using T = typename DS::T;
+    using G = PQ<PREC>;
     static_assert(NS >= 4, "step t reads three planes; one more must be in flight");
     int z0 = (int)blockIdx.z * a.zchunk, z1 = min(a.D, z0 + a.zchunk);
     if constexpr (MASKED) {
@@ -1364,7 +1378,8 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     const bool xl = x + 1 < a.W, yl = y + 1 < a.H;
     const bool xg = x > 0, yg = y > 0;
     const int e = ey * EXW + ex;            // position in the ubar / vbar ring
-    const int ob = ey * BW + ex + XO - 1;   // position in the p and q boxes
+    const int ob = ey * BW + ex + XO - 1;        // position in the u, f, v boxes
+    const int oq = ey * G::BW + ex + G::XO - 1;  // position in the p and q boxes
     const int D = a.D;
     const int pbase = max(z0 - 1, 0);       // first plane of p, q this block loads
     const int plast = min(D - 1, z1);       // last one
@@ -1380,21 +1395,22 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     if constexpr (kCheckBounds) {
         // every index this thread's role uses: its column over the chunk, the staged
         // boxes with the neighbours the primal reads, and the ring
-        constexpr int nB = BW * BH;
+        constexpr int nB = BW * BH, nQ = G::BW * BH;
         bool ok = true;
         if (role != IDLE) {
             ok = TGV_IN_BOUNDS(col, a.WH, 40) && ok;
             ok = TGV_IN_BOUNDS((size_t)qlast * a.WH + col, a.WH * (size_t)D, 41) && ok;
             ok = TGV_IN_BOUNDS(ob, nB, 42) && ok;
+            ok = TGV_IN_BOUNDS(oq, nQ, 52) && ok;
             ok = TGV_IN_BOUNDS(e, NE, 43) && ok;
         }
         if (need_u) {
-            if (xg) ok = TGV_IN_BOUNDS(ob - 1, nB, 44) && ok;
-            if (yg) ok = TGV_IN_BOUNDS(ob - BW, nB, 45) && ok;
+            if (xg) ok = TGV_IN_BOUNDS(oq - 1, nQ, 44) && ok;
+            if (yg) ok = TGV_IN_BOUNDS(oq - G::BW, nQ, 45) && ok;
         }
         if (need_v) {
-            if (xl) ok = TGV_IN_BOUNDS(ob + 1, nB, 46) && ok;
-            if (yl) ok = TGV_IN_BOUNDS(ob + BW, nB, 47) && ok;
+            if (xl) ok = TGV_IN_BOUNDS(oq + 1, nQ, 46) && ok;
+            if (yl) ok = TGV_IN_BOUNDS(oq + G::BW, nQ, 47) && ok;
         }
         if (tile) {
             if (xl) ok = TGV_IN_BOUNDS(e + 1, NE, 48) && ok;
@@ -1405,20 +1421,26 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         if (__syncthreads_or(!ok)) return;
     }
     auto stage_at = [&](int plane) {
-        return (const float*)(stages + ((plane - pbase) % NS) * STAGE);
+        return (const T*)(stages + ((plane - pbase) % NS) * G::STAGE);
+    };
+    // p component c and q slot k of a stage at a box position, decoded to float
+    auto pval = [&](const T* st, int c, int off) { return DS::ld(st, c * G::BOXE + off, a.pdec); };
+    auto qval = [&](const T* st, int k, int off) {
+        return DS::ld(st, (3 + k) * G::BOXE + off, a.qdec);
     };
     auto issue = [&](int plane) {  // producer thread only
         if (plane < 0 || plane > plast) return;
         const int slot = (plane - pbase) % NS;
-        uint8_t* st = stages + slot * STAGE;
+        uint8_t* st = stages + slot * G::STAGE;
         uint64_t* bar = &full[slot];
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)),
-                     "r"(TX_BYTES)
+                     "r"(G::TX_BYTES)
                      : "memory");
-        const int xb = x0 - XO, yb = y0 - 1;
-        for (int c = 0; c < 3; ++c) tma::tma_load(st + c * BOX, &a.maps.p[c], xb, yb, plane, bar);
+        const int xb = x0 - G::XO, yb = y0 - 1;
+        for (int c = 0; c < 3; ++c)
+            tma::tma_load(st + c * G::BOX, &a.maps.p[c], xb, yb, plane, bar);
         for (int k = 0; k < 6; ++k)
-            tma::tma_load(st + (3 + k) * BOX, &a.maps.q[k], xb, yb, plane, bar);
+            tma::tma_load(st + (3 + k) * G::BOX, &a.maps.q[k], xb, yb, plane, bar);
     };
     bool ok = true;
     int waited_upto = pbase - 1;  // every plane <= this one has landed
@@ -1458,10 +1480,10 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // the plane is one of the block's (u and v stored); otherwise only the tile's own
     // ubar is wanted (the dual of the block's last plane reads it).
     float pzm = 0.f;
-    auto primal_at = [&](const float* S, const float* Sn, bool has_next, float* R,
+    auto primal_at = [&](const T* S, const T* Sn, bool has_next, float* R,
                          const float* Us, uint32_t i, bool full, float& ub_out,
                          float* vb_out, bool lv) {
-        const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+        const float pv[3] = {pval(S, 0, oq), pval(S, 1, oq), pval(S, 2, oq)};
         if (!lv) {  // frozen: ubar = u, vbar = 0 (p = 0 here), nothing stored
             const float ub = Us[ob];
             ub_out = ub;
@@ -1476,8 +1498,8 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         if (need_u) {
             // u <- prox(u - tau B.p), ubar                (tgv2_l1.cu:39-52)
             const float pu = Us[ob], pf = Us[BOXF + ob];
-            const float bx = (xg ? S[ob - 1] : 0.f) - pv[0];
-            const float by = (yg ? S[BOXF + ob - BW] : 0.f) - pv[1];
+            const float bx = (xg ? pval(S, 0, oq - 1) : 0.f) - pv[0];
+            const float by = (yg ? pval(S, 1, oq - G::BW) : 0.f) - pv[1];
             float div = bx + by;
             const float bz = pzm - pv[2];
             if (!a.skip_bz) div = div + bz;
@@ -1499,18 +1521,16 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         }
         if (need_v && full) {
             // v <- v - tau (div q - p), vbar               (tgv2_common.cu:290-347)
-            const float* Q = S + QOFF;
-            const float* Qn = Sn + QOFF;
-            const float qxx = Q[ob], qyy = Q[BOXF + ob], qxy = Q[2 * BOXF + ob];
-            const float qzz = Q[3 * BOXF + ob], qxz = Q[4 * BOXF + ob], qyz = Q[5 * BOXF + ob];
+            const float qxx = qval(S, 0, oq), qyy = qval(S, 1, oq), qxy = qval(S, 2, oq);
+            const float qzz = qval(S, 3, oq), qxz = qval(S, 4, oq), qyz = qval(S, 5, oq);
             float d[3];
-            d[0] = (xl ? Q[ob + 1] - qxx : 0.f) + (yl ? Q[2 * BOXF + ob + BW] - qxy : 0.f);
-            d[1] = (yl ? Q[BOXF + ob + BW] - qyy : 0.f) + (xl ? Q[2 * BOXF + ob + 1] - qxy : 0.f);
-            d[0] = d[0] + (has_next ? Qn[4 * BOXF + ob] - qxz : 0.f);
-            d[1] = d[1] + (has_next ? Qn[5 * BOXF + ob] - qyz : 0.f);
-            d[2] = ((has_next ? Qn[3 * BOXF + ob] - qzz : 0.f) +
-                    (xl ? Q[4 * BOXF + ob + 1] - qxz : 0.f)) +
-                   (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
+            d[0] = (xl ? qval(S, 0, oq + 1) - qxx : 0.f) + (yl ? qval(S, 2, oq + G::BW) - qxy : 0.f);
+            d[1] = (yl ? qval(S, 1, oq + G::BW) - qyy : 0.f) + (xl ? qval(S, 2, oq + 1) - qxy : 0.f);
+            d[0] = d[0] + (has_next ? qval(Sn, 4, oq) - qxz : 0.f);
+            d[1] = d[1] + (has_next ? qval(Sn, 5, oq) - qyz : 0.f);
+            d[2] = ((has_next ? qval(Sn, 3, oq) - qzz : 0.f) +
+                    (xl ? qval(S, 4, oq + 1) - qxz : 0.f)) +
+                   (yl ? qval(S, 5, oq + G::BW) - qyz : 0.f);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const float vo = Us[(2 + c) * BOXF + ob];
@@ -1526,13 +1546,13 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     // ---- the dual step at plane t (stage S, ring slot R of plane t), tile threads:
     // ubar own of planes t, t + 1 and vbar own of planes t - 1, t from registers, the
     // neighbours from the ring
-    auto dual_at = [&](const float* S, const float* R, float ubc, float ubn, bool has_next,
+    auto dual_at = [&](const T* S, const float* R, float ubc, float ubn, bool has_next,
                        const float* vbc, const float* vbm, bool has_prev, uint32_t i, bool lv) {
         if (!lv) return;  // p = q = 0 already, in both slots
         float g[3] = {xl ? R[e + 1] - ubc : 0.f, yl ? R[e + EXW] - ubc : 0.f,
                       has_next ? ubn - ubc : 0.f};
         float vb[3] = {vbc[0], vbc[1], vbc[2]};
-        float pp[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
+        float pp[3] = {pval(S, 0, oq), pval(S, 1, oq), pval(S, 2, oq)};
         dual_p_update<true>(g, vb, pp, a.sigma, a.alpha1, a.thr_p);
         float xm[3], ym[3], zm[3], q[6];
 #pragma unroll
@@ -1543,16 +1563,13 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
             zm[c] = has_prev ? vbm[c] : 0.f;
         }
 #pragma unroll
-        for (int k = 0; k < 6; ++k) q[k] = S[QOFF + k * BOXF + ob];
+        for (int k = 0; k < 6; ++k) q[k] = qval(S, k, oq);
         dual_q_update<true>(vb, xm, ym, zm, q, a.sigma, a.alpha0, a.thr_q);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) __stcs(a.p_out[c] + i, pp[c]);
-        __stcs(a.q_out[0] + i, q[0]);
-        __stcs(a.q_out[1] + i, q[1]);
-        __stcs(a.q_out[3] + i, q[2]);
-        __stcs(a.q_out[2] + i, q[3]);
-        __stcs(a.q_out[4] + i, q[4]);
-        __stcs(a.q_out[5] + i, q[5]);
+        for (int c = 0; c < 3; ++c) DS::st_cs((T*)a.p_out[c], i, pp[c], a.penc);
+        const int qmap[6] = {0, 1, 3, 2, 4, 5};  // slot -> state order
+#pragma unroll
+        for (int k = 0; k < 6; ++k) DS::st_cs((T*)a.q_out[qmap[k]], i, q[k], a.qenc);
     };
 
     if (tid == 0) {
@@ -1579,23 +1596,22 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     float ubc = 0.f, vbc[3] = {0.f, 0.f, 0.f}, vbm[3] = {0.f, 0.f, 0.f};
     if (ok) {
         if (z0 > 0) {
-            const float* S = stage_at(z0 - 1);
+            const T* S = stage_at(z0 - 1);
             if (tile && live(z0 - 1)) {
                 const float* Us = ustage_at(z0 - 1);
-                const float* Q = S + QOFF;
-                const float* Qn = stage_at(z0) + QOFF;
-                const float pv[3] = {S[ob], S[BOXF + ob], S[2 * BOXF + ob]};
-                const float qxx = Q[ob], qyy = Q[BOXF + ob], qxy = Q[2 * BOXF + ob];
-                const float qzz = Q[3 * BOXF + ob], qxz = Q[4 * BOXF + ob];
-                const float qyz = Q[5 * BOXF + ob];
+                const T* Sn = stage_at(z0);
+                const float pv[3] = {pval(S, 0, oq), pval(S, 1, oq), pval(S, 2, oq)};
+                const float qxx = qval(S, 0, oq), qyy = qval(S, 1, oq), qxy = qval(S, 2, oq);
+                const float qzz = qval(S, 3, oq), qxz = qval(S, 4, oq), qyz = qval(S, 5, oq);
                 float d[3];
-                d[0] = (xl ? Q[ob + 1] - qxx : 0.f) + (yl ? Q[2 * BOXF + ob + BW] - qxy : 0.f);
-                d[1] = (yl ? Q[BOXF + ob + BW] - qyy : 0.f) +
-                       (xl ? Q[2 * BOXF + ob + 1] - qxy : 0.f);
-                d[0] = d[0] + (Qn[4 * BOXF + ob] - qxz);
-                d[1] = d[1] + (Qn[5 * BOXF + ob] - qyz);
-                d[2] = ((Qn[3 * BOXF + ob] - qzz) + (xl ? Q[4 * BOXF + ob + 1] - qxz : 0.f)) +
-                       (yl ? Q[5 * BOXF + ob + BW] - qyz : 0.f);
+                d[0] = (xl ? qval(S, 0, oq + 1) - qxx : 0.f) +
+                       (yl ? qval(S, 2, oq + G::BW) - qxy : 0.f);
+                d[1] = (yl ? qval(S, 1, oq + G::BW) - qyy : 0.f) +
+                       (xl ? qval(S, 2, oq + 1) - qxy : 0.f);
+                d[0] = d[0] + (qval(Sn, 4, oq) - qxz);
+                d[1] = d[1] + (qval(Sn, 5, oq) - qyz);
+                d[2] = ((qval(Sn, 3, oq) - qzz) + (xl ? qval(S, 4, oq + 1) - qxz : 0.f)) +
+                       (yl ? qval(S, 5, oq + G::BW) - qyz : 0.f);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const float vo = Us[(2 + c) * BOXF + ob];
@@ -1603,10 +1619,10 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
                     vbm[c] = vn + a.theta * (vn - vo);
                 }
             }
-            if (role != IDLE) pzm = S[2 * BOXF + ob];
+            if (role != IDLE) pzm = pval(S, 2, oq);
         }
         const bool hn = z0 + 1 < D;
-        const float* S = stage_at(z0);
+        const T* S = stage_at(z0);
         if (role != IDLE)
             primal_at(S, hn ? stage_at(z0 + 1) : S, hn, ring + (z0 & 1) * 4 * NE, ustage_at(z0),
                       (uint32_t)z0 * wh + col, true, ubc, vbc, live(z0));
@@ -1627,9 +1643,9 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
         wait_u(t + 1);
         const int s1 = s0 + 1 == NS ? 0 : s0 + 1;
         const int s2 = s1 + 1 == NS ? 0 : s1 + 1;
-        const float* St = (const float*)(stages + s0 * STAGE);  // plane t
-        const float* S1 = (const float*)(stages + s1 * STAGE);  // plane t + 1
-        const float* S2 = (const float*)(stages + s2 * STAGE);  // plane t + 2
+        const T* St = (const T*)(stages + s0 * G::STAGE);  // plane t
+        const T* S1 = (const T*)(stages + s1 * G::STAGE);  // plane t + 1
+        const T* S2 = (const T*)(stages + s2 * G::STAGE);  // plane t + 2
         // A thread whose wait gave up skips the plane; the barrier below shares the
         // outcome and the whole block leaves together.
         if (ok) {
@@ -1685,7 +1701,7 @@ __device__ __forceinline__ void shifted_pass(const shp::Args& a, uint8_t* stages
     __syncthreads();
 }
 
-template <int DATA, int NS, bool MASKED>
+template <int PREC, int DATA, int NS, bool MASKED>
 __global__ void __launch_bounds__(shp::NTHREADS, 2)
     tgv_shifted_tma_kernel(const __grid_constant__ shp::Args a) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
@@ -1693,9 +1709,9 @@ __global__ void __launch_bounds__(shp::NTHREADS, 2)
     __shared__ uint64_t full[NS + shp::NU];
     // a pipeline wait of an earlier block or launch timed out: do nothing more
     if (__syncthreads_or(threadIdx.x == 0 ? *(volatile int*)a.err : 0)) return;
-    uint8_t* ustages = smem + NS * shp::STAGE;
+    uint8_t* ustages = smem + NS * shp::PQ<PREC>::STAGE;
     float* ring = (float*)(ustages + shp::NU * shp::USTAGE);
-    shifted_pass<DATA, NS, MASKED>(a, smem, ustages, ring, full, full + NS);
+    shifted_pass<PREC, DATA, NS, MASKED>(a, smem, ustages, ring, full, full + NS);
 }
 
 size_t elem_bytes(int precision) { return precision == TGVDCT_STATE_FP32 ? 4 : 2; }
@@ -2009,11 +2025,17 @@ void iterate_fused(TgvState& s, const TgvStep& k, cudaStream_t st) {
 // ---- the shifted passes: host side ----------------------------------------------------
 // Stages of p and q in flight: step t reads planes t .. t + 2, so SHIFTED_NS - 3 planes
 // land while it computes.
-constexpr int SHIFTED_NS = 5;
+// Stages of p and q in flight: step t reads planes t .. t + 2, so shifted_stages() - 3
+// planes land while it computes (two CTAs per SM: 110.8 KB of shared memory in FP32,
+// 91.0 KB with 16-bit duals).
+template <int PREC>
+constexpr int shifted_stages() {
+    return PREC == TGVDCT_STATE_FP32 ? 5 : 6;
+}
 
 bool shifted_ok(const TgvState& s) {
-    return s.kernel == TGV_KERNEL_SHIFTED && s.precision == TGVDCT_STATE_FP32 && s.three &&
-           s.D >= 2 && s.W % 4 == 0 && s.err &&
+    const int need = s.precision == TGVDCT_STATE_FP32 ? 4 : 8;  // 16-byte TMA strides
+    return s.kernel == TGV_KERNEL_SHIFTED && s.three && s.D >= 2 && s.W % need == 0 && s.err &&
            (uint64_t)s.W * s.H * s.D < (1ull << 32);  // 32-bit voxel indices
 }
 
@@ -2025,8 +2047,8 @@ bool shifted_ok(const TgvState& s) {
 struct ShiftedSlot {
     float* u;
     float* v[3];
-    float* p[3];
-    float* q[6];  // state order
+    void* p[3];  // the state's dual element type
+    void* q[6];  // state order
 };
 
 ShiftedSlot shifted_slot(const TgvState& s, int c, int parity) {
@@ -2035,9 +2057,9 @@ ShiftedSlot shifted_slot(const TgvState& s, int c, int parity) {
     r.u = parity ? s.set[c].ubar : s.u;
     for (int k = 0; k < 3; ++k) {
         r.v[k] = parity ? s.set[c].vbar[k] : s.v[k];
-        r.p[k] = (float*)F.p[k];
+        r.p[k] = F.p[k];
     }
-    for (int k = 0; k < 6; ++k) r.q[k] = (float*)F.q[k];
+    for (int k = 0; k < 6; ++k) r.q[k] = F.q[k];
     return r;
 }
 
@@ -2045,8 +2067,10 @@ struct ShiftedCache {
     shp::Args args[2][2];  // [c][parity of the input]: tensor maps and pointers of a pass
 };
 
+template <int PREC>
 ShiftedCache* shifted_cache(TgvState& s) {
     if (!s.shifted_cache) {
+        using G = shp::PQ<PREC>;
         auto cache = std::make_shared<ShiftedCache>();
         const int qmap[6] = {0, 1, 3, 2, 4, 5};  // kernel slot -> state order
         for (int c = 0; c < 2; ++c)
@@ -2055,11 +2079,12 @@ ShiftedCache* shifted_cache(TgvState& s) {
                 std::memset(&a, 0, sizeof(a));
                 const ShiftedSlot in = shifted_slot(s, c, par), out = shifted_slot(s, c, par ^ 1);
                 for (int k = 0; k < 3; ++k)
-                    encode_box(&a.maps.p[k], in.p[k], 4, s, shp::BW, shp::BH);
+                    encode_box(&a.maps.p[k], in.p[k], G::DES, s, G::BW, shp::BH);
                 for (int k = 0; k < 6; ++k)
-                    encode_box(&a.maps.q[k], in.q[qmap[k]], 4, s, shp::BW, shp::BH);
+                    encode_box(&a.maps.q[k], in.q[qmap[k]], G::DES, s, G::BW, shp::BH);
                 const float* uf[5] = {in.u, s.f, in.v[0], in.v[1], in.v[2]};
-                for (int k = 0; k < 5; ++k) encode_box(&a.maps.uf[k], uf[k], 4, s, shp::BW, shp::BH);
+                for (int k = 0; k < 5; ++k)
+                    encode_box(&a.maps.uf[k], uf[k], 4, s, shp::BW, shp::BH);
                 a.W = s.W;
                 a.H = s.H;
                 a.D = s.D;
@@ -2080,19 +2105,21 @@ ShiftedCache* shifted_cache(TgvState& s) {
 }
 
 // Raises the shared-memory limit of the shifted kernel on the current device, once.
-template <int DATA, bool MASKED>
+template <int PREC, int DATA, bool MASKED>
 void shifted_attr() {
+    constexpr int NS = shifted_stages<PREC>();
     static std::atomic<uint64_t> configured{0};  // per template instance
-    smem_attr_once((const void*)tgv_shifted_tma_kernel<DATA, SHIFTED_NS, MASKED>,
-                   shp::smem_bytes<SHIFTED_NS>(), configured);
+    smem_attr_once((const void*)tgv_shifted_tma_kernel<PREC, DATA, NS, MASKED>,
+                   shp::smem_bytes<NS, PREC>(), configured);
 }
 
-template <int DATA, bool MASKED>
+template <int PREC, int DATA, bool MASKED>
 void launch_shifted(const shp::Args& a, cudaStream_t st) {
-    constexpr int NS = SHIFTED_NS;
-    auto kern = tgv_shifted_tma_kernel<DATA, NS, MASKED>;
-    constexpr size_t smem = shp::smem_bytes<NS>();
-    shifted_attr<DATA, MASKED>();
+    constexpr int NS = shifted_stages<PREC>();
+    auto kern = tgv_shifted_tma_kernel<PREC, DATA, NS, MASKED>;
+    constexpr size_t smem = shp::smem_bytes<NS, PREC>();
+    static_assert(smem <= 113 * 1024, "two CTAs per SM");
+    shifted_attr<PREC, DATA, MASKED>();
     const dim3 grid(ceil_div(a.W, shp::TX), ceil_div(a.H, shp::TY), ceil_div(a.D, a.zchunk));
     kern<<<grid, shp::NTHREADS, smem, st>>>(a);
     TGV_CHECK_LAUNCH();
@@ -2102,16 +2129,16 @@ void launch_shifted(const shp::Args& a, cudaStream_t st) {
 // first, n - 1 shifted passes, the primal step of the last.  The standard state ends in
 // set c when n is even and in set c ^ 1 when n is odd (as after n single passes).
 // Returns the number of kernel launches.
+template <int PREC>
 int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) {
-    constexpr int FP = TGVDCT_STATE_FP32;
     const int c = s.cur;
-    ShiftedCache* cache = shifted_cache(s);
+    ShiftedCache* cache = shifted_cache<PREC>(s);
     const dim3 block(BX, BY, 1);
     const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
     {   // p^(n+1), q^(n+1) of the current state into set c ^ 1
         float* const v[3] = {s.v[0], s.v[1], s.v[2]};
-        const auto a = make_args<FP>(s, k, s.set[c], s.u, v, s.set[c ^ 1], s.u, v);
-        tgv_dual_kernel<FP, true><<<grid, block, 0, st>>>(a);
+        const auto a = make_args<PREC>(s, k, s.set[c], s.u, v, s.set[c ^ 1], s.u, v);
+        tgv_dual_kernel<PREC, true><<<grid, block, 0, st>>>(a);
         TGV_CHECK_LAUNCH();
     }
     for (uint32_t j = 0; j + 1 < n; ++j) {
@@ -2123,6 +2150,10 @@ int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) 
         a.tau_lambda = k.tau * k.lambda;
         a.alpha0 = k.alpha0;
         a.alpha1 = k.alpha1;
+        a.penc = 32767.f / k.alpha1;
+        a.pdec = k.alpha1 / 32767.f;
+        a.qenc = 32767.f / k.alpha0;
+        a.qdec = k.alpha0 / 32767.f;
         a.thr_p = projection_skip_bound(k.alpha1);
         a.thr_q = projection_skip_bound(k.alpha0);
         a.skip_bz = (k.data_term == TGVDCT_DATA_L2 && s.D == 1) ? 1 : 0;
@@ -2133,11 +2164,11 @@ int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) 
                                                                                   : nullptr;
         const bool m = a.dom != nullptr;
         if (k.data_term == TGVDCT_DATA_L1) {
-            if (m) launch_shifted<TGVDCT_DATA_L1, true>(a, st);
-            else launch_shifted<TGVDCT_DATA_L1, false>(a, st);
+            if (m) launch_shifted<PREC, TGVDCT_DATA_L1, true>(a, st);
+            else launch_shifted<PREC, TGVDCT_DATA_L1, false>(a, st);
         } else {
-            if (m) launch_shifted<TGVDCT_DATA_L2, true>(a, st);
-            else launch_shifted<TGVDCT_DATA_L2, false>(a, st);
+            if (m) launch_shifted<PREC, TGVDCT_DATA_L2, true>(a, st);
+            else launch_shifted<PREC, TGVDCT_DATA_L2, false>(a, st);
         }
     }
     {   // the primal step of the last iteration, into the standard state: u, v to their
@@ -2147,11 +2178,11 @@ int iterate_shifted(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) 
         const int set = par ? c : c ^ 1;
         float* const v_in[3] = {d.v[0], d.v[1], d.v[2]};
         float* const v_out[3] = {s.v[0], s.v[1], s.v[2]};
-        const auto a = make_args<FP>(s, k, s.set[set], d.u, v_in, s.set[set], s.u, v_out);
+        const auto a = make_args<PREC>(s, k, s.set[set], d.u, v_in, s.set[set], s.u, v_out);
         if (k.data_term == TGVDCT_DATA_L1)
-            tgv_primal_kernel<FP, true, TGVDCT_DATA_L1><<<grid, block, 0, st>>>(a);
+            tgv_primal_kernel<PREC, true, TGVDCT_DATA_L1><<<grid, block, 0, st>>>(a);
         else
-            tgv_primal_kernel<FP, true, TGVDCT_DATA_L2><<<grid, block, 0, st>>>(a);
+            tgv_primal_kernel<PREC, true, TGVDCT_DATA_L2><<<grid, block, 0, st>>>(a);
         TGV_CHECK_LAUNCH();
         s.cur = set;
     }
@@ -2460,17 +2491,32 @@ int tgv_kernels_per_iteration(const TgvState& s) { return s.kernel == TGV_KERNEL
 bool tgv_uses_shifted(const TgvState& s) { return shifted_ok(s); }
 
 int tgv_iterate_n(TgvState& s, const TgvStep& k, uint32_t n, cudaStream_t st) {
-    if (n >= 2 && shifted_ok(s)) return iterate_shifted(s, k, n, st);
+    if (n >= 2 && shifted_ok(s)) {
+        switch (s.precision) {
+            case TGVDCT_STATE_FP32: return iterate_shifted<TGVDCT_STATE_FP32>(s, k, n, st);
+            case TGVDCT_STATE_BF16_DUAL: return iterate_shifted<TGVDCT_STATE_BF16_DUAL>(s, k, n, st);
+            case TGVDCT_STATE_FX16_DUAL: return iterate_shifted<TGVDCT_STATE_FX16_DUAL>(s, k, n, st);
+        }
+    }
     for (uint32_t i = 0; i < n; ++i) tgv_iterate(s, k, st);
     return (int)n * tgv_kernels_per_iteration(s);
 }
 
+template <int PREC>
+void prepare_shifted() {
+    shifted_attr<PREC, TGVDCT_DATA_L1, false>();
+    shifted_attr<PREC, TGVDCT_DATA_L2, false>();
+    shifted_attr<PREC, TGVDCT_DATA_L1, true>();
+    shifted_attr<PREC, TGVDCT_DATA_L2, true>();
+}
+
 void tgv_prepare_launches(const TgvState& s) {
     if (!shifted_ok(s)) return;
-    shifted_attr<TGVDCT_DATA_L1, false>();
-    shifted_attr<TGVDCT_DATA_L2, false>();
-    shifted_attr<TGVDCT_DATA_L1, true>();
-    shifted_attr<TGVDCT_DATA_L2, true>();
+    switch (s.precision) {
+        case TGVDCT_STATE_FP32: prepare_shifted<TGVDCT_STATE_FP32>(); break;
+        case TGVDCT_STATE_BF16_DUAL: prepare_shifted<TGVDCT_STATE_BF16_DUAL>(); break;
+        case TGVDCT_STATE_FX16_DUAL: prepare_shifted<TGVDCT_STATE_FX16_DUAL>(); break;
+    }
 }
 
 }  // namespace tgvdct

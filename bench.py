@@ -43,8 +43,8 @@ WORKLOADS = {
 # vbar3, p3, q6; write u, ubar, v3, vbar3, p3, q6), by state precision
 ALGO_BYTES = {0: 140, 1: 104, 2: 104}
 # the shifted pass (primal of one iteration, dual of the next) keeps ubar and vbar on
-# chip: read f, u, v3, p3, q6, write u, v3, p3, q6 (FP32 state only)
-ALGO_BYTES_SHIFTED = 108
+# chip: read f, u, v3, p3, q6, write u, v3, p3, q6 (p, q in the dual element size)
+ALGO_BYTES_SHIFTED = {0: 108, 1: 72, 2: 72}
 KERNELS = {"shifted": 4, "fused": 2, "two_pass": 1}
 # the kernel a roofline line times, per --kernel
 KERNEL_NAMES = {"shifted": "tgv_shifted_tma_kernel", "fused": "tgv_fused_tma_kernel",
@@ -53,7 +53,7 @@ KERNEL_NAMES = {"shifted": "tgv_shifted_tma_kernel", "fused": "tgv_fused_tma_ker
 
 def algo_bytes(kernel, precision):
     """Algorithmic bytes per voxel-iteration of the iteration kernel that runs."""
-    return ALGO_BYTES_SHIFTED if (kernel, precision) == ("shifted", 0) else ALGO_BYTES[precision]
+    return (ALGO_BYTES_SHIFTED if kernel == "shifted" else ALGO_BYTES)[precision]
 # the extra measurements a default run adds to its line, in the order they run
 EXTRAS = ["iteration_variants", "dct_poisson_256cube", "adjoint", "adjoint_256x256x192",
           "other_configs", "downsampled_deshade", "masked_deshade", "accuracy_vs_fp64"]
@@ -210,13 +210,13 @@ TRAFFIC_256x256x192 = {("fused", 0): 914891776 + 801782528,
                        ("shifted", 0): 715630000 + 606720000}
 
 
-def time_shifted_pass(pkg, torch, w, h, d, f, stream, n_pass=100):
+def time_shifted_pass(pkg, torch, w, h, d, f, stream, precision=0, n_pass=100):
     """Milliseconds per launch of the shifted pass: tgvdct_tgv2_step_dev runs n iterations
     as one dual step, n - 1 shifted passes and one primal step, so the difference of
     runs of n_pass + 2 and 2 iterations is n_pass launches of the pass alone (CUDA events
     on `stream`)."""
     prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=1,
-                             iteration_kernel=KERNELS["shifted"])
+                             state_precision=precision, iteration_kernel=KERNELS["shifted"])
     L = pkg.lib()
     sh = ctypes.c_void_p(stream.cuda_stream)
     with pkg.Context(prm) as ctx:
@@ -512,9 +512,8 @@ def run_ours(args):
                             args.profile_iterations, stream)
     launches_per_it = 2 if args.kernel == "two_pass" else 1
     launch_ms = it_ms / launches_per_it
-    shifted = (args.kernel, args.precision) == ("shifted", 0)
-    if shifted:  # the pass itself, without the dual and primal steps around each run
-        launch_ms = time_shifted_pass(pkg, torch, w, h, d, f, stream)
+    if args.kernel == "shifted":  # the pass alone, without the steps around each run
+        launch_ms = time_shifted_pass(pkg, torch, w, h, d, f, stream, args.precision)
     peak, peak_kind = hbm_peak()
     algo = algo_bytes(args.kernel, args.precision)
     # algorithmic bytes of one iteration per second of the dominant kernel
@@ -554,7 +553,8 @@ def run_ours(args):
             if "iteration_variants" in want:
                 var = {}
                 for kernel, prec in (("two_pass", 0), ("fused", 0), ("shifted", 0),
-                                     ("two_pass", 2), ("fused", 2), ("fused", 1)):
+                                     ("two_pass", 2), ("fused", 2), ("fused", 1),
+                                     ("shifted", 2), ("shifted", 1)):
                     t = time_iterations(pkg, torch, w, h, d, f, kernel, prec, 200, stream)
                     var[f"{kernel}_{PREC_NAMES[prec]}"] = {
                         "ms_per_iteration": t, "voxel_iters_per_s": V / (t * 1e-3),

@@ -7,7 +7,7 @@ sequence as in the two-pass and fused kernels, so the results must be bit-identi
 theirs: for both parities of a run, every z-chunking, shapes whose blocks all touch the
 volume's faces and shapes with blocks that run without boundary tests, both data terms,
 callbacks between runs, CUDA graph replays of long runs, the stepping entry point and
-the state snapshot, and masked runs (frozen voxels outside the domain)."""
+the state snapshot, masked runs (frozen voxels outside the domain) and 16-bit duals."""
 import ctypes
 
 import numpy as np
@@ -43,6 +43,20 @@ def test_runs_equal_two_pass(gpu_lib, iterations, shape, z_chunk):
     f = tissue_phantom_3d(*shape, seed=21)
     ref = _process(f, pkg.KERNEL_TWO_PASS, iterations)
     _equal(ref, _process(f, pkg.KERNEL_FUSED_SHIFTED, iterations, z_chunk=z_chunk))
+
+
+@pytest.mark.parametrize("prec", [pkg.STATE_FX16_DUAL, pkg.STATE_BF16_DUAL])
+@pytest.mark.parametrize("iterations", [2, 5])
+@pytest.mark.parametrize("shape,z_chunk", [((9, 26, 104), 2), ((12, 40, 136), 0),
+                                           ((3, 20, 40), 1)])
+def test_16bit_duals_equal_two_pass(gpu_lib, prec, iterations, shape, z_chunk):
+    # p, q stored in 16 bits (widths a multiple of 8 for the TMA strides), every update
+    # in FP32: the same rounding of the stored duals as the other kernels
+    f = tissue_phantom_3d(*shape, seed=28)
+    ref = _process(f, pkg.KERNEL_TWO_PASS, iterations, state_precision=prec)
+    _equal(ref, _process(f, pkg.KERNEL_FUSED_SHIFTED, iterations, state_precision=prec,
+                         z_chunk=z_chunk))
+    _equal(ref, _process(f, pkg.KERNEL_FUSED, iterations, state_precision=prec))
 
 
 # extreme shapes: one row, a width of 4 (one column of TMA alignment), two planes,
