@@ -444,6 +444,8 @@ def time_adjoint(pkg, torch, stream, shape=(96, 96, 96), K=200, every=20):
             torch.cuda.synchronize()
             out[name + "_ms"] = e0.elapsed_time(e1)
     out["backward_over_forward"] = out["backward_ms"] / out["forward_ms"]
+    # the forward a gradient computation runs: the same loop keeping its checkpoints
+    out["backward_over_forward_checkpointed"] = out["backward_ms"] / out["forward_checkpointed_ms"]
     out["workload"] = f"{w}x{h}x{d}, K = {K}, checkpoints every {every}"
     return out
 
