@@ -1249,11 +1249,12 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
 // (u, ubar, v, vbar from u^n, v^n, f and the stencils of p^(n+1), q^(n+1)) and then the
 // dual step of iteration n + 1 (p^(n+2), q^(n+2) from the stencils of ubar^(n+1),
 // vbar^(n+1) and the own p^(n+1), q^(n+1)).  ubar and vbar never leave the chip, so a
-// voxel-iteration moves u, v, p, q, f in (14 floats) and u, v, p, q out (13): 108
-// bytes, against 140 for the pass that starts with the dual step.  Every update is the
-// same arithmetic in the same order as in the other kernels (bit-identical results).
-// A dual step (tgv_dual_kernel) before the first pass and a primal step
-// (tgv_primal_kernel) after the last convert the loop state to this form and back.
+// voxel-iteration moves u, v, p, q, f in (14 values) and u, v, p, q out (13): 108 bytes
+// in FP32 (72 with p, q in 16 bits), against 140 for the pass that starts with the dual
+// step.  Every update is the same arithmetic in the same order as in the other kernels
+// (bit-identical results).  A dual step (tgv_dual_kernel) before the first pass and a
+// primal step (tgv_primal_kernel) after the last convert the loop state to this form
+// and back.
 //
 // A block owns a 32 x 8 column tile and marches along z through its planes.  Step t
 // computes the primal of plane t + 1, then the dual of plane t:
@@ -1264,12 +1265,15 @@ __global__ void __launch_bounds__(tma::NTHREADS, 2)
 //                      differences read
 // ubar and vbar pass through a two-plane shared-memory ring: the dual of plane t reads
 // plane t's, written one step earlier; the own values of planes t - 1 .. t + 1 stay in
-// registers.  p and q of every plane arrive by TMA as 40 x 10 boxes (x0 - 4 .. x0 + 35,
-// y0 - 1 .. y0 + 8) into a ring of NS stages, completing on the stage's mbarrier; step t
-// reads planes t .. t + 2, so NS - 3 planes are in flight while it computes.  u, f and v
-// arrive the same way into a ring of NU stages of their own (step t reads plane t + 1,
-// so NU - 1 planes are in flight); no thread loads from global memory.  The block meets
-// one barrier per plane.
+// registers.  p and q of every plane arrive by TMA as boxes of rows y0 - 1 .. y0 + 8
+// and columns x0 - 4 .. x0 + 35 (FP32) or x0 - 8 .. x0 + 39 (16-bit) into a ring of NS
+// stages, completing on the stage's mbarrier; step t reads planes t .. t + 2, so NS - 3
+// planes are in flight while it computes.  u, f and v arrive the same way (40 x 10 FP32
+// boxes) into a ring of NU stages of their own (step t reads plane t + 1, so NU - 1
+// planes are in flight); no thread loads from global memory.  The block meets one
+// barrier per plane.  The masked instance reads each voxel's domain flag per plane:
+// outside the domain the primal step passes the frozen ubar = u, vbar = 0 to the ring
+// and stores nothing, and the dual step is skipped (p = q = 0 already).
 namespace shp {
 
 constexpr int TX = 32, TY = 8;
