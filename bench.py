@@ -524,7 +524,7 @@ def run_ours(args):
         if args.workload == "deshade_256x256x192" else None
 
     # ---- e2e through the host-buffer C-ABI call (reference-facing)
-    e2e_ms, e2e_calls = None, []
+    e2e_ms, e2e_calls, e2e_clocks = None, [], None
     if not args.no_e2e:
         # pinned host buffers (numpy views of page-locked torch tensors), as a caller
         # streaming volumes through the library would hold them
@@ -532,15 +532,16 @@ def run_ours(args):
         pinned += [torch.empty(f_host.shape, dtype=torch.float32).pin_memory() for _ in range(3)]
         fh, uo, lo, ro = (t.numpy() for t in pinned)
         times = []
-        for k in range(args.e2e_steps + 1):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            st = pkg.lib().tgvdct_process_tgv2_l1(ctypes.byref(prm), fh, None, 0, 0, 1,
-                                                  pkg.CALLBACK(), None, uo, lo, ro)
-            torch.cuda.synchronize()
-            if st != pkg.OK:
-                raise RuntimeError(pkg.lib().tgvdct_last_error().decode())
-            times.append(time.perf_counter() - t0)
+        with ClockSampler(local) as e2e_clocks:
+            for k in range(args.e2e_steps + 1):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                st = pkg.lib().tgvdct_process_tgv2_l1(ctypes.byref(prm), fh, None, 0, 0, 1,
+                                                      pkg.CALLBACK(), None, uo, lo, ro)
+                torch.cuda.synchronize()
+                if st != pkg.OK:
+                    raise RuntimeError(pkg.lib().tgvdct_last_error().decode())
+                times.append(time.perf_counter() - t0)
         e2e_calls = [round(1e3 * t, 3) for t in times]  # the first builds the context
         e2e_ms = 1e3 * float(np.median(times[1:]))
     if not args.no_e2e:
@@ -604,6 +605,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "voxel-iter/s",
                     "h2d_bytes_per_step": V * 4, "d2h_bytes_per_step": 3 * V * 4,
                     "ms_per_step": e2e_ms, "call_ms": e2e_calls,
+                    "clocks": e2e_clocks.summary() if e2e_clocks else None,
                     "call": "tgvdct_process_tgv2_l1, pinned host buffers; the library keeps "
                             "its context between calls (the first, untimed call builds it)"},
             "gpu_launches": gpu_launches * args.steps,
