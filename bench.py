@@ -381,7 +381,7 @@ def time_masked(pkg, torch, stream):
     """The masked deshade (TGVDeshadeMaskedProcessor) of the 256x256x192 tissue phantom
     with an ellipsoid mask (38% of the voxels inside), 1500 iterations, the clamp
     and the background add-back, device-timed; the loop runs the masked instance of
-    the fused TMA kernel."""
+    the shifted pass."""
     import numpy as np
     from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
     d, h, w = 192, 256, 256
