@@ -27,7 +27,8 @@ def _run(f, kernel, iterations, precision=pkg.STATE_FP32):
 @pytest.mark.parametrize("shape,iterations", [((192, 256, 256), 40), ((256, 512, 512), 8)])
 def test_fused_equals_two_pass_at_full_size(gpu_lib, shape, iterations):
     """The benchmark volume, and a 512x512x256 volume (67 M voxels, 8.3 GB of state):
-    the TMA-pipelined fused kernel and the two-pass kernels give identical bits."""
+    the shifted passes, the TMA-pipelined fused kernel and the two-pass kernels give
+    identical bits."""
     import torch
     if shape[0] <= 192:
         f = torch.from_numpy(np.log(tissue_phantom_3d(*shape, seed=2))).cuda()
@@ -36,8 +37,9 @@ def test_fused_equals_two_pass_at_full_size(gpu_lib, shape, iterations):
         f = torch.randn(shape, generator=g, device="cuda", dtype=torch.float32)
     a = _run(f, pkg.KERNEL_FUSED, iterations)
     b = _run(f, pkg.KERNEL_TWO_PASS, iterations)
-    for x, y in zip(a, b):
-        assert torch.equal(x, y)
+    c = _run(f, pkg.KERNEL_FUSED_SHIFTED, iterations)
+    for x, y, z in zip(a, b, c):
+        assert torch.equal(x, y) and torch.equal(x, z)
 
 
 def test_poisson_identity_at_256_cubed(gpu_lib):
