@@ -1,7 +1,7 @@
 """Bounded pipeline waits that run out on the GPU, on purpose and without a fault.
 
-The fused TMA iteration kernel and the pipelined tensor-core DCT passes wait on
-mbarriers for their staged data.  Every such wait is bounded; when one runs out the
+The fused and shifted TMA iteration kernels and the pipelined tensor-core DCT passes
+wait on mbarriers for their staged data.  Every such wait is bounded; when one runs out the
 kernel raises the context's device error flag, lets its own copies (and tensor-core
 operations) in flight finish, and returns, and later launches return at once.  Here
 the limit is set to 0 with tgvdct_set_pipeline_wait_limit, so the first wait that
@@ -54,6 +54,48 @@ def test_iteration_pipeline_wait_runs_out_and_the_context_recovers(gpu_lib):
         fresh.check_device_error()
     for a, b in zip(out, ref):
         assert torch.equal(a, b)
+
+
+def test_shifted_pass_wait_runs_out_and_the_context_recovers(gpu_lib):
+    """The shifted passes (p, q ring and u, f, v ring): five iterations through the
+    stepping entry point are one dual step, four shifted passes and one primal step, so
+    the first kernel that waits on a pipeline is a shifted pass.  Its waits give up, its
+    producer drains both rings, and the context then reproduces a fresh one's state."""
+    import ctypes
+    import torch
+    D, H, W = 40, 48, 64
+    f = torch.from_numpy(np.log(tissue_phantom_3d(D, H, W, seed=9))).cuda()
+    prm = pkg.default_params(width=W, height=H, depth=D, iteration_count=1,
+                             iteration_kernel=pkg.KERNEL_FUSED_SHIFTED)
+    L = pkg.lib()
+
+    def run(ctx):
+        assert L.tgvdct_state_init_dev(ctx._ctx, ctypes.c_void_p(f.data_ptr()), None) == pkg.OK
+        assert L.tgvdct_tgv2_step_dev(ctx._ctx, 5, None) == pkg.OK
+        assert ctx.loop_launches() == 6
+
+    def snapshot(ctx):
+        buf = torch.empty(ctx.state_bytes() // 4 + 1, dtype=torch.float32, device="cuda")
+        ctx.save_state_dev(buf.data_ptr())
+        torch.cuda.synchronize()
+        return buf
+
+    with pkg.Context(prm) as ctx:
+        ctx.set_pipeline_wait_limit(0)
+        run(ctx)
+        _expect_timeout(ctx)
+        ctx.check_device_error()  # cleared by the report
+        ctx.set_pipeline_wait_limit(DEFAULT_NS)
+        run(ctx)
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+        got = snapshot(ctx)
+    with pkg.Context(prm) as fresh:
+        run(fresh)
+        torch.cuda.synchronize()
+        fresh.check_device_error()
+        ref = snapshot(fresh)
+    assert torch.equal(got, ref)
 
 
 @pytest.mark.parametrize("mode", [pkg.DCT_BF16X3, pkg.DCT_TF32])
