@@ -2215,17 +2215,18 @@ tgvdct_status tgvdct_request_stop(tgvdct_context* c) {
 }
 
 tgvdct_status tgvdct_bounds_check(uint64_t* first_bad) {
-    return guarded([&] {
+    return guarded([&]() -> tgvdct_status {
         TGV_REQUIRE(first_bad != nullptr, "null output");
-        if (!kCheckBounds) {
+        if constexpr (kCheckBounds) {
+            TGV_CUDA(cudaDeviceSynchronize());
+            const uint64_t w[3] = {tgv_kernels_bounds_take(), adjoint_bounds_take(),
+                                   resize_bounds_take()};
+            *first_bad = w[0] ? w[0] : w[1] ? w[1] : w[2];
+            return TGVDCT_OK;
+        } else {
             set_error("this library is built without bounds checks (libtgvdct_checked.so has them)");
             throw Error{TGVDCT_ERR_UNSUPPORTED};
         }
-        TGV_CUDA(cudaDeviceSynchronize());
-        const uint64_t w[3] = {tgv_kernels_bounds_take(), adjoint_bounds_take(),
-                               resize_bounds_take()};
-        *first_bad = w[0] ? w[0] : w[1] ? w[1] : w[2];
-        return TGVDCT_OK;
     });
 }
 
