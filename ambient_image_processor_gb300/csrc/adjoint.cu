@@ -41,6 +41,7 @@ struct AdjArgs {
     TgvFullDev S;   // S_k
     TgvFullDev S1;  // S_{k+1}
     TgvFullDev A;   // in: adjoint of S_{k+1}; out: adjoint of S_k (in place)
+    TgvFullDev Ao;  // the fused pass's output: a(u), a(v), a(p), a(q) of S_k (A is its input)
     float* uta;     // a(u~)
     float* va[3];   // a(v')
     float* grad_f;
@@ -48,6 +49,7 @@ struct AdjArgs {
     float tau, sigma, theta, tau_lambda, alpha0, alpha1;
     int data_term, skip_bz;
     int zm;  // planes per thread of the z-marching kernels
+    int zc;  // planes per block of the fused pass
 };
 
 __device__ __forceinline__ void block_add(double* dst, float v) {
@@ -77,10 +79,15 @@ struct R1In {
     float uo, fi;       // S.u[i], f[i]
 };
 
-// R1 at voxel i, with a(ubar) and a(vbar) of S_{k+1} given: returns the d/dlambda term.
-__device__ __forceinline__ float r1_vals(const AdjArgs& a, size_t i, const R1In& in, float aub,
-                                         const float* avb) {
-    float glam = 0.f;
+// R1's u part at one voxel, from a(u) and a(ubar) of S_{k+1}: a(u~), the new a(u), the
+// d/df term and the d/dlambda term.
+struct R1U {
+    float uta, au, gf, glam;
+};
+__device__ __forceinline__ R1U r1_u(const AdjArgs& a, const R1In& in, float au_in, float aub) {
+    R1U o;
+    o.glam = 0.f;
+    o.gf = 0.f;
     // u~ exactly as the forward primal pass computed it
     const float bx = in.px - in.p0;
     const float by = in.py - in.p1;
@@ -88,36 +95,52 @@ __device__ __forceinline__ float r1_vals(const AdjArgs& a, size_t i, const R1In&
     const float bz = in.pz - in.p2;
     if (!a.skip_bz) div = div + bz;
     const float ut = in.uo - a.tau * div;
-    const float ua = a.A.u[i] + (1.f + a.theta) * aub;
-    float uta, gf = 0.f;
+    const float ua = au_in + (1.f + a.theta) * aub;
+    float uta;
     if (a.data_term == TGVDCT_DATA_L1) {
         const float dd = ut - in.fi;
         if (dd > a.tau_lambda) {
             uta = ua;
-            glam = -a.tau * ua;
+            o.glam = -a.tau * ua;
         } else if (dd < -a.tau_lambda) {
             uta = ua;
-            glam = a.tau * ua;
+            o.glam = a.tau * ua;
         } else {
             uta = 0.f;
-            gf = ua;
+            o.gf = ua;
         }
     } else {
         const float den = 1.f + a.tau_lambda;
         uta = ua / den;
-        gf = a.tau_lambda * ua / den;
-        glam = ua * a.tau * (in.fi - ut) / (den * den);
+        o.gf = a.tau_lambda * ua / den;
+        o.glam = ua * a.tau * (in.fi - ut) / (den * den);
     }
-    a.A.u[i] = -a.theta * aub + uta;
-    a.uta[i] = uta;
-    if (gf != 0.f) a.grad_f[i] += gf;
+    o.au = -a.theta * aub + uta;
+    o.uta = uta;
+    return o;
+}
+// R1's v part, one component: a(v') from a(v) and a(vbar) of S_{k+1}, then the new a(v).
+__device__ __forceinline__ float r1_va(const AdjArgs& a, float av_in, float avb) {
+    return av_in + (1.f + a.theta) * avb;
+}
+__device__ __forceinline__ float r1_av(const AdjArgs& a, float va, float avb) {
+    return va - a.theta * avb;
+}
+
+// R1 at voxel i, with a(ubar) and a(vbar) of S_{k+1} given: returns the d/dlambda term.
+__device__ __forceinline__ float r1_vals(const AdjArgs& a, size_t i, const R1In& in, float aub,
+                                         const float* avb) {
+    const R1U o = r1_u(a, in, a.A.u[i], aub);
+    a.A.u[i] = o.au;
+    a.uta[i] = o.uta;
+    if (o.gf != 0.f) a.grad_f[i] += o.gf;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float va = a.A.v[c][i] + (1.f + a.theta) * avb[c];
+        const float va = r1_va(a, a.A.v[c][i], avb[c]);
         a.va[c][i] = va;
-        a.A.v[c][i] = va - a.theta * avb[c];
+        a.A.v[c][i] = r1_av(a, va, avb[c]);
     }
-    return glam;
+    return o.glam;
 }
 
 // R3 inputs at voxel i: a(p) with its -x, -y, -z neighbours, a(q) with the +x, +y, +z
@@ -132,14 +155,16 @@ struct R3In {
 };
 
 // R3 at voxel i: a(ubar) and a(vbar) of S_k from a(p), a(q) (after R2).
-__device__ __forceinline__ void r3_vals(const AdjArgs& a, bool xl, bool yl, bool zl,
-                                        const R3In& in, float& aub, float* avb) {
-    // a(ubar) = sigma sum_c F_c^T a(p)_c
+// a(ubar) = sigma sum_c F_c^T a(p)_c (reads p0..p2 and px, py, pz)
+__device__ __forceinline__ float r3_aub(const AdjArgs& a, bool xl, bool yl, bool zl,
+                                        const R3In& in) {
     const float ftx = in.px - (xl ? in.p0 : 0.f);
     const float fty = in.py - (yl ? in.p1 : 0.f);
     const float ftz = in.pz - (zl ? in.p2 : 0.f);
-    aub = a.sigma * ((ftx + fty) + ftz);
-    // a(vbar)_c = -sigma a(p)_c + sigma sum_a w B_a^T a(q)_{c a}
+    return a.sigma * ((ftx + fty) + ftz);
+}
+// a(vbar)_c = -sigma a(p)_c + sigma sum_a w B_a^T a(q)_{c a} (reads p0..p2 and the q values)
+__device__ __forceinline__ void r3_avb(const AdjArgs& a, const R3In& in, float* avb) {
     const float* q = in.q;  // xx yy zz xy xz yz
     const float ex = (in.qx0 - q[0]) + 0.5f * (in.qy3 - q[3]) + 0.5f * (in.qz4 - q[4]);
     const float ey = 0.5f * (in.qx3 - q[3]) + (in.qy1 - q[1]) + 0.5f * (in.qz5 - q[5]);
@@ -147,6 +172,11 @@ __device__ __forceinline__ void r3_vals(const AdjArgs& a, bool xl, bool yl, bool
     avb[0] = -a.sigma * in.p0 + a.sigma * ex;
     avb[1] = -a.sigma * in.p1 + a.sigma * ey;
     avb[2] = -a.sigma * in.p2 + a.sigma * ez;
+}
+__device__ __forceinline__ void r3_vals(const AdjArgs& a, bool xl, bool yl, bool zl,
+                                        const R3In& in, float& aub, float* avb) {
+    aub = r3_aub(a, xl, yl, zl, in);
+    r3_avb(a, in, avb);
 }
 
 // The in-plane loads of R1 and R3 (the z neighbours are passed in).
@@ -286,10 +316,12 @@ struct R2In {
     float vb0[3], vbx[3], vby[3], vbz[3];
 };
 
-// R2 at voxel i: the projection Jacobians; accumulates d/dalpha0, d/dalpha1.
+// R2 at voxel i: the projection Jacobians, written to `out`; accumulates d/dalpha0,
+// d/dalpha1.
 __device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, const R2Pw& P, bool xl,
                                         bool yl, bool zl, bool xf, bool yf, bool zf,
-                                        const R2In& L, float& ga0, float& ga1) {
+                                        const R2In& L, float& ga0, float& ga1,
+                                        const TgvFullDev& out) {
     // a(p') = a(p) + tau a(v') - tau B^T a(u~)
     const float bt[3] = {(xl ? L.utx : 0.f) - L.ut0, (yl ? L.uty : 0.f) - L.ut0,
                          (zl ? L.utz : 0.f) - L.ut0};
@@ -358,9 +390,9 @@ __device__ __forceinline__ void r2_vals(const AdjArgs& a, size_t i, const R2Pw& 
         ga0 += yg / nq;
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) a.A.p[c][i] = pa[c];
+    for (int c = 0; c < 3; ++c) out.p[c][i] = pa[c];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a.A.q[k][i] = qa[k];
+    for (int k = 0; k < 6; ++k) out.q[k][i] = qa[k];
 }
 
 // The in-plane loads of R2 (the z neighbours are set by the caller).
@@ -404,7 +436,7 @@ __global__ void __launch_bounds__(BX* BY) adjoint_r2(AdjArgs a) {
         }
         R2Pw P;
         r2_pw_load(a, i, P);
-        r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
+        r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1, a.A);
     }
     block_add(&a.gp[1], ga0);
     block_add(&a.gp[2], ga1);
@@ -457,7 +489,7 @@ __global__ void __launch_bounds__(BX* BY, 3) adjoint_r2_zm(AdjArgs a) {
             r2_load(a, i, xl, yl, xf, yf, L);
             L.utz = zl ? a.uta[i + WH] : 0.f;
             L.ubz = zl ? a.S.ubar[i + WH] : 0.f;
-            r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1);
+            r2_vals(a, i, P, xl, yl, zl, xf, yf, zf, L, ga0, ga1, a.A);
             P = Pn;
             L.ut0 = L.utz;
             L.u0 = L.ubz;
@@ -468,6 +500,260 @@ __global__ void __launch_bounds__(BX* BY, 3) adjoint_r2_zm(AdjArgs a) {
             }
         }
     }
+    block_add(&a.gp[1], ga0);
+    block_add(&a.gp[2], ga1);
+}
+
+// ---- the fused pass: R3 of iteration k, then R1 and R2 of iteration k - 1 ----------
+//
+// R2 at voxel i reads a(u~) at i and its +x, +y, +z neighbours and a(v') at i and its
+// -x, -y, -z neighbours, both made by R1 of the same iteration; R1 is pointwise in the
+// a(ubar), a(vbar) that R3 of the iteration after makes.  One block owns a 32 x 8 column
+// tile and marches its planes along z: at step s it runs R3.R1 on plane s and R2 on
+// plane s - 1, so a(u~) and a(v') stay on chip (a three-plane shared ring for the
+// in-plane neighbours, registers for the z neighbours).  Three more warps run the
+// R3.R1 parts that the tile's R2 needs just outside it: a(u~) on the +x column and the
+// +y row, a(v') on the -x column and the -y row.  A block's first step makes a(v') of
+// the plane below its chunk and its last a(u~) of the plane above.  The pass reads the
+// adjoint state A and writes a second one, Ao, because the rim threads read A at voxels
+// that a neighbouring block updates.  Per voxel it moves 44 fields: A (13) and S_k.p (3),
+// S_{k-1}'s u, ubar, vbar, p, q (14) and f read, Ao (13) written, d/df updated where
+// the prox is inactive; R3.R1 and R2 as separate passes moved 61.  Each update is the
+// same sequence of operations as in adjoint_r3r1 and adjoint_r2, so the results are
+// bit-identical.
+//
+// Loads are plain global loads, each phase's issued before its first store (R2's before
+// the plane barrier), with the fields of the next plane prefetched into L2.  The pass
+// is bound by load latency at two blocks (22 warps) per SM: at 256 x 256 x 192 it takes
+// 0.55 ms against 0.57 ms for R3.R1 and R2 as separate passes.  Staging the inputs in
+// shared memory with per-thread 4-byte asynchronous copies (cp.async) was slower (0.89
+// ms): the copies cost as many memory instructions as the loads and queued behind the
+// shared-memory reads.
+namespace fz {
+constexpr int TX = 32, TY = 8;
+constexpr int NTHREADS = TX * TY + 96;  // eight tile warps, three rim warps
+constexpr int SX = TX + 1, SY = TY + 1;   // a plane of the tile with one rim row and column
+constexpr int RING = 3;
+enum Role { TILE, RIM_U, RIM_V, IDLE };
+}  // namespace fz
+
+// a(u~) at voxel i of A and S_{k-1} (R3's a(ubar) part, R1's u part), nothing stored.
+__device__ __forceinline__ float fused_uta(const AdjArgs& a, size_t i, bool xf, bool yf,
+                                           bool zf, bool xl, bool yl, bool zl) {
+    const size_t W = a.W, WH = a.WH;
+    R3In r3;
+    r3.p0 = a.A.p[0][i];
+    r3.p1 = a.A.p[1][i];
+    r3.p2 = a.A.p[2][i];
+    r3.px = xf ? a.A.p[0][i - 1] : 0.f;
+    r3.py = yf ? a.A.p[1][i - W] : 0.f;
+    r3.pz = zf ? a.A.p[2][i - WH] : 0.f;
+    const float aub = r3_aub(a, xl, yl, zl, r3);
+    R1In r1;
+    r1_load(a, i, xf, yf, r1);
+    r1.pz = zf ? a.S1.p[2][i - WH] : 0.f;
+    return r1_u(a, r1, a.A.u[i], aub).uta;
+}
+
+// a(v') at voxel i (R3's a(vbar) part, R1's v part), nothing stored.
+__device__ __forceinline__ void fused_va(const AdjArgs& a, size_t i, bool xl, bool yl, bool zl,
+                                         float* va) {
+    const size_t W = a.W, WH = a.WH;
+    const float* const* P = a.A.p;
+    const float* const* Q = a.A.q;
+    R3In r3;
+    r3.p0 = P[0][i];
+    r3.p1 = P[1][i];
+    r3.p2 = P[2][i];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r3.q[k] = Q[k][i];
+    r3.qx0 = xl ? Q[0][i + 1] : 0.f;
+    r3.qx3 = xl ? Q[3][i + 1] : 0.f;
+    r3.qx4 = xl ? Q[4][i + 1] : 0.f;
+    r3.qy3 = yl ? Q[3][i + W] : 0.f;
+    r3.qy1 = yl ? Q[1][i + W] : 0.f;
+    r3.qy5 = yl ? Q[5][i + W] : 0.f;
+    r3.qz4 = zl ? Q[4][i + WH] : 0.f;
+    r3.qz5 = zl ? Q[5][i + WH] : 0.f;
+    r3.qz2 = zl ? Q[2][i + WH] : 0.f;
+    float avb[3];
+    r3_avb(a, r3, avb);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) va[c] = r1_va(a, a.A.v[c][i], avb[c]);
+}
+
+// The fields a tile thread reads at plane z, prefetched into L2 one plane ahead.
+__device__ __forceinline__ void fused_prefetch(const AdjArgs& a, uint32_t j) {
+    prefetch_l2(a.A.u + j);
+    prefetch_l2(a.S.u + j);
+    prefetch_l2(a.f + j);
+    prefetch_l2(a.grad_f + j);
+    prefetch_l2(a.S.ubar + j);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        prefetch_l2(a.A.v[c] + j);
+        prefetch_l2(a.A.p[c] + j);
+        prefetch_l2(a.S1.p[c] + j);
+        prefetch_l2(a.S.vbar[c] + j);
+        prefetch_l2(a.S.p[c] + j);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        prefetch_l2(a.A.q[k] + j);
+        prefetch_l2(a.S.q[k] + j);
+    }
+}
+
+__global__ void __launch_bounds__(fz::NTHREADS, 2) adjoint_fused(AdjArgs a) {
+    __shared__ float s_ut[fz::RING][fz::SY][fz::SX];     // a(u~) at (tx, ty), tx, ty >= 0
+    __shared__ float s_va[fz::RING][3][fz::SY][fz::SX];  // a(v') at (tx + 1, ty + 1)
+    const int w = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    fz::Role role;
+    int tx = lane, ty = w;
+    if (w < fz::TY) {
+        role = fz::TILE;
+    } else if (w == fz::TY) {
+        role = fz::RIM_U;
+        ty = fz::TY;
+    } else if (w == fz::TY + 1) {
+        role = fz::RIM_V;
+        ty = -1;
+    } else if (lane < fz::TY) {
+        role = fz::RIM_U;
+        tx = fz::TX;
+        ty = lane;
+    } else if (lane < 2 * fz::TY) {
+        role = fz::RIM_V;
+        tx = -1;
+        ty = lane - fz::TY;
+    } else {
+        role = fz::IDLE;
+        tx = 0;
+        ty = 0;
+    }
+    const int W = a.W, H = a.H, D = a.D;
+    const int x = (int)blockIdx.x * fz::TX + tx, y = (int)blockIdx.y * fz::TY + ty;
+    const int z0 = (int)blockIdx.z * a.zc, z1 = min(D, z0 + a.zc);
+    const bool inside = role != fz::IDLE && x >= 0 && x < W && y >= 0 && y < H;
+    const bool tile = role == fz::TILE && inside;
+    const bool xl = x + 1 < W, yl = y + 1 < H, xf = x > 0, yf = y > 0;
+    const uint32_t WH = (uint32_t)a.WH, n = WH * (uint32_t)D;
+    // the voxel (x, y) of plane z (meaningful where `inside`)
+    auto at = [&](int z) {
+        return ((uint32_t)z * (uint32_t)H + (uint32_t)y) * (uint32_t)W + (uint32_t)x;
+    };
+    float glam = 0.f, ga0 = 0.f, ga1 = 0.f;
+    float va_m1[3] = {0.f, 0.f, 0.f}, va_m2[3] = {0.f, 0.f, 0.f};  // a(v') at s - 1, s - 2
+    if (tile && z0 - 1 >= 0 && TGV_IN_BOUNDS(at(z0 - 1), n, 44)) fused_prefetch(a, at(z0 - 1));
+    if (tile && TGV_IN_BOUNDS(at(z0), n, 44)) fused_prefetch(a, at(z0));
+    for (int s = z0 - 1; s <= z1; ++s) {
+        const int slot = (s - z0 + 1) % fz::RING;
+        float ut_s = 0.f, va_s[3] = {0.f, 0.f, 0.f};  // a(u~), a(v') at (x, y, s)
+        if (tile && s + 1 <= z1 && s + 1 < D && TGV_IN_BOUNDS(at(s + 1), n, 44))
+            fused_prefetch(a, at(s + 1));
+        if (s >= 0 && s < D) {
+            const uint32_t i = at(s);
+            const bool zl = s + 1 < D, zf = s > 0;
+            const bool own = s >= z0 && s < z1;
+            if (role == fz::TILE) {
+                if (inside && TGV_IN_BOUNDS(i, n, 40)) {
+                    if (own) {
+                        // R3 of iteration k and R1 of iteration k - 1, stored to Ao; every
+                        // load comes before the first store
+                        R3In r3;
+                        r3_load(a, i, xf, yf, xl, yl, r3);
+                        r3.pz = zf ? a.A.p[2][i - WH] : 0.f;
+                        r3.qz4 = zl ? a.A.q[4][i + WH] : 0.f;
+                        r3.qz5 = zl ? a.A.q[5][i + WH] : 0.f;
+                        r3.qz2 = zl ? a.A.q[2][i + WH] : 0.f;
+                        R1In r1;
+                        r1_load(a, i, xf, yf, r1);
+                        r1.pz = zf ? a.S1.p[2][i - WH] : 0.f;
+                        const float au_in = a.A.u[i];
+                        float av_in[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) av_in[c] = a.A.v[c][i];
+                        const float gf_in = a.grad_f[i];
+                        float aub, avb[3];
+                        r3_vals(a, xl, yl, zl, r3, aub, avb);
+                        const R1U o = r1_u(a, r1, au_in, aub);
+                        ut_s = o.uta;
+                        glam += o.glam;
+                        float av_out[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            va_s[c] = r1_va(a, av_in[c], avb[c]);
+                            av_out[c] = r1_av(a, va_s[c], avb[c]);
+                        }
+                        a.Ao.u[i] = o.au;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) a.Ao.v[c][i] = av_out[c];
+                        if (o.gf != 0.f) a.grad_f[i] = gf_in + o.gf;
+                    } else if (s < z0) {
+                        fused_va(a, i, xl, yl, zl, va_s);  // the plane below the chunk
+                    } else {
+                        ut_s = fused_uta(a, i, xf, yf, zf, xl, yl, zl);  // the plane above
+                    }
+                }
+                s_ut[slot][ty][tx] = ut_s;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) s_va[slot][c][ty + 1][tx + 1] = va_s[c];
+            } else if (role == fz::RIM_U && own) {
+                float u = 0.f;
+                if (inside && TGV_IN_BOUNDS(i, n, 41)) u = fused_uta(a, i, xf, yf, zf, xl, yl, zl);
+                s_ut[slot][ty][tx] = u;
+            } else if (role == fz::RIM_V && own) {
+                float v[3] = {0.f, 0.f, 0.f};
+                if (inside && TGV_IN_BOUNDS(i, n, 42)) fused_va(a, i, xl, yl, zl, v);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) s_va[slot][c][ty + 1][tx + 1] = v[c];
+            }
+        }
+        // R2 of iteration k - 1 on plane t = s - 1: its global loads before the plane
+        // barrier, its a(u~), a(v') neighbours from the ring after it
+        const int t = s - 1;
+        const bool r2 = tile && t >= z0 && t < z1 && TGV_IN_BOUNDS(at(t), n, 43);
+        const bool zl = t + 1 < D, zf = t > 0;
+        R2In L;
+        R2Pw P;
+        if (r2) {
+            const uint32_t i = at(t);
+            L.u0 = a.S.ubar[i];
+            L.ubx = xl ? a.S.ubar[i + 1] : 0.f;
+            L.uby = yl ? a.S.ubar[i + W] : 0.f;
+            L.ubz = zl ? a.S.ubar[i + WH] : 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                L.vb0[c] = a.S.vbar[c][i];
+                L.vbx[c] = xf ? a.S.vbar[c][i - 1] : 0.f;
+                L.vby[c] = yf ? a.S.vbar[c][i - W] : 0.f;
+                L.vbz[c] = zf ? a.S.vbar[c][i - WH] : 0.f;
+            }
+            r2_pw_load(a, i, P);
+        }
+        __syncthreads();
+        if (r2) {
+            const int ts = (t - z0 + 1) % fz::RING;
+            L.ut0 = s_ut[ts][ty][tx];
+            L.utx = xl ? s_ut[ts][ty][tx + 1] : 0.f;
+            L.uty = yl ? s_ut[ts][ty + 1][tx] : 0.f;
+            L.utz = zl ? ut_s : 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                L.va0[c] = s_va[ts][c][ty + 1][tx + 1];
+                L.vax[c] = xf ? s_va[ts][c][ty + 1][tx] : 0.f;
+                L.vay[c] = yf ? s_va[ts][c][ty][tx + 1] : 0.f;
+                L.vaz[c] = zf ? va_m2[c] : 0.f;
+            }
+            r2_vals(a, at(t), P, xl, yl, zl, xf, yf, zf, L, ga0, ga1, a.Ao);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            va_m2[c] = va_m1[c];
+            va_m1[c] = va_s[c];
+        }
+    }
+    block_add(&a.gp[0], glam);
     block_add(&a.gp[1], ga0);
     block_add(&a.gp[2], ga1);
 }
@@ -494,14 +780,19 @@ uint64_t adjoint_bounds_take() {
 
 namespace {
 
-// Planes per thread: about (tiles x D) / (16 blocks per SM), between 1 and ZM_MAX.
-int zm_for(const TgvState& s) {
+int sm_count() {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
         cudaGetLastError();
         sms = 152;
     }
+    return sms;
+}
+
+// Planes per thread: about (tiles x D) / (16 blocks per SM), between 1 and ZM_MAX.
+int zm_for(const TgvState& s) {
+    const int sms = sm_count();
     const long long tiles = (long long)ceil_div(s.W, BX) * ceil_div(s.H, BY);
     const long long zm = tiles * s.D / (16LL * sms);
     return (int)std::max(1LL, std::min<long long>(ZM_MAX, zm));
@@ -533,8 +824,9 @@ void tgv_full_state_zero(const TgvFullDev& s, size_t n, cudaStream_t st) {
 }
 
 void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* states,
-                         int len, const TgvFullDev& A, float* uta, float* const* va,
-                         float* grad_f, double* gp, cudaStream_t st) {
+                         int len, AdjointPasses passes, TgvFullDev& A, TgvFullDev& A2,
+                         float* uta, float* const* va, float* grad_f, double* gp,
+                         cudaStream_t st) {
     AdjArgs a;
     a.W = s.W;
     a.H = s.H;
@@ -542,6 +834,7 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
     a.WH = (size_t)s.W * s.H;
     a.f = s.f;
     a.A = A;
+    a.Ao = A2;
     a.uta = uta;
     for (int c = 0; c < 3; ++c) a.va[c] = va[c];
     a.grad_f = grad_f;
@@ -558,29 +851,45 @@ void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* 
     const dim3 grid(ceil_div(s.W, BX), ceil_div(s.H, BY), s.D);
     a.zm = zm_for(s);
     const dim3 zgrid(ceil_div(s.W, BX), ceil_div(s.H, BY), ceil_div(s.D, a.zm));
+    // the fused pass's z-chunk: the iteration kernels' (same tile, two blocks per SM)
+    a.zc = s.zchunk > 0 ? std::min(s.zchunk, s.D) : s.D;
+    const dim3 fgrid(ceil_div(s.W, fz::TX), ceil_div(s.H, fz::TY), ceil_div(s.D, a.zc));
+    // the fused pass indexes voxels in 32 bits
+    const size_t fblocks = (size_t)fgrid.x * fgrid.y * fgrid.z;
+    const bool fused = a.WH * (size_t)s.D < (size_t(1) << 32) &&
+                       (passes == ADJ_FUSED ||
+                        (passes == ADJ_FUSED_LARGE && fblocks >= 3 * 2 * (size_t)sm_count()));
     // R3.R1 block rows: the widest of 256, 128, 32 voxels that W fills
     const int tbx = s.W >= 256 ? 256 : (s.W >= 128 ? 128 : 32);
     const dim3 rblock(tbx, BX * BY / tbx, 1);
     const dim3 rgrid(ceil_div(s.W, tbx), ceil_div(s.H, BX * BY / tbx), s.D);
+    auto r2 = [&] {
+        if (a.zm > 1) adjoint_r2_zm<<<zgrid, block, 0, st>>>(a);
+        else adjoint_r2<<<grid, block, 0, st>>>(a);
+    };
     // iteration j of the segment maps states[j] -> states[j + 1]
     a.S = states[len - 1];
     a.S1 = states[len];
     adjoint_r1<<<grid, block, 0, st>>>(a);
-    for (int j = len - 1; j >= 0; --j) {
-        a.S = states[j];
-        a.S1 = states[j + 1];
-        if (a.zm > 1) adjoint_r2_zm<<<zgrid, block, 0, st>>>(a);
-        else adjoint_r2<<<grid, block, 0, st>>>(a);
-        if (j > 0) {
-            a.S = states[j - 1];
-            a.S1 = states[j];
+    r2();
+    for (int j = len - 1; j > 0; --j) {
+        a.S = states[j - 1];
+        a.S1 = states[j];
+        if (fused) {
+            // R3 of iteration j, R1 and R2 of iteration j - 1, from A into A2
+            a.A = A;
+            a.Ao = A2;
+            adjoint_fused<<<fgrid, fz::NTHREADS, 0, st>>>(a);
+            std::swap(A, A2);
+            a.A = A;
+        } else {
             if (tbx == 256) adjoint_r3r1<256><<<rgrid, rblock, 0, st>>>(a);
             else if (tbx == 128) adjoint_r3r1<128><<<rgrid, rblock, 0, st>>>(a);
             else adjoint_r3r1<32><<<rgrid, rblock, 0, st>>>(a);
-        } else {
-            adjoint_r3<<<grid, block, 0, st>>>(a);
+            r2();
         }
     }
+    adjoint_r3<<<grid, block, 0, st>>>(a);
     TGV_CHECK_LAUNCH();
 }
 

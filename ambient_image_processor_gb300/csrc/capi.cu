@@ -71,6 +71,7 @@ struct tgvdct_context {
         const void *ckpt = nullptr, *seg = nullptr, *adj = nullptr;
         uint32_t every = 0, K = 0, count = 0;
         int zchunk = 0;
+        int passes = 0;  // AdjointPasses
         TgvStep step{};
     } bwd_key;
 };
@@ -1297,12 +1298,28 @@ tgvdct_status tgvdct_tgv2_forward_checkpointed_dev(tgvdct_context* c, const floa
 }
 
 namespace {
+// The reverse sweep's passes for the context's iteration kernel: the fused adjoint pass
+// (R3 of one iteration with R1 and R2 of the one before) for shifted passes, and for
+// the automatic choice when its grid fills the GPU; separate passes otherwise.
+AdjointPasses adjoint_passes(const tgvdct_params& p) {
+    switch (p.iteration_kernel) {
+        case TGVDCT_KERNEL_FUSED_SHIFTED: return ADJ_FUSED;
+        case TGVDCT_KERNEL_AUTO: return ADJ_FUSED_LARGE;
+        default: return ADJ_SEPARATE;
+    }
+}
+
 // The reverse sweep over every segment, last to first, then the u_0 = ubar_0 = f term.
-void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A, float* uta,
-                       float* const* va, float* grad_f, double* gp, cudaStream_t s) {
+// The fused adjoint passes alternate between the adjoint states A and A2 (each segment
+// swaps the descriptors as it goes); the sweep's result is in whichever one the last
+// segment left current, which is the same one on every replay of a captured sweep.
+void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A0,
+                       const TgvFullDev& A20, float* uta, float* const* va, float* grad_f,
+                       double* gp, cudaStream_t s) {
     NvtxRange range("tgvdct reverse sweep");
     const size_t n = voxels(c->prm);
     const uint32_t every = c->ckpt_every, K = c->ckpt_K;
+    TgvFullDev A = A0, A2 = A20;
     std::vector<TgvFullDev> states(every + 1);
     for (int seg = (int)c->ckpt_count - 1; seg >= 0; --seg) {
         const uint32_t k0 = (uint32_t)seg * every, k1 = k0 + every < K ? k0 + every : K;
@@ -1312,7 +1329,8 @@ void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A,
         states[len] = full_state_at(c->ckpt_block, seg + 1, n);
         for (int j = 0; j + 1 < len; ++j)
             tgv_step_fp32(c->st, k, states[j], states[j + 1], c->step_cache, s);
-        tgv_adjoint_segment(c->st, k, states.data(), len, A, uta, va, grad_f, gp, s);
+        tgv_adjoint_segment(c->st, k, states.data(), len, adjoint_passes(c->prm), A, A2, uta,
+                            va, grad_f, gp, s);
     }
     tgv_adjoint_finish(grad_f, A, n, s);
 }
@@ -1323,7 +1341,8 @@ void backward_segments(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A,
 // caller then runs the sweep directly.  The iteration kernel's shared-memory
 // attribute was set by the checkpointed forward that every backward follows.
 cudaGraphExec_t backward_graph(tgvdct_context* c, const TgvStep& k, const TgvFullDev& A,
-                               float* uta, float* const* va, float* grad_f, double* gp) {
+                               const TgvFullDev& A2, float* uta, float* const* va,
+                               float* grad_f, double* gp) {
     tgvdct_context::BwdKey key;
     key.ckpt = c->ckpt_block;
     key.seg = c->seg_block;
@@ -1333,10 +1352,11 @@ cudaGraphExec_t backward_graph(tgvdct_context* c, const TgvStep& k, const TgvFul
     key.count = c->ckpt_count;
     key.zchunk = c->st.zchunk;
     key.step = k;
+    key.passes = adjoint_passes(c->prm);
     const auto& o = c->bwd_key;
     if (c->bwd_graph && o.ckpt == key.ckpt && o.seg == key.seg && o.adj == key.adj &&
         o.every == key.every && o.K == key.K && o.count == key.count && o.zchunk == key.zchunk &&
-        same_step(o.step, k))
+        o.passes == key.passes && same_step(o.step, k))
         return c->bwd_graph;
     if (c->bwd_graph) {
         cudaGraphExecDestroy(c->bwd_graph);
@@ -1354,7 +1374,7 @@ cudaGraphExec_t backward_graph(tgvdct_context* c, const TgvStep& k, const TgvFul
     cudaGraph_t g = nullptr;
     bool built = true;
     try {
-        backward_segments(c, k, A, uta, va, grad_f, gp, c->capture_stream);
+        backward_segments(c, k, A, A2, uta, va, grad_f, gp, c->capture_stream);
     } catch (...) {
         built = false;
     }
@@ -1393,13 +1413,15 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_de
         if (every > 1 &&
             ensure_block(&c->seg_block, &c->seg_bytes, (size_t)(every - 1) * tgv_full_state_bytes(n)))
             c->step_cache.reset();
-        // adjoint state, scratch a(u~) and a(v'), and the sweep's own d/df and
-        // d/d(lambda, alpha0, alpha1) (copied to the caller's buffers at the end, so a
-        // captured sweep does not depend on them)
+        // two adjoint states (the fused passes write from one into the other), scratch
+        // a(u~) and a(v'), and the sweep's own d/df and d/d(lambda, alpha0, alpha1)
+        // (copied to the caller's buffers at the end, so a captured sweep does not depend
+        // on them)
         const size_t field = (n * 4 + 255) & ~size_t(255);
-        ensure_block(&c->adj_block, &c->adj_bytes, tgv_full_state_bytes(n) + 5 * field + 256);
+        ensure_block(&c->adj_block, &c->adj_bytes, 2 * tgv_full_state_bytes(n) + 5 * field + 256);
         TgvFullDev A = full_state_at(c->adj_block, 0, n);
-        char* scratch = (char*)c->adj_block + tgv_full_state_bytes(n);
+        TgvFullDev A2 = full_state_at(c->adj_block, 1, n);
+        char* scratch = (char*)c->adj_block + 2 * tgv_full_state_bytes(n);
         float* uta = (float*)scratch;
         float* va[3] = {(float*)(scratch + field), (float*)(scratch + 2 * field),
                         (float*)(scratch + 3 * field)};
@@ -1413,10 +1435,10 @@ tgvdct_status tgvdct_tgv2_backward_dev(tgvdct_context* c, const float* grad_u_de
         TGV_CUDA(cudaMemsetAsync(gf, 0, n * 4, s));
         TGV_CUDA(cudaMemsetAsync(gp, 0, 3 * sizeof(double), s));
         const TgvStep k = step_of(c->prm);
-        if (cudaGraphExec_t g = backward_graph(c, k, A, uta, va, gf, gp))
+        if (cudaGraphExec_t g = backward_graph(c, k, A, A2, uta, va, gf, gp))
             TGV_CUDA(cudaGraphLaunch(g, s));
         else
-            backward_segments(c, k, A, uta, va, gf, gp, s);
+            backward_segments(c, k, A, A2, uta, va, gf, gp, s);
         TGV_CUDA(cudaMemcpyAsync(grad_f_dev, gf, n * 4, cudaMemcpyDeviceToDevice, s));
         TGV_CUDA(cudaMemcpyAsync(grad_params_dev, gp, 3 * sizeof(double), cudaMemcpyDeviceToDevice,
                                  s));

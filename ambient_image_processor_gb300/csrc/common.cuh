@@ -218,12 +218,20 @@ void tgv_save_state(const TgvState& s, const TgvFullDev& out, cudaStream_t st);
 void tgv_step_fp32(const TgvState& s, const TgvStep& k, const TgvFullDev& in,
                    const TgvFullDev& out, std::shared_ptr<void>& cache, cudaStream_t st);
 // Adjoint of the `len` iterations states[0] -> ... -> states[len] (len + 1 states):
+// How a segment's reverse passes run: R3.R1 and R2 as separate passes, or the fused pass
+// (R3 of one iteration with R1 and R2 of the one before) between them -- always, or
+// when its grid is at least three waves of two blocks per SM (below that the separate
+// one-voxel passes fill the GPU better: 96^3 ran 14.1 ms fused against 13.6 ms).
+enum AdjointPasses { ADJ_SEPARATE = 0, ADJ_FUSED_LARGE = 1, ADJ_FUSED = 2 };
 // A holds the adjoint of states[len] on entry and of states[0] on return; accumulates
 // d/df into grad_f and d/d(lambda, alpha0, alpha1) into gp[0..2]; uta and va are
-// scratch (1 + 3 fields).
+// scratch (1 + 3 fields).  A2 is a second adjoint state of the same layout: the fused
+// passes write from one into the other, and the two descriptors are swapped after
+// each, so that on return A names the one holding the result.
 void tgv_adjoint_segment(const TgvState& s, const TgvStep& k, const TgvFullDev* states,
-                         int len, const TgvFullDev& A, float* uta, float* const* va,
-                         float* grad_f, double* gp, cudaStream_t st);
+                         int len, AdjointPasses passes, TgvFullDev& A, TgvFullDev& A2,
+                         float* uta, float* const* va, float* grad_f, double* gp,
+                         cudaStream_t st);
 // grad_f += a(u_0) + a(ubar_0) (the loop starts from u = ubar = f).
 void tgv_adjoint_finish(float* grad_f, const TgvFullDev& A, size_t n, cudaStream_t st);
 

@@ -235,3 +235,46 @@ def test_backward_graph_replay_and_rebuild(gpu_lib):
             gf, gp = run(ctx, every)
             assert np.array_equal(gf, want[0])
             assert np.allclose(gp, want[1], rtol=1e-9, atol=0)
+
+
+def _gradient(f, K, every, data_term=pkg.DATA_L1, z_chunk=0, kernel=pkg.KERNEL_AUTO, seed=5):
+    """d/df and d/d(lambda, alpha0, alpha1) of <g, u> + <h, v> through the C ABI."""
+    import torch
+    d, h, w = f.shape
+    rng = np.random.default_rng(seed)
+    ft = torch.from_numpy(f).cuda()
+    g = [torch.from_numpy(rng.standard_normal(f.shape).astype(np.float32)).cuda()
+         for _ in range(4)]
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=K, data_term=data_term,
+                             z_chunk=z_chunk, iteration_kernel=kernel)
+    with pkg.Context(prm) as ctx:
+        u, vx, vy, vz, gf = (torch.empty_like(ft) for _ in range(5))
+        gp = torch.empty(3, dtype=torch.float64, device="cuda")
+        ctx.forward_checkpointed_dev(ft.data_ptr(), u.data_ptr(), vx.data_ptr(), vy.data_ptr(),
+                                     vz.data_ptr(), every)
+        ctx.backward_dev(*(x.data_ptr() for x in g), gf.data_ptr(), gp.data_ptr())
+        torch.cuda.synchronize()
+        ctx.check_device_error()
+        return gf.cpu().numpy(), gp.cpu().numpy()
+
+
+# (depth, height, width), z-chunk: edge tiles with idle columns and rows, single-plane
+# and two-plane volumes, several z-chunks per column of tiles (each with its first and
+# last plane made again by the neighbouring chunk), one plane per chunk
+@pytest.mark.parametrize("data_term", [pkg.DATA_L1, pkg.DATA_L2])
+@pytest.mark.parametrize("shape,z_chunk", [((9, 12, 20), 0), ((20, 24, 40), 3),
+                                           ((13, 17, 70), 5), ((1, 20, 24), 0),
+                                           ((2, 9, 33), 1), ((30, 33, 36), 7)])
+def test_fused_adjoint_passes_equal_separate_passes(gpu_lib, data_term, shape, z_chunk):
+    """With shifted passes as the iteration kernel the reverse sweep runs the fused
+    adjoint pass (R3 of one iteration, R1 and R2 of the one before) between a segment's
+    first and last iterations; with the two-pass kernels it runs R3.R1 and R2 as separate
+    passes, and with a checkpoint at every iteration no fused pass at all.  d/df must be
+    bit-identical; the parameter gradients are block sums accumulated in FP64 in launch
+    order, so they agree to rounding."""
+    f = np.log(tissue_phantom_3d(*shape, seed=16)).astype(np.float32)
+    ref = _gradient(f, 11, 11, data_term, z_chunk, pkg.KERNEL_TWO_PASS)
+    for every in (1, 2, 11):
+        got = _gradient(f, 11, every, data_term, z_chunk, pkg.KERNEL_FUSED_SHIFTED)
+        assert np.array_equal(got[0], ref[0])
+        assert np.allclose(got[1], ref[1], rtol=1e-5, atol=1e-7 * np.abs(ref[0]).sum())

@@ -92,16 +92,20 @@ def test_masked_and_downsampled_paths_stay_in_bounds(gpu_lib):
         assert np.array_equal(a, b, equal_nan=True) and np.isfinite(a).any()
 
 
-@pytest.mark.parametrize("shape", [(10, 12, 16), (40, 40, 40)])
-def test_reverse_mode_stays_in_bounds(gpu_lib, shape):
+@pytest.mark.parametrize("kernel", [pkg.KERNEL_AUTO, pkg.KERNEL_FUSED_SHIFTED])
+@pytest.mark.parametrize("shape", [(10, 12, 16), (40, 40, 40), (21, 19, 44)])
+def test_reverse_mode_stays_in_bounds(gpu_lib, shape, kernel):
     """The reverse sweep: one-voxel adjoint kernels at the small shape, the z-marching
-    projection pass at the larger one."""
+    projection pass at the larger ones; with shifted passes as the iteration kernel the
+    fused adjoint pass between them (edge tiles with idle rows and columns at 21 x 19 x
+    44)."""
     import torch
     Lc = pkg.lib_checked()
     d, h, w = shape
     f = torch.from_numpy(np.log(tissue_phantom_3d(*shape, seed=15))).cuda()
     gu = torch.ones_like(f)
-    p = pkg.default_params(width=w, height=h, depth=d, iteration_count=12)
+    p = pkg.default_params(width=w, height=h, depth=d, iteration_count=12,
+                           iteration_kernel=kernel)
     ctx = ctypes.c_void_p()
     assert Lc.tgvdct_create(ctypes.byref(p), ctypes.byref(ctx)) == pkg.OK
     try:
