@@ -101,7 +101,11 @@ typedef enum tgvdct_iteration_kernel {
        voxel-iteration moves 108 bytes (FP32 state, 3-D, depth >= 2, width a
        multiple of 4; masked runs too); one dual step before a run and one primal step
        after it (the two-pass kernels) convert the state.  Single iterations and the
-       cases it does not take run as TGVDCT_KERNEL_FUSED.  Same bits as the others. */
+       cases it does not take run as TGVDCT_KERNEL_FUSED.  Same bits as the others.
+       The reverse sweep (tgvdct_tgv2_backward_dev) runs its fused adjoint pass (R3 of
+       one iteration with R1 and R2 of the one before) with this kernel always, with
+       TGVDCT_KERNEL_AUTO for volumes large enough to fill the GPU three times over,
+       and separate adjoint passes otherwise; the gradients are the same bits. */
     TGVDCT_KERNEL_FUSED_SHIFTED = 4
 } tgvdct_iteration_kernel;
 
