@@ -46,6 +46,7 @@ ALGO_BYTES = {0: 140, 1: 104, 2: 104}
 # chip: read f, u, v3, p3, q6, write u, v3, p3, q6 (p, q in the dual element size)
 ALGO_BYTES_SHIFTED = {0: 108, 1: 72, 2: 72}
 KERNELS = {"shifted": 4, "fused": 2, "two_pass": 1}
+ADJOINT_KERNELS = {"auto": 0, "two_pass": 1, "shifted": 4}
 # the kernel a roofline line times, per --kernel
 KERNEL_NAMES = {"shifted": "tgv_shifted_tma_kernel", "fused": "tgv_fused_tma_kernel",
                 "two_pass": "tgv_dual_kernel + tgv_primal_kernel"}
@@ -410,14 +411,17 @@ def time_masked(pkg, torch, stream):
             "ms": ms, "voxel_iters_per_s": w * h * d * 1500 / (ms * 1e-3)}
 
 
-def time_adjoint(pkg, torch, stream, shape=(96, 96, 96), K=200, every=20):
+def time_adjoint(pkg, torch, stream, shape=(96, 96, 96), K=200, every=20, kernel=0):
     """Backward over forward time of the checkpointed reverse mode (default: 96^3,
-    K = 200, checkpoints every 20)."""
+    K = 200, checkpoints every 20).  `kernel` is the context's iteration kernel, which
+    also picks the reverse sweep's passes (0, automatic: the fused adjoint pass for
+    large volumes; 4, shifted passes: the fused adjoint pass always)."""
     from ambient_image_processor_gb300.phantoms import tissue_phantom_3d
     d, h, w = shape
     f = torch.from_numpy(tissue_phantom_3d(d, h, w, bias=False, noise=0.05, rician=False,
                                            seed=4)).cuda()
-    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=K)
+    prm = pkg.default_params(width=w, height=h, depth=d, iteration_count=K,
+                             iteration_kernel=kernel)
     u, vx, vy, vz, gu, gf = (torch.empty_like(f) for _ in range(6))
     gu.normal_()
     gp = torch.empty(3, dtype=torch.float64, device=f.device)
@@ -565,11 +569,12 @@ def run_ours(args):
                 extra["iteration_variants"] = var
             if "dct_poisson_256cube" in want:
                 extra["dct_poisson_256cube"] = time_dct_poisson(pkg, torch, stream)
+            akern = ADJOINT_KERNELS[args.adjoint_kernel]
             if "adjoint" in want:
-                extra["adjoint"] = time_adjoint(pkg, torch, stream)
+                extra["adjoint"] = time_adjoint(pkg, torch, stream, kernel=akern)
             if "adjoint_256x256x192" in want:
                 extra["adjoint_256x256x192"] = time_adjoint(pkg, torch, stream, (192, 256, 256),
-                                                            K=100, every=20)
+                                                            K=100, every=20, kernel=akern)
             if "other_configs" in want:
                 extra["other_configs"] = time_other_configs(pkg, torch, stream)
             if "downsampled_deshade" in want:
@@ -709,6 +714,9 @@ def main():
     ap.add_argument("--eigen", type=int, default=1, choices=[0, 1])
     ap.add_argument("--dct", default="bf16x3", choices=sorted(DCT_MODES))
     ap.add_argument("--kernel", default="shifted", choices=sorted(KERNELS))
+    ap.add_argument("--adjoint-kernel", default="auto", choices=sorted(ADJOINT_KERNELS),
+                    help="iteration kernel of the adjoint extras (it picks the reverse "
+                         "sweep's passes: shifted forces the fused adjoint pass)")
     ap.add_argument("--z-chunk", type=int, default=0)
     ap.add_argument("--iterations", type=int, default=0, help="override the iteration count")
     ap.add_argument("--profile-iterations", type=int, default=200)
