@@ -139,7 +139,7 @@ def _loop_state(kernel, f, steps, **kw):
         for n in steps:
             assert L.tgvdct_tgv2_step_dev(ctx._ctx, n, None) == pkg.OK
             launches.append(ctx.loop_launches())
-        buf = torch.empty(ctx.state_bytes() // 4 + 1, dtype=torch.float32, device="cuda")
+        buf = torch.zeros((ctx.state_bytes() + 3) // 4, dtype=torch.float32, device="cuda")
         ctx.save_state_dev(buf.data_ptr())
         torch.cuda.synchronize()
         ctx.check_device_error()

@@ -75,7 +75,7 @@ def test_shifted_pass_wait_runs_out_and_the_context_recovers(gpu_lib):
         assert ctx.loop_launches() == 6
 
     def snapshot(ctx):
-        buf = torch.empty(ctx.state_bytes() // 4 + 1, dtype=torch.float32, device="cuda")
+        buf = torch.zeros((ctx.state_bytes() + 3) // 4, dtype=torch.float32, device="cuda")
         ctx.save_state_dev(buf.data_ptr())
         torch.cuda.synchronize()
         return buf
