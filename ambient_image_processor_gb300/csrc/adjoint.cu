@@ -19,8 +19,10 @@
 // (B_a^T g)[j] = g[j+e] (j_a < N-1) - g[j].  R3 of iteration k and R1 of iteration
 // k-1 are pointwise in a(ubar), a(vbar), so inside a segment they run as one kernel
 // (adjoint_r3r1) and those four fields never reach memory: per voxel and iteration
-// the adjoint moves 63 fields (252 bytes).  An FP64 restatement of the same algebra
-// in the oracle gives the reference gradient (central differences pin it).
+// the adjoint moves 63 fields (252 bytes).  For large volumes R2 of iteration k-1 joins
+// them (adjoint_fused), so that a(u~) and a(v') stay on chip as well: 44 fields
+// (176 bytes).  An FP64 restatement of the same algebra in the oracle gives the
+// reference gradient (central differences pin it).
 #include <algorithm>
 
 #include "common.cuh"
