@@ -75,3 +75,16 @@ def test_unknown_extras_are_refused_before_device_work(monkeypatch, capsys):
         bench.main()
     assert e.value.code == 2
     assert "bogus" in capsys.readouterr().err
+
+
+def test_adjoint_kernel_names_map_to_iteration_kernels(monkeypatch, capsys):
+    """--adjoint-kernel picks the context's iteration kernel for the adjoint extras (it
+    also picks the reverse sweep's passes); an unknown name stops at argument parsing."""
+    import ambient_image_processor_gb300 as pkg
+    assert bench.ADJOINT_KERNELS == {"auto": pkg.KERNEL_AUTO, "two_pass": pkg.KERNEL_TWO_PASS,
+                                     "shifted": pkg.KERNEL_FUSED_SHIFTED}
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--adjoint-kernel", "fused_register"])
+    with pytest.raises(SystemExit) as e:
+        bench.main()
+    assert e.value.code == 2
+    assert "adjoint-kernel" in capsys.readouterr().err
