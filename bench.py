@@ -635,7 +635,8 @@ def run_ours(args):
 ACCURACY_FORMS = [("fp32", 0, "fp32", 0), ("fp32", 0, "fp32", 1), ("fp32", 0, "bf16x3", 1),
                   ("fp32", 0, "tf32", 1), ("fx16_dual", 2, "fp32", 1), ("bf16_dual", 1, "fp32", 1),
                   ("fx16_dual", 2, "bf16x3", 1)]
-# the benchmark spec's bound on the relative L2 error of the corrected image and the shading
+# the target bound on the relative L2 error (against FP64) of the corrected image and the
+# shading field for a mixed-precision form
 ACCURACY_TOL = 1e-4
 
 
